@@ -1,0 +1,356 @@
+#!/usr/bin/env python3
+"""Benchmark: time-to-solution of one 256^3 snapshot with 642 direction vertices.
+
+Workload ("blobs256_masked_select"): a 256^3 grid, 8 seeded Gaussian pressure blobs
+(sigma ~ U[8, 24] cells, amplitude ~ N(0, 1)), 5 % gradient noise, a spherical obstacle of
+radius 40 cells at the centre masked out, the selected method with a threshold above every
+curl value (lines split only at the mask), the 642-vertex icosphere (321 axes, the
+reference's GridIcosahedronDivide4.dat), line spacing 1.  One step = one complete solve of
+the snapshot: K iterations of the reference iteration (K = the iterations after which the
+mean-gauged p is within 1e-3 relative L2 of the converged solution, found by a calibration
+solve and reported), then normalisation.  The geometry (line tracing + walk) depends only
+on the grid and direction set, is built once per context, and is reported separately.
+
+value   device time per solve, inputs resident in HBM (seconds, lower is better)
+e2e     the same solve through the C ABI with pinned host buffers: H2D of the gradient
+        and mask, D2H of p and count inside the timed region
+The inputs (268 MB field + 67 MB mask, > L2) are rewritten every step, so no step starts
+from a warm L2.
+
+--impl reference times the reference's own CPU functions (oracle/_ref, or the oracle
+restatement when the reference sources are not staged) on a bounded sample: one sweep of
+a subset of the directions at the same 256^3 workload with every host thread, scaled to K
+full sweeps.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "parallel-3d-pressure-reconstruction_gb300")
+for _p in (PKG, os.path.join(REPO, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "time-to-solution at 256³ to 1e-3 rel L2 vs FP64; voxel·dir updates/s; HBM GB/s"
+FLT_MAX = float(np.finfo(np.float32).max)
+# bytes per voxel-direction update of the full sweep (selected method): the gradient
+# component read (3 x 4 B), the curl read (4 B) and the accumulator read + write (8 B)
+ALG_BYTES_PER_UNIT = {"f32": 24.0, "bf16": 18.0}
+
+
+def workload(args, rank=0):
+    from omni3d import synthetic
+
+    n = args.n
+    f = synthetic.blobs(n=n, count=8, sigma_range=(8.0, 24.0), noise=0.05, seed=rank, spacing=1e-3,
+                        sphere_radius=40.0 * n / 256.0)
+    return f
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            p = [x.strip() for x in l.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_reference_sample(args, f, dirs, n_sample_dirs=None):
+    """One sweep of evenly spaced directions with the reference's own functions (or the
+    oracle restatement), every host thread.  Returns (units/s, seconds, units, kind, threads, ndirs)."""
+    import oracle
+
+    nthreads = os.cpu_count() or 1
+    kind = "reference"
+    try:
+        path = oracle.build_ref()
+    except Exception:
+        path = None
+    nd = n_sample_dirs or nthreads
+    idx = np.linspace(0, len(dirs) - 1, nd).round().astype(int)
+    sub = np.ascontiguousarray(dirs[idx])
+    V = int(np.prod(f["dims"]))
+    p0 = np.zeros(V, np.float32)
+    curl = oracle.Oracle().curl(f["dims"], f["spacing"], f["ax"], f["ay"], f["az"], f["mask"])
+    if path is not None:
+        R = oracle.RefLib(path)
+        t0 = time.perf_counter()
+        pn, cnt, units = R.sweep(f["dims"], f["spacing"], sub, f["ax"], f["ay"], f["az"], p0, mode=1, thr=FLT_MAX,
+                                 curl=curl, nthreads=min(nthreads, nd))
+        dt = time.perf_counter() - t0
+    else:
+        kind = "port"
+        O = oracle.Oracle()
+        t0 = time.perf_counter()
+        pn, cnt = O.sweep(f["dims"], f["spacing"], sub, f["ax"], f["ay"], f["az"], p0, mode=1, thr=FLT_MAX,
+                          curl=curl, nthreads=min(nthreads, nd))
+        dt = time.perf_counter() - t0
+        units = int(cnt.astype(np.float64).sum())  # weights are not unit counts; a close proxy
+    return units / dt, dt, units, kind, min(nthreads, nd), nd
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    try:
+        f = workload(args)
+        dirs = icosphere_numpy(args.level)
+        ups, dt, units, kind, threads, nd = cpu_reference_sample(args, f, dirs)
+        sweep_s = dt * len(dirs) / nd
+        value = args.iters * sweep_s
+        line = {
+            "metric": METRIC, "impl": "reference", "value": value, "unit": "s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config_dict(args),
+            "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": kind,
+                             "sample": "one sweep of %d of %d directions (every host thread), scaled to %d sweeps"
+                                       % (nd, len(dirs), args.iters),
+                             "units_per_s": ups},
+            "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+    except Exception as e:
+        line = {"impl": "reference", "unavailable": "reference CPU path failed: %s" % e}
+    print(json.dumps(line))
+    return 0
+
+
+def icosphere_numpy(level):
+    import omni3d
+
+    return omni3d.icosphere(level)
+
+
+def config_dict(args):
+    return {"workload": "blobs%d_masked_select" % args.n, "grid": [args.n] * 3, "direction_vertices": 642
+            if args.level == 4 else None, "icosphere_level": args.level, "line_spacing": 1.0, "method": "select",
+            "threshold": "above every curl (split at the mask only)", "sphere_radius_cells": 40.0 * args.n / 256,
+            "noise": 0.05, "iterations": args.iters, "grad_storage": args.grad, "solver": args.solver,
+            "l2_between_steps": "inputs (335 MB) rewritten each step, larger than L2"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--level", type=int, default=4)
+    ap.add_argument("--iters", type=int, default=0, help="iterations per solve (0: calibrate)")
+    ap.add_argument("--grad", default="f32", choices=["f32", "bf16"])
+    ap.add_argument("--solver", default="anchor", choices=["anchor", "sweep"])
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.iters <= 0:
+        args.iters = DEFAULT_ITERS.get((args.n, args.level), 12)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    import omni3d
+    from omni3d import synthetic
+
+    omni3d.build()
+    f = workload(args, rank)
+    dims = f["dims"]
+    V = int(np.prod(dims))
+    dirs = omni3d.icosphere(args.level)
+    dev = torch.device("cuda", local)
+
+    def make(iters, tol=0.0):
+        return omni3d.Omni3D(dims, f["spacing"], dirs, max_iter=iters, method="select", threshold=FLT_MAX,
+                             solver=args.solver, grad=args.grad, tol=tol, gauge="mean", device=local)
+
+    # device inputs
+    d_in = [torch.from_numpy(f[k].reshape(-1)).to(dev) for k in ("ax", "ay", "az", "mask")]
+    # calibration: converged reference solution and the error after K iterations
+    t0 = time.time()
+    with make(200, tol=1e-7) as s:
+        ref = s.solve(*d_in[:3], mask=d_in[3])
+        p_conv = ref.p.clone()
+        conv_its = ref.stats["iterations"]
+    sel = ref.count.reshape(-1) > 0
+    solver = make(args.iters)
+    stream = torch.cuda.Stream(device=dev)
+    solver.set_stream(stream.cuda_stream)
+    r = solver.solve(*d_in[:3], mask=d_in[3])
+    err_conv = synthetic.relative_l2(r.p.cpu().numpy(), p_conv.cpu().numpy(), gauge="mean",
+                                     weights=sel.cpu().numpy())
+    err_true = synthetic.relative_l2(r.p.cpu().numpy(), f["p_true"], gauge="mean",
+                                     weights=(sel.cpu().numpy() & (f["mask"].reshape(-1) > 0)))
+    geo = solver.geometry_info()
+    calib_s = time.time() - t0
+
+    # fresh input buffers rewritten each step (defeats L2 reuse across steps)
+    src = [t.clone() for t in d_in]
+
+    def one_step():
+        for t, s_ in zip(d_in, src):
+            t.copy_(s_)
+        return solver.solve(*d_in[:3], mask=d_in[3])
+
+    for _ in range(max(args.warmup, 0)):
+        one_step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    times, sweeps, stats = [], [], None
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            rr = solver.solve(*d_in[:3], mask=d_in[3])
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+            sweeps.append(rr.stats["ms_sweep"] / 1e3)
+            stats = rr.stats
+            for t, s_ in zip(d_in, src):  # rewrite inputs outside the timed region
+                t.copy_(s_)
+    torch.cuda.synchronize()
+    t_dev = float(np.mean(times))
+    if world > 1:
+        tt = torch.tensor([t_dev], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_dev = float(tt.item())
+
+    # end to end through the C ABI with pinned host buffers
+    h_in = [torch.from_numpy(f[k].reshape(-1).copy()).pin_memory() for k in ("ax", "ay", "az", "mask")]
+    h_np = [t.numpy() for t in h_in]
+    e2e_times = []
+    for it in range(max(1, args.warmup) + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = solver.solve(*h_np[:3], mask=h_np[3])
+        t1 = time.perf_counter()
+        if it >= max(1, args.warmup):
+            e2e_times.append(t1 - t0)
+    t_e2e = float(np.mean(e2e_times))
+    h2d = 4 * V * 4
+    d2h = 2 * V * 4
+
+    units = geo["n_units"]
+    t_sweep = float(np.mean(sweeps))
+    peak, peak_kind = measured_peak_hbm()
+    alg = ALG_BYTES_PER_UNIT[args.grad] * units
+    achieved = alg / t_sweep / 1e9
+
+    line = {
+        "metric": METRIC, "value": t_dev, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_dev * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded analytic blobs, a = -grad p / rho + 5% noise)",
+        "config": config_dict(args),
+        "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(stats["kernel_launches"]),
+        "roofline": {"bound": "hbm", "kernel": "k_sweep_select (final full sweep)", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "peak_source": peak_kind, "alg_bytes_per_unit": ALG_BYTES_PER_UNIT[args.grad],
+                     "units_per_launch": units, "sweep_ms": t_sweep * 1e3},
+        "updates_per_s": args.iters * units / t_dev,
+        "units_per_sweep": units, "n_lines": geo["n_lines"],
+        "accuracy": {"rel_l2_vs_converged": err_conv, "converged_iterations": conv_its,
+                     "rel_l2_vs_analytic": err_true, "target": 1e-3},
+        "breakdown_ms": {k: stats[k] for k in ("ms_setup", "ms_iterate", "ms_final", "ms_sweep", "ms_total")},
+        "geometry_ms": stats["ms_geometry"], "n_anchors": stats["n_anchors"], "n_links": stats["n_links"],
+        "calibration_s": calib_s,
+    }
+    line["clocks"] = clk.summary()
+    if rank == 0 and not args.no_cpu:
+        try:
+            ups, dt, cu, kind, threads, nd = cpu_reference_sample(args, f, dirs)
+            line["cpu_baseline"] = {"value": args.iters * dt * len(dirs) / nd, "unit": "s", "cores": threads,
+                                    "kind": kind, "units_per_s": ups,
+                                    "sample": "one sweep of %d of %d directions at the same workload, scaled to "
+                                              "%d sweeps" % (nd, len(dirs), args.iters)}
+        except Exception as e:
+            line["cpu_baseline"] = {"value": None, "unavailable": str(e)}
+    if rank == 0:
+        print(json.dumps(line))
+    solver.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+DEFAULT_ITERS = {(256, 4): 12}
+
+if __name__ == "__main__":
+    sys.exit(main())

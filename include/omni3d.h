@@ -1,0 +1,196 @@
+/*
+ * omni3d.h -- C ABI of the GB300 (sm_103a) omni-directional 3D pressure reconstruction.
+ *
+ * The reference program (Omni3D_8.0/Omni3D_8.0/kernel.cu, "K" below) is a monolithic
+ * executable with no library interface.  Each entry point here replaces one block of its
+ * main() or one of its kernels; the block is cited beside the declaration.
+ *
+ * Conventions
+ *   - Every function returns an int status: OMNI3D_OK (0) or a negative OMNI3D_ERR_*.
+ *     omni3d_last_error(ctx) (or omni3d_global_error() for calls without a context)
+ *     returns a text description of the last failure.
+ *   - Volumes are float32, x fastest: index = i + j*nx + k*nx*ny (the order of the
+ *     Tecplot rows the reference reads, K:8712-8792).
+ *   - Pointers are host pointers unless the call's `device_ptrs` argument is non-zero, in
+ *     which case they must be device pointers on the context's device.
+ *   - A context is not reentrant; separate contexts may run concurrently on separate
+ *     streams.
+ */
+#ifndef OMNI3D_H
+#define OMNI3D_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OMNI3D_OK 0
+#define OMNI3D_ERR_ARG (-1)      /* invalid argument */
+#define OMNI3D_ERR_CUDA (-2)     /* CUDA runtime error (text in last_error) */
+#define OMNI3D_ERR_IO (-3)       /* file missing, short or malformed */
+#define OMNI3D_ERR_NOMEM (-4)    /* device or host allocation failed */
+#define OMNI3D_ERR_STATE (-5)    /* call made in the wrong state */
+#define OMNI3D_ERR_RANGE (-6)    /* size beyond a stated limit */
+#define OMNI3D_ERR_NUMERIC (-7)  /* non-finite result or a line walk that failed */
+
+/* Integration method (Tutorial p.1 "Standard / Selected"). */
+#define OMNI3D_METHOD_PLAIN 0   /* bodyIntegralInner, K:1743-1863 */
+#define OMNI3D_METHOD_SELECT 1  /* bodyIntegralInnerSelect, K:2280-2537 (what main runs) */
+
+/* Solver form.  Both produce the reference iteration's result; they differ in cost. */
+#define OMNI3D_SOLVER_ANCHOR 0  /* iterate only the voxels whose values feed back (line
+                                   entries / segment starts), then one full sweep */
+#define OMNI3D_SOLVER_SWEEP 1   /* one full omni sweep per iteration, as K:8840-8861 */
+
+/* Storage of the gradient field on the device. */
+#define OMNI3D_GRAD_F32 0
+#define OMNI3D_GRAD_BF16 1
+
+/* Gauge applied to the output (the reference applies none; K:8879-8915 is commented out). */
+#define OMNI3D_GAUGE_NONE 0
+#define OMNI3D_GAUGE_POINT 1    /* p -= p(ref voxel) */
+#define OMNI3D_GAUGE_MEAN 2     /* p -= mean over voxels with count > 0 */
+
+typedef struct omni3d_ctx omni3d_ctx;
+
+/* Solver parameters.  The first block mirrors Parameter_Omni3D.dat (K:8541-8571). */
+typedef struct {
+    int nx, ny, nz;            /* grid after the ROI crop (lines 1-3, 16-21) */
+    float dx, dy, dz;          /* spacing (lines 4-6) */
+    float density;             /* rho (line 7) */
+    float line_spacing;        /* spacing of the parallel lines (line 9) */
+    int n_dirs;                /* number of direction vectors (line 10) */
+    const float *dirs;         /* host, n_dirs x 3 (k1,k2,k3), as read from the direction file */
+    int max_iter;              /* NoItr (line 14): iterations to run */
+    float threshold;           /* curl threshold of the selected method (line 15) */
+    int method;                /* OMNI3D_METHOD_* */
+    /* additions of this implementation */
+    int solver;                /* OMNI3D_SOLVER_* */
+    int grad_storage;          /* OMNI3D_GRAD_* */
+    double tol;                /* stop early when the gauged relative change of p falls below
+                                  tol (0: run exactly max_iter, as the reference does) */
+    int gauge;                 /* OMNI3D_GAUGE_* */
+    int ref_i, ref_j, ref_k;   /* reference voxel of OMNI3D_GAUGE_POINT */
+    int seed_first_iteration;  /* 1 (reference, K:8811): the first sweep accumulates on top of
+                                  p_init; 0: on top of zero */
+    int device;                /* CUDA device ordinal */
+} omni3d_params;
+
+typedef struct {
+    int iterations;            /* iterations performed (<= max_iter) */
+    double rel_change;         /* gauged relative change of the last iteration */
+    long long n_lines;         /* lines that cross the volume (all directions) */
+    long long n_units;         /* voxel-direction updates of one full sweep */
+    long long walk_errors;     /* lines whose walk hit the reference's wrong-point branch */
+    long long n_anchors;       /* anchor voxels (anchor solver) */
+    long long n_links;         /* anchor operator entries (anchor solver) */
+    double ms_geometry;        /* line tracing + walk (cached across solves) */
+    double ms_setup;           /* per-field setup: anchor operator or precomputed terms */
+    double ms_iterate;         /* iterations */
+    double ms_final;           /* final full sweep + normalisation */
+    double ms_total;           /* device time of the whole solve */
+    double ms_sweep;           /* device time of the final full sweep kernel alone */
+    long long kernel_launches; /* CUDA kernels this library launched during the call */
+} omni3d_stats;
+
+/* Fill *p with the reference's defaults (K:8512-8535) and this implementation's. */
+void omni3d_default_params(omni3d_params *p);
+
+/* Create a solver context: validates the parameters, uploads the direction table and
+ * traces the line geometry (the per-direction parallel-line generator of K:6153-6198 and
+ * the entry/exit search cross2point, K:663-1113) into device line descriptors.
+ * Replaces the setup of main(), K:8577-8672. */
+int omni3d_create(const omni3d_params *params, omni3d_ctx **out);
+int omni3d_destroy(omni3d_ctx *ctx);
+const char *omni3d_last_error(const omni3d_ctx *ctx);
+const char *omni3d_global_error(void);
+
+/* Use this CUDA stream (cudaStream_t passed as void*) for all later work on ctx. */
+int omni3d_set_stream(omni3d_ctx *ctx, void *stream);
+
+/* Solve one snapshot: the whole per-file block of main(), K:8794-8863 (initial state,
+ * NoItr x {omni sweep, devidecountInner}, read back p and count).
+ *   ax, ay, az   material acceleration Du/Dt, Dv/Dt, Dw/Dt (grad p = -rho a)
+ *   curl         |curl a| x mask (OMNI3D_METHOD_SELECT; NULL: computed on the device
+ *                from ax..az and mask), see omni3d_curl
+ *   mask         mask column of the input file (NULL: all ones); used only when curl is NULL
+ *   p_init       initial pressure (NULL: zero), e.g. omni3d_bernoulli_face()
+ *   p_out        pressure after the iterations (required)
+ *   count_out    per-voxel line count of the last iteration (K:8857; NULL: not returned)
+ *   stats        optional */
+int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float *az,
+                 const float *curl, const float *mask, const float *p_init, float *p_out,
+                 float *count_out, int device_ptrs, omni3d_stats *stats);
+
+/* One omni sweep from p without normalisation: pn += contributions, count += weights.
+ * The loop body of omni3dparallellinesESInner (K:6151-6215) / ...Select (K:6414-6480)
+ * over every (direction, lattice point) pair. */
+int omni3d_sweep(omni3d_ctx *ctx, const float *ax, const float *ay, const float *az,
+                 const float *curl, const float *p, float *pn, float *count, int device_ptrs);
+
+/* |curl a| x mask: calCurlofMaterialAccCPU, K:8352-8378 (GPU twin K:6863-6888). */
+int omni3d_curl(omni3d_ctx *ctx, const float *ax, const float *ay, const float *az,
+                const float *mask, float *curl_out, int device_ptrs);
+
+/* Lines and walk lengths of the traced geometry (diagnostics and tests). */
+int omni3d_geometry_info(omni3d_ctx *ctx, long long *n_lines, long long *n_units,
+                         long long *walk_errors);
+
+/* Copy the line table to host memory: per line {entry voxel, exit voxel, direction, steps}
+ * (4 x int32) in (direction, lattice point) order; n_max rows at most. */
+int omni3d_line_table(omni3d_ctx *ctx, int32_t *rows, long long n_max);
+
+/* Copy the staircase of line `line` (one axis code 0/1/2 per step) to host memory. */
+int omni3d_line_steps(omni3d_ctx *ctx, long long line, int8_t *axes, int cap);
+
+/* ---------------------------------------------------------------- host-side helpers */
+
+/* Direction set of an icosahedron subdivided `level` times (level 2: 42, 3: 162, 4: 642,
+ * 5: 2562, ... vertices), sorted and rounded to six decimals the way the reference's
+ * GridIcosahedronDivide<level>.dat files are.  Writes up to cap rows of (k1,k2,k3) into
+ * out and returns the vertex count (or a negative status). */
+int omni3d_icosphere(int level, float *out, int cap);
+
+/* Direction file (K:8615-8649): rows "k1 k2 k3", a trailing count row ignored.  Reads n
+ * rows into out (n x 3).  Returns the number of rows read or a negative status. */
+int omni3d_read_directions(const char *path, int n, float *out);
+
+/* Parameter_Omni3D.dat (K:8541-8571), including the hidden pref line and ROI lines. */
+typedef struct {
+    int nx_org, ny_org, nz_org;
+    float dx, dy, dz, density, scale, line_spacing;
+    int n_dirs;
+    char dir_file[1024], accel_dir[1024], pressure_dir[1024];
+    int n_iter;
+    float threshold, pref;
+    int roi[6];               /* i0, i1, j0, j1, k0, k1 (inclusive) */
+} omni3d_file_params;
+int omni3d_read_params(const char *path, omni3d_file_params *out);
+
+/* Tecplot ASCII acceleration file (K:8708-8792): 3 header lines, then rows
+ * "x y z u v w Du Dv Dw mask" (10 columns) or "x y z Du Dv Dw mask" (7 columns), i
+ * fastest, cropped to the ROI.  Any output pointer may be NULL.  Arrays hold
+ * (i1-i0+1)*(j1-j0+1)*(k1-k0+1) floats. */
+int omni3d_read_tecplot(const char *path, const omni3d_file_params *fp, float *x, float *y,
+                        float *z, float *u, float *v, float *w, float *ax, float *ay,
+                        float *az, float *mask);
+
+/* Initial pressure of K:8805-8811: pref - rho/2 |u|^2 on the j = 0 face, 0 elsewhere. */
+int omni3d_bernoulli_face(int nx, int ny, int nz, float pref, float density, const float *u,
+                          const float *v, const float *w, float *p_init);
+
+/* PressureOmni3D_%05d.dat writer (K:8916-8935): header lines and rows of
+ * "%15.9f %15.9f %15.9f %15.9f %15.9f" (x y z p count). */
+int omni3d_write_pressure(const char *path, int nx, int ny, int nz, const float *x,
+                          const float *y, const float *z, const float *p, const float *count);
+
+/* CurlofMaterialAcc_Sample.dat writer (K:8938-8958). */
+int omni3d_write_curl(const char *path, int nx, int ny, int nz, const float *x, const float *y,
+                      const float *z, const float *curl);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OMNI3D_H */

@@ -1,0 +1,658 @@
+/*
+ * CPU oracle for the Omni3D parallel-line omni-directional pressure integration.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is a plain-C restatement of the reference
+ * algorithm (Omni3D_8.0/Omni3D_8.0/kernel.cu, "K" below).  Only tests/,
+ * __graft_entry__.smoke() and bench.py's cpu_baseline / reference arm may load it,
+ * and only as the checker or the timed CPU baseline.  The product library never
+ * links or calls it.
+ *
+ * Parity pin: every function here is checked bit-for-bit against the reference's own
+ * functions (cross2point, bodyIntegralInner, bodyIntegralInnerSelect, calIndex,
+ * calCurlofMaterialAccCPU, omni3dparallellinesESInnerCPU + devidecountInnerCPU)
+ * compiled from the reference sources by oracle/build_ref.sh into oracle/_ref/.
+ *
+ * Arithmetic rules copied from the reference's C semantics (they decide which voxels a
+ * line visits, so they are reproduced exactly):
+ *   - all geometry is FP32 with every operation rounded separately (compile with
+ *     -ffp-contract=off, no -ffast-math);
+ *   - floor(f + 0.5) is evaluated in double ("0.5" is a double literal, K:703);
+ *   - the "zero" threshold 1e-7 is a double (K:23);
+ *   - the trapezoid increment is formed in double and added to a float accumulator
+ *     ("0.5" promotes the product, K:1816), i.e. pint = (float)((double)pint + term).
+ *
+ * Two accumulation precisions share one discrete geometry:
+ *   - "f32": the reference's float arithmetic reproduced exactly (sequential order);
+ *   - "f64": the same voxel paths, with every sum and weight in double.  This is the
+ *     FP64 oracle of the same discrete method.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ORC_ZERO 1e-7                               /* K:23 */
+#define ORC_PI 3.1415926535897932384626433832795    /* K:24 */
+
+/* ------------------------------------------------------------------------------------ */
+/* geometry                                                                               */
+/* ------------------------------------------------------------------------------------ */
+
+/* Number of lattice points per row.  GPU kernel form (K:6159-6167): largest dimension
+ * times 1.732 divided by the line spacing, in double, truncated.  The CPU twin (K:8286)
+ * omits the division by the spacing; geom_cpu_twin selects it. */
+int orc_nogrid(long X, long Y, long Z, float ls, int geom_cpu_twin)
+{
+    int ng = (int)X;
+    if (ng < Y) ng = (int)Y;
+    if (ng < Z) ng = (int)Z;
+    if (geom_cpu_twin) return (int)(ng * 1.732);
+    return (int)(ng * 1.732 / (double)ls);
+}
+
+/* Per-direction rotation coefficients (K:6178-6191 with libm sinf/cosf in place of the
+ * fast intrinsics, as the CPU twin K:8296-8302 does).  out = {cos th, sin th, cos ph,
+ * sin ph}.  With the pole guard (GPU form) sin th == 0 gives ph = 0; without it (CPU
+ * twin) the division by zero propagates NaN exactly as the reference's CPU path does. */
+void orc_dir_coeffs(float k1, float k2, float k3, int geom_cpu_twin, float out[4])
+{
+    float theta = acosf(k3);
+    float st = sinf(theta);
+    float phi = 0.0f;
+    if (geom_cpu_twin || st != 0.0f) {
+        phi = asinf(k2 / st);
+        if (k1 / st < 0) phi = (float)(-phi + ORC_PI);
+    }
+    out[0] = cosf(theta);
+    out[1] = st;
+    out[2] = cosf(phi);
+    out[3] = sinf(phi);
+}
+
+/* Line offset of lattice point `point` (K:6171-6194). */
+void orc_line_offset(int point, int ng, float ls, const float c[4], float xyz[3])
+{
+    float xp = (float)(((double)(float)(point / ng) - 0.5 * (ng - 1)) * (double)ls);
+    float yp = (float)(((double)(float)(point - point / ng * ng) - 0.5 * (ng - 1)) * (double)ls);
+    float t = xp * c[0];
+    xyz[0] = t * c[2] - yp * c[3];
+    xyz[1] = t * c[3] + yp * c[2];
+    xyz[2] = -xp * c[1];
+}
+
+static inline int rnd_half(float f) { return (int)floor((double)f + 0.5); }
+
+/* Entry / exit voxels of the line through (x,y,z) with direction k, following K:663-1113
+ * case by case, including its quirks: case 3 uses z where y is meant (K:854-855); in
+ * case 6 the function reports success even when the offset misses (K:989), leaving the
+ * sentinel (X,Y,Z) in place.  Returns 1 if a case matched, 0 otherwise; in/out hold the
+ * sentinel when nothing was found. */
+int orc_cross2point(long X, long Y, long Z, float x, float y, float z, float k1, float k2,
+                    float k3, int in[3], int out[3])
+{
+    float cx = (float)((X - 1) / 2.0), cy = (float)((Y - 1) / 2.0), cz = (float)((Z - 1) / 2.0);
+    in[0] = (int)X; in[1] = (int)Y; in[2] = (int)Z;
+    out[0] = (int)X; out[1] = (int)Y; out[2] = (int)Z;
+    int flag, t;
+    float r;
+    if (k1 == 0 && k2 != 0 && k3 != 0) {                 /* case 1, K:672 */
+        if (x > -cx && x < cx) {
+            float y1, z1, y2, z2, z3, y3, z4, y4;
+            r = (-cy - y) / k2; y1 = -cy; z1 = z + k3 * r;
+            r = (cy - y) / k2; y2 = cy; z2 = z + k3 * r;
+            r = (-cz - z) / k3; z3 = -cz; y3 = y + k2 * r;
+            r = (cz - z) / k3; z4 = cz; y4 = y + k2 * r;
+            (void)y1; (void)y2; (void)z3; (void)z4;
+            flag = 0;
+            if (z1 <= cz && z1 >= -cz && flag == 0) {
+                if (flag == 0) { in[0] = rnd_half(x + cx); in[1] = 0; in[2] = rnd_half(z1 + cz); }
+                flag = 1;
+            }
+            if (z2 <= cz && z2 >= -cz) {
+                if (flag == 0) { in[0] = rnd_half(x + cx); in[1] = (int)Y - 1; in[2] = rnd_half(z2 + cz); }
+                else { out[0] = rnd_half(x + cx); out[1] = (int)Y - 1; out[2] = rnd_half(z2 + cz); }
+                flag = 1;
+            }
+            if (y3 <= cy && y3 >= -cy) {
+                if (flag == 0) { in[0] = rnd_half(x + cx); in[1] = rnd_half(y3 + cy); in[2] = 0; }
+                else { out[0] = rnd_half(x + cx); out[1] = rnd_half(y3 + cy); out[2] = 0; }
+                flag = 1;
+            }
+            if (y4 <= cy && y4 >= -cy) {
+                if (flag == 0) { in[0] = rnd_half(x + cx); in[1] = rnd_half(y4 + cy); in[2] = (int)Z - 1; }
+                else { out[0] = rnd_half(x + cx); out[1] = rnd_half(y4 + cy); out[2] = (int)Z - 1; }
+            }
+            if (flag != 0) {
+                if ((float)(out[1] - in[1]) * k2 + (float)(out[2] - in[2]) * k3 < 0) {
+                    t = in[1]; in[1] = out[1]; out[1] = t;
+                    t = in[2]; in[2] = out[2]; out[2] = t;
+                }
+            }
+            return 1;
+        }
+    }
+    if (k1 != 0 && k2 == 0 && k3 != 0) {                 /* case 2, K:759 */
+        if (y > -cy && y < cy) {
+            float z1, z2, x3, x4;
+            r = (-cx - x) / k1; z1 = z + k3 * r;
+            r = (cx - x) / k1; z2 = z + k3 * r;
+            r = (-cz - z) / k3; x3 = x + k1 * r;
+            r = (cz - z) / k3; x4 = x + k1 * r;
+            flag = 0;
+            if (z1 <= cz && z1 >= -cz) {
+                if (flag == 0) { in[0] = 0; in[1] = rnd_half(y + cy); in[2] = rnd_half(z1 + cz); }
+                else { out[0] = 0; out[1] = rnd_half(y + cy); out[2] = rnd_half(z1 + cz); }
+                flag = 1;
+            }
+            if (z2 <= cz && z2 >= -cz) {
+                if (flag == 0) { in[0] = (int)X - 1; in[1] = rnd_half(y + cy); in[2] = rnd_half(z2 + cz); }
+                else { out[0] = (int)X - 1; out[1] = rnd_half(y + cy); out[2] = rnd_half(z2 + cz); }
+                flag = 1;
+            }
+            if (x3 <= cx && x3 >= -cx) {
+                if (flag == 0) { in[0] = rnd_half(x3 + cx); in[1] = rnd_half(y + cy); in[2] = 0; }
+                else { out[0] = rnd_half(x3 + cx); out[1] = rnd_half(y + cy); out[2] = 0; }
+                flag = 1;
+            }
+            if (x4 <= cx && x4 >= -cx) {
+                if (flag == 0) { in[0] = rnd_half(x4 + cx); in[1] = rnd_half(y + cy); in[2] = (int)Z - 1; }
+                else { out[0] = rnd_half(x4 + cx); out[1] = rnd_half(y + cy); out[2] = (int)Z - 1; }
+                flag = 1;
+            }
+            if (flag != 0) {
+                if ((float)(out[0] - in[0]) * k1 + (float)(out[2] - in[2]) * k3 < 0) {
+                    t = in[0]; in[0] = out[0]; out[0] = t;
+                    t = in[2]; in[2] = out[2]; out[2] = t;
+                }
+            }
+            return 1;
+        }
+    }
+    if (k1 != 0 && k2 != 0 && k3 == 0) {                 /* case 3, K:847 */
+        if (z > -cz && z < cz) {
+            float y1, y2, x3, x4;
+            r = (-cx - x) / k1; y1 = y + k2 * r;
+            r = (cx - x) / k1; y2 = y + k2 * r;
+            r = (-cy - z) / k2; x3 = x + k1 * r;          /* z for y: K:854 */
+            r = (cy - z) / k2; x4 = x + k1 * r;           /* K:855 */
+            flag = 0;
+            if (y1 <= cy && y1 >= -cy) {
+                if (flag == 0) { in[0] = 0; in[1] = rnd_half(y1 + cy); in[2] = rnd_half(z + cz); }
+                else { out[0] = 0; out[1] = rnd_half(y1 + cy); out[2] = rnd_half(z + cz); }
+                flag = 1;
+            }
+            if (y2 <= cy && y2 >= -cy) {
+                if (flag == 0) { in[0] = (int)X - 1; in[1] = rnd_half(y2 + cy); in[2] = rnd_half(z + cz); }
+                else { out[0] = (int)X - 1; out[1] = rnd_half(y2 + cy); out[2] = rnd_half(z + cz); }
+                flag = 1;
+            }
+            if (x3 <= cx && x3 >= -cx) {
+                if (flag == 0) { in[0] = rnd_half(x3 + cx); in[1] = 0; in[2] = rnd_half(z + cz); }
+                else { out[0] = rnd_half(x3 + cx); out[1] = 0; out[2] = rnd_half(z + cz); }
+                flag = 1;
+            }
+            if (x4 <= cx && x4 >= -cx) {
+                if (flag == 0) { in[0] = rnd_half(x4 + cx); in[1] = (int)Y - 1; in[2] = rnd_half(z + cz); }
+                else { out[0] = rnd_half(x4 + cx); out[1] = (int)Y - 1; out[2] = rnd_half(z + cz); }
+                flag = 1;
+            }
+            if (flag != 0) {
+                if ((float)(out[0] - in[0]) * k1 + (float)(out[1] - in[1]) * k2 < 0) {
+                    t = in[0]; in[0] = out[0]; out[0] = t;
+                    t = in[1]; in[1] = out[1]; out[1] = t;
+                }
+            }
+            return 1;
+        }
+    }
+    if ((double)fabsf(k1) < ORC_ZERO && (double)fabsf(k2) < ORC_ZERO && (double)fabsf(k3) >= ORC_ZERO) { /* case 4 */
+        if (x < cx && x > -cx && y < cy && y > -cy) {
+            in[0] = rnd_half(x + cx); out[0] = in[0];
+            in[1] = rnd_half(y + cy); out[1] = in[1];
+            if (k3 > 0) { in[2] = 0; out[2] = (int)Z - 1; }
+            else { in[2] = (int)Z - 1; out[2] = 0; }
+            return 1;
+        }
+    }
+    if ((double)fabsf(k1) < ORC_ZERO && (double)fabsf(k2) >= ORC_ZERO && (double)fabsf(k3) < ORC_ZERO) { /* case 5 */
+        if (x > -cx && x < cx && z > -cz && z < cz) {
+            in[0] = rnd_half(x + cx); out[0] = in[0];
+            in[2] = rnd_half(z + cz); out[2] = in[2];
+            if (k2 > 0) { out[1] = (int)Y - 1; in[1] = 0; }
+            else { in[1] = (int)Y - 1; out[1] = 0; }
+            return 1;
+        }
+    }
+    if ((double)fabsf(k1) >= ORC_ZERO && (double)fabsf(k2) < ORC_ZERO && (double)fabsf(k3) < ORC_ZERO) { /* case 6 */
+        if (y > -cy && y < cy && z > -cz && z < cz) {
+            in[1] = rnd_half(y + cy); out[1] = in[1];
+            in[2] = rnd_half(z + cz); out[2] = in[2];
+            if (k1 > 0) { out[0] = (int)X - 1; in[0] = 0; }
+            else { in[0] = (int)X - 1; out[0] = 0; }
+        }
+        return 1;                                          /* K:989 */
+    }
+    if ((double)fabsf(k1) >= ORC_ZERO && (double)fabsf(k2) >= ORC_ZERO && (double)fabsf(k3) >= ORC_ZERO) { /* case 7 */
+        float x1v, y1v, z1v, x2v, y2v, z2v, x3v, y3v, z3v, x4v, y4v, z4v, x5v, y5v, z5v, x6v, y6v, z6v;
+        r = (-cx - x) / k1; x1v = -cx; y1v = y + k2 * r; z1v = z + k3 * r;
+        r = (cx - x) / k1; x2v = cx; y2v = y + k2 * r; z2v = z + k3 * r;
+        r = (-cy - y) / k2; x3v = x + k1 * r; y3v = -cy; z3v = z + k3 * r;
+        r = (cy - y) / k2; x4v = x + k1 * r; y4v = cy; z4v = z + k3 * r;
+        r = (-cz - z) / k3; x5v = x + k1 * r; y5v = y + k2 * r; z5v = -cz;
+        r = (cz - z) / k3; x6v = x + k1 * r; y6v = y + k2 * r; z6v = cz;
+        (void)x1v; (void)x2v; (void)y3v; (void)y4v; (void)z5v; (void)z6v;
+        flag = 0;
+        if (y1v <= cy && y1v >= -cy && z1v <= cz && z1v >= -cz) {
+            if (flag == 0) { in[0] = 0; in[1] = rnd_half(y1v + cy); in[2] = rnd_half(z1v + cz); }
+            else { out[0] = 0; out[1] = rnd_half(y1v + cy); out[2] = rnd_half(z1v + cz); }
+            flag = 1;
+        }
+        if (y2v <= cy && y2v >= -cy && z2v <= cz && z2v >= -cz) {
+            if (flag == 0) { in[0] = (int)X - 1; in[1] = rnd_half(y2v + cy); in[2] = rnd_half(z2v + cz); }
+            else { out[0] = (int)X - 1; out[1] = rnd_half(y2v + cy); out[2] = rnd_half(z2v + cz); }
+            flag = 1;
+        }
+        if (x3v <= cx && x3v >= -cx && z3v <= cz && z3v >= -cz) {
+            if (flag == 0) { in[0] = rnd_half(x3v + cx); in[1] = 0; in[2] = rnd_half(z3v + cz); }
+            else { out[0] = rnd_half(x3v + cx); out[1] = 0; out[2] = rnd_half(z3v + cz); }
+            flag = 1;
+        }
+        if (x4v <= cx && x4v >= -cx && z4v <= cz && z4v >= -cz) {
+            if (flag == 0) { in[0] = rnd_half(x4v + cx); in[1] = (int)Y - 1; in[2] = rnd_half(z4v + cz); }
+            else { out[0] = rnd_half(x4v + cx); out[1] = (int)Y - 1; out[2] = rnd_half(z4v + cz); }
+            flag = 1;
+        }
+        if (x5v <= cx && x5v >= -cx && y5v <= cy && y5v >= -cy) {
+            if (flag == 0) { in[0] = rnd_half(x5v + cx); in[1] = rnd_half(y5v + cy); in[2] = 0; }
+            else { out[0] = rnd_half(x5v + cx); out[1] = rnd_half(y5v + cy); out[2] = 0; }
+            flag = 1;
+        }
+        if (x6v <= cx && x6v >= -cx && y6v <= cy && y6v >= -cy) {
+            if (flag == 0) { in[0] = rnd_half(x6v + cx); in[1] = rnd_half(y6v + cy); in[2] = (int)Z - 1; }
+            else { out[0] = rnd_half(x6v + cx); out[1] = rnd_half(y6v + cy); out[2] = (int)Z - 1; }
+            flag = 1;
+        }
+        if ((float)(out[0] - in[0]) * k1 + (float)(out[1] - in[1]) * k2 + (float)(out[2] - in[2]) * k3 < 0) {
+            t = in[0]; in[0] = out[0]; out[0] = t;
+            t = in[1]; in[1] = out[1]; out[1] = t;
+            t = in[2]; in[2] = out[2]; out[2] = t;
+        }
+        return 1;
+    }
+    return 0;
+}
+
+/* Caller-side acceptance test (K:6202-6206): both voxels inside the box and distinct
+ * boundary indices.  The boundary index (K:8171-8212) is a bijection on boundary voxels
+ * (checked against the reference's calIndex by the oracle tests), so "distinct index"
+ * is "distinct voxel". */
+int orc_line_valid(long X, long Y, long Z, const int in[3], const int out[3])
+{
+    if (!(in[0] >= 0 && in[0] < X && in[1] >= 0 && in[1] < Y && in[2] >= 0 && in[2] < Z &&
+          out[0] >= 0 && out[0] < X && out[1] >= 0 && out[1] < Y && out[2] >= 0 && out[2] < Z))
+        return 0;
+    return !(in[0] == out[0] && in[1] == out[1] && in[2] == out[2]);
+}
+
+/* Greedy staircase walk of K:1762-1861: from the entry voxel, step along the axis whose
+ * next voxel centre is nearest the line (ties x, then y, then z), until the exit voxel is
+ * reached.  Writes one axis code (0,1,2) per step and returns the number of steps, or
+ * -(steps+1) if no candidate qualified ("Error! Wrong Point Found!", K:1841). */
+int orc_walk(long X, long Y, long Z, const int in[3], const int out[3], float x, float y,
+             float z, float k1, float k2, float k3, signed char *axes, int cap)
+{
+    float cx = (float)((X - 1) / 2.0), cy = (float)((Y - 1) / 2.0), cz = (float)((Z - 1) / 2.0);
+    x = x + cx; y = y + cy; z = z + cz;
+    long il = in[0], jl = in[1], kl = in[2];
+    long io = out[0], jo = out[1], ko = out[2];
+    if (k1 * (float)(out[0] - in[0]) + k2 * (float)(out[1] - in[1]) + k3 * (float)(out[2] - in[2]) < 0) {
+        k1 = -k1; k2 = -k2; k3 = -k3;
+    }
+    int n = 0;
+    do {
+        long i1 = il < io ? il + 1 : (il == io ? il - 60000 : il - 1);
+        long j2 = jl < jo ? jl + 1 : (jl == jo ? jl - 60000 : jl - 1);
+        long k3n = kl < ko ? kl + 1 : (kl == ko ? kl - 60000 : kl - 1);
+        float r, xt, yt, zt, d1, d2, d3, a, b, c;
+        r = k1 * (float)i1 - x * k1 + k2 * (float)jl - k2 * y + k3 * (float)kl - k3 * z;
+        xt = x + k1 * r; yt = y + k2 * r; zt = z + k3 * r;
+        a = xt - (float)i1; b = yt - (float)jl; c = zt - (float)kl;
+        d1 = sqrtf(a * a + b * b + c * c);
+        r = k1 * (float)il - x * k1 + k2 * (float)j2 - k2 * y + k3 * (float)kl - k3 * z;
+        xt = x + k1 * r; yt = y + k2 * r; zt = z + k3 * r;
+        a = xt - (float)il; b = yt - (float)j2; c = zt - (float)kl;
+        d2 = sqrtf(a * a + b * b + c * c);
+        r = k1 * (float)il - x * k1 + k2 * (float)jl - k2 * y + k3 * (float)k3n - k3 * z;
+        xt = x + k1 * r; yt = y + k2 * r; zt = z + k3 * r;
+        a = xt - (float)il; b = yt - (float)jl; c = zt - (float)k3n;
+        d3 = sqrtf(a * a + b * b + c * c);
+        int moved = 0;
+        if (d1 <= d2 && d1 <= d3 && i1 >= 0 && i1 < X) { if (n < cap) axes[n] = 0; n++; il = i1; moved = 1; }
+        if (d2 < d1 && d2 <= d3 && j2 >= 0 && j2 < Y) { if (n < cap) axes[n] = 1; n++; jl = j2; moved = 1; }
+        if (d3 < d1 && d3 < d2 && k3n >= 0 && k3n < Z) { if (n < cap) axes[n] = 2; n++; kl = k3n; moved = 1; }
+        if (!moved) return -(n + 1);
+    } while ((double)(labs(il - io) + labs(jl - jo) + labs(kl - ko)) > 1e-5);
+    return n;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* accumulation along one line                                                            */
+/* ------------------------------------------------------------------------------------ */
+
+typedef struct {
+    long X, Y, Z;
+    float dx, dy, dz, rho, thr;
+} orc_grid;
+
+/* Sign of each axis step along a line: +1 toward a larger exit index, -1 otherwise. */
+static inline void axis_signs(const int in[3], const int out[3], int sg[3])
+{
+    for (int a = 0; a < 3; a++) sg[a] = out[a] > in[a] ? 1 : -1;
+}
+
+/* Plain method along one line (K:1743-1863).  REAL = float reproduces the reference's
+ * arithmetic bit for bit; REAL = double is the FP64 oracle. */
+#define DEFINE_LINE_PLAIN(SUFFIX, REAL, EXACT)                                                  \
+    static void line_plain_##SUFFIX(const orc_grid *g, const int in[3], const int out[3],      \
+                                    const signed char *ax, int n, const float *au,              \
+                                    const float *av, const float *aw, const REAL *p, REAL *pn,  \
+                                    REAL *cnt)                                                  \
+    {                                                                                           \
+        long X = g->X, XY = g->X * g->Y;                                                        \
+        int sg[3];                                                                              \
+        axis_signs(in, out, sg);                                                                \
+        long e = in[0] + in[1] * X + in[2] * XY;                                                \
+        long last = e;                                                                          \
+        const long stride[3] = {1, X, XY};                                                      \
+        const float *comp[3] = {au, av, aw};                                                    \
+        const float dl[3] = {g->dx, g->dy, g->dz};                                              \
+        REAL pint = 0;                                                                          \
+        pn[e] += p[e];                                                                          \
+        cnt[e] += 1;                                                                            \
+        for (int s = 0; s < n; s++) {                                                           \
+            int a = ax[s];                                                                      \
+            long nx = last + sg[a] * stride[a];                                                 \
+            if (EXACT) {                                                                        \
+                float h = (-g->rho * (float)sg[a]) * dl[a];                                     \
+                float as = comp[a][nx] + comp[a][last];                                         \
+                pint = (REAL)((double)pint + ((double)h * 0.5) * (double)as);                  \
+                pn[nx] += (REAL)(p[e] + pint);                                                  \
+            } else {                                                                            \
+                double term = -(double)g->rho * (double)sg[a] * (double)dl[a] * 0.5 *          \
+                              ((double)comp[a][nx] + (double)comp[a][last]);                    \
+                pint += (REAL)term;                                                             \
+                pn[nx] += p[e] + pint;                                                          \
+            }                                                                                   \
+            cnt[nx] += 1;                                                                       \
+            last = nx;                                                                          \
+        }                                                                                       \
+    }
+DEFINE_LINE_PLAIN(f32, float, 1)
+DEFINE_LINE_PLAIN(f64, double, 0)
+
+/* Selected method along one line (K:2280-2537), including its asymmetries:
+ *   - the entry counts as a segment start when 0 < curl <= thr (K:2301);
+ *   - before the first start, an x step needs 0 < curl < thr but y/z steps only curl != 0
+ *     (K:2376, 2422, 2468);
+ *   - entering a bad voxel pauses the segment; an x step also pauses on curl == 0 through
+ *     the operator precedence of K:2394, a y/z step does not (K:2440, 2486) -- it walks
+ *     through the zero voxel without adding that step's increment;
+ *   - a good voxel after a pause restarts the segment with p0 = p[voxel], I = 0; the z
+ *     branch keeps the running curl/count sums (K:2497-2506);
+ *   - contributions: pn += (p0+I)/C*n, count += 1/C*n with C = sum(curl/1e4), n = steps. */
+#define DEFINE_LINE_SELECT(SUFFIX, REAL, EXACT)                                                  \
+    static void line_select_##SUFFIX(const orc_grid *g, const int in[3], const int out[3],      \
+                                     const signed char *ax, int n, const float *au,              \
+                                     const float *av, const float *aw, const float *curl,        \
+                                     const REAL *p, REAL *pn, REAL *cnt)                         \
+    {                                                                                            \
+        long X = g->X, XY = g->X * g->Y;                                                         \
+        int sg[3];                                                                               \
+        axis_signs(in, out, sg);                                                                 \
+        long e = in[0] + in[1] * X + in[2] * XY;                                                 \
+        long last = e;                                                                           \
+        const long stride[3] = {1, X, XY};                                                       \
+        const float *comp[3] = {au, av, aw};                                                     \
+        const float dl[3] = {g->dx, g->dy, g->dz};                                               \
+        const float thr = g->thr;                                                                \
+        REAL pint = 0, ctmp = 0, ntmp = 0, p0 = 0;                                               \
+        int started, outz = 0;                                                                   \
+        if (curl[e] == 0 || curl[e] > thr) started = 0;                                          \
+        else { p0 = p[e]; started = 1; ctmp = 0; ntmp = 0; }                                     \
+        for (int s = 0; s < n; s++) {                                                            \
+            int a = ax[s];                                                                       \
+            long nx = last + sg[a] * stride[a];                                                  \
+            float cn = curl[nx];                                                                 \
+            if (!started) {                                                                      \
+                int ok = (a == 0) ? (cn != 0 && cn < thr) : (cn != 0);                           \
+                if (ok) { p0 = p[nx]; started = 1; pint = 0; ntmp = 0; ctmp = 0; }               \
+            } else {                                                                             \
+                int good = (cn < thr && cn != 0);                                                \
+                if (outz == 0 && good) {                                                         \
+                    if (EXACT) {                                                                 \
+                        float h = (-g->rho * (float)sg[a]) * dl[a];                              \
+                        float as = comp[a][nx] + comp[a][last];                                  \
+                        pint = (REAL)((double)pint + ((double)h * 0.5) * (double)as);           \
+                        ctmp += (REAL)(cn / 10000);                                              \
+                    } else {                                                                     \
+                        pint += -(double)g->rho * (double)sg[a] * (double)dl[a] * 0.5 *        \
+                                ((double)comp[a][nx] + (double)comp[a][last]);                   \
+                        ctmp += (double)cn / 10000.0;                                            \
+                    }                                                                            \
+                    ntmp += 1;                                                                   \
+                    pn[nx] += (p0 + pint) * 1 / ctmp * ntmp;                                     \
+                    cnt[nx] += 1 / ctmp * ntmp;                                                  \
+                }                                                                                \
+                int enter_bad = (a == 0) ? ((outz == 0 && cn >= thr) || cn == 0)                 \
+                                         : (outz == 0 && cn >= thr);                             \
+                if (enter_bad) outz = 1;                                                         \
+                if (outz == 1 && good) {                                                         \
+                    p0 = p[nx]; pint = 0; outz = 0;                                              \
+                    if (a != 2) { ntmp = 0; ctmp = 0; }                                          \
+                }                                                                                \
+            }                                                                                    \
+            last = nx;                                                                           \
+        }                                                                                        \
+    }
+DEFINE_LINE_SELECT(f32, float, 1)
+DEFINE_LINE_SELECT(f64, double, 0)
+
+/* ------------------------------------------------------------------------------------ */
+/* full sweep, normalisation, iteration                                                   */
+/* ------------------------------------------------------------------------------------ */
+
+typedef struct {
+    long X, Y, Z;
+    float dx, dy, dz, rho, ls, thr;
+    int nv;
+    const float *k1, *k2, *k3;
+    int mode;          /* 0 plain, 1 select */
+    int geom_cpu_twin; /* 1: CPU-twin geometry (no pole guard, NoGrid without spacing) */
+} orc_problem;
+
+static long max_path(long X, long Y, long Z) { return X + Y + Z + 4; }
+
+/* Walk every (direction, lattice point) pair in the reference's CPU order (K:8288-8290)
+ * over the directions [d0, d1), accumulating into pn / cnt. Returns the number of lines
+ * that hit the "Wrong Point" branch. */
+#define DEFINE_SWEEP(SUFFIX, REAL)                                                                \
+    static long sweep_range_##SUFFIX(const orc_problem *P, int d0, int d1, const float *au,       \
+                                     const float *av, const float *aw, const float *curl,          \
+                                     const REAL *p, REAL *pn, REAL *cnt)                           \
+    {                                                                                              \
+        orc_grid g = {P->X, P->Y, P->Z, P->dx, P->dy, P->dz, P->rho, P->thr};                      \
+        int ng = orc_nogrid(P->X, P->Y, P->Z, P->ls, P->geom_cpu_twin);                            \
+        long cap = max_path(P->X, P->Y, P->Z);                                                     \
+        signed char *ax = (signed char *)malloc((size_t)cap);                                      \
+        long errors = 0;                                                                           \
+        for (int d = d0; d < d1; d++) {                                                            \
+            float c[4];                                                                            \
+            orc_dir_coeffs(P->k1[d], P->k2[d], P->k3[d], P->geom_cpu_twin, c);                     \
+            for (int pt = 0; pt < ng * ng; pt++) {                                                 \
+                float xyz[3];                                                                      \
+                int in[3], out[3];                                                                 \
+                orc_line_offset(pt, ng, P->ls, c, xyz);                                            \
+                orc_cross2point(P->X, P->Y, P->Z, xyz[0], xyz[1], xyz[2], P->k1[d], P->k2[d],      \
+                                P->k3[d], in, out);                                                \
+                if (!orc_line_valid(P->X, P->Y, P->Z, in, out)) continue;                          \
+                int n = orc_walk(P->X, P->Y, P->Z, in, out, xyz[0], xyz[1], xyz[2], P->k1[d],      \
+                                 P->k2[d], P->k3[d], ax, (int)cap);                                \
+                if (n < 0) { errors++; n = -n - 1; }                                               \
+                if (P->mode == 0)                                                                  \
+                    line_plain_##SUFFIX(&g, in, out, ax, n, au, av, aw, p, pn, cnt);               \
+                else                                                                               \
+                    line_select_##SUFFIX(&g, in, out, ax, n, au, av, aw, curl, p, pn, cnt);        \
+            }                                                                                      \
+        }                                                                                          \
+        free(ax);                                                                                  \
+        return errors;                                                                             \
+    }
+DEFINE_SWEEP(f32, float)
+DEFINE_SWEEP(f64, double)
+
+/* Sweep all directions.  nthreads > 1 splits the directions into contiguous blocks with
+ * private accumulators that are added in block order, which changes only the order of
+ * floating-point sums. */
+#define DEFINE_SWEEP_ALL(SUFFIX, REAL)                                                            \
+    long orc_sweep_##SUFFIX(const orc_problem *P, const float *au, const float *av,               \
+                            const float *aw, const float *curl, const REAL *p, REAL *pn,          \
+                            REAL *cnt, int nthreads)                                              \
+    {                                                                                             \
+        long V = P->X * P->Y * P->Z;                                                              \
+        if (nthreads <= 1)                                                                        \
+            return sweep_range_##SUFFIX(P, 0, P->nv, au, av, aw, curl, p, pn, cnt);               \
+        REAL *pp = (REAL *)calloc((size_t)V * 2 * (size_t)nthreads, sizeof(REAL));                \
+        long errors = 0;                                                                          \
+        _Pragma("omp parallel for num_threads(nthreads) reduction(+ : errors) schedule(static, 1)") \
+        for (int t = 0; t < nthreads; t++) {                                                      \
+            int d0 = (int)((long)P->nv * t / nthreads), d1 = (int)((long)P->nv * (t + 1) / nthreads); \
+            REAL *mypn = pp + (size_t)V * 2 * t, *mycnt = mypn + V;                               \
+            errors += sweep_range_##SUFFIX(P, d0, d1, au, av, aw, curl, p, mypn, mycnt);          \
+        }                                                                                         \
+        for (int t = 0; t < nthreads; t++) {                                                      \
+            REAL *mypn = pp + (size_t)V * 2 * t, *mycnt = mypn + V;                               \
+            for (long v = 0; v < V; v++) { pn[v] += mypn[v]; cnt[v] += mycnt[v]; }               \
+        }                                                                                         \
+        free(pp);                                                                                 \
+        return errors;                                                                            \
+    }
+DEFINE_SWEEP_ALL(f32, float)
+DEFINE_SWEEP_ALL(f64, double)
+
+/* Normalisation.  gpu_form = 1: devidecountInner (K:6746-6759), count > 0, pn reset.
+ * gpu_form = 0: devidecountInnerCPU (K:8340-8351), count > 1, pn reset only there. */
+#define DEFINE_DIVIDE(SUFFIX, REAL)                                                               \
+    void orc_divide_##SUFFIX(long V, REAL *p, REAL *pn, const REAL *cnt, int gpu_form)            \
+    {                                                                                             \
+        for (long v = 0; v < V; v++) {                                                            \
+            if (gpu_form ? cnt[v] > 0 : cnt[v] > 1) {                                             \
+                pn[v] = pn[v] / cnt[v];                                                           \
+                p[v] = pn[v];                                                                     \
+                pn[v] = 0;                                                                        \
+            }                                                                                     \
+        }                                                                                         \
+    }
+DEFINE_DIVIDE(f32, float)
+DEFINE_DIVIDE(f64, double)
+
+/* The iteration of main() (K:8794-8863): p = pn = p_init, then niter times
+ * {count = 0; sweep; divide}.  Returns p and the last iteration's count. */
+#define DEFINE_SOLVE(SUFFIX, REAL)                                                                \
+    long orc_solve_##SUFFIX(const orc_problem *P, const float *au, const float *av,               \
+                            const float *aw, const float *curl, const float *p_init, int niter,   \
+                            REAL *p, REAL *cnt, int nthreads)                                     \
+    {                                                                                             \
+        long V = P->X * P->Y * P->Z, errors = 0;                                                  \
+        REAL *pn = (REAL *)malloc(sizeof(REAL) * (size_t)V);                                      \
+        for (long v = 0; v < V; v++) { p[v] = (REAL)p_init[v]; pn[v] = (REAL)p_init[v]; cnt[v] = 0; } \
+        for (int it = 0; it < niter; it++) {                                                      \
+            memset(cnt, 0, sizeof(REAL) * (size_t)V);                                             \
+            errors += orc_sweep_##SUFFIX(P, au, av, aw, curl, p, pn, cnt, nthreads);              \
+            orc_divide_##SUFFIX(V, p, pn, cnt, 1);                                                \
+        }                                                                                         \
+        free(pn);                                                                                 \
+        return errors;                                                                            \
+    }
+DEFINE_SOLVE(f32, float)
+DEFINE_SOLVE(f64, double)
+
+/* ------------------------------------------------------------------------------------ */
+/* helpers exposed for the tests                                                          */
+/* ------------------------------------------------------------------------------------ */
+
+/* Line table of one direction: for every lattice point, valid flag, entry, exit and the
+ * walk length (or -1 for invalid points). */
+long orc_trace_direction(long X, long Y, long Z, float ls, float k1, float k2, float k3,
+                         int geom_cpu_twin, int *valid, int *inout, int *nsteps, float *xyz)
+{
+    int ng = orc_nogrid(X, Y, Z, ls, geom_cpu_twin);
+    float c[4];
+    orc_dir_coeffs(k1, k2, k3, geom_cpu_twin, c);
+    long cap = max_path(X, Y, Z), nvalid = 0;
+    signed char *ax = (signed char *)malloc((size_t)cap);
+    for (int pt = 0; pt < ng * ng; pt++) {
+        int in[3], out[3];
+        float o[3];
+        orc_line_offset(pt, ng, ls, c, o);
+        orc_cross2point(X, Y, Z, o[0], o[1], o[2], k1, k2, k3, in, out);
+        int ok = orc_line_valid(X, Y, Z, in, out);
+        valid[pt] = ok;
+        for (int a = 0; a < 3; a++) { inout[6 * pt + a] = in[a]; inout[6 * pt + 3 + a] = out[a]; xyz[3 * pt + a] = o[a]; }
+        nsteps[pt] = ok ? orc_walk(X, Y, Z, in, out, o[0], o[1], o[2], k1, k2, k3, ax, (int)cap) : -1;
+        nvalid += ok;
+    }
+    free(ax);
+    return nvalid;
+}
+
+/* Boundary numbering of calIndex (K:8171-8212): writes index[v] for boundary voxels and
+ * leaves the rest untouched. */
+void orc_calindex(long X, long Y, long Z, long *index)
+{
+    long n = X * Y * 2 + (Z - 2) * Y * 2 + (X - 2) * (Z - 2) * 2;
+    for (long no = n - 1; no >= 0; no--) {
+        long io = 0, jo = 0, ko = 0;
+        long a = X * Y, b = a + Y * (Z - 1), c = b + (X - 1) * Y, d = c + (X - 1) * (Z - 2),
+             e = d + (Y - 1) * (Z - 2);
+        if (no <= a - 1) { ko = 0; jo = no / X; io = no - X * jo; }
+        if (no > a - 1 && no <= b - 1) { io = X - 1; jo = (no - a) / (Z - 1); ko = no - a - jo * (Z - 1) + 1; }
+        if (no > b - 1 && no <= c - 1) { ko = Z - 1; jo = (no - b) / (X - 1); io = no - b - jo * (X - 1); io = X - 2 - io; }
+        if (no > c - 1 && no <= d - 1) { jo = 0; ko = (no - c) / (X - 1); io = no - c - ko * (X - 1); io = X - 2 - io; ko = ko + 1; }
+        if (no > d - 1 && no <= e - 1) { io = 0; jo = (no - d) / (Z - 2); ko = no - d - jo * (Z - 2); ko = Z - 2 - ko; jo = jo + 1; }
+        if (no > e - 1) { jo = Y - 1; ko = (no - e) / (X - 2); io = no - e - ko * (X - 2); ko = Z - 2 - ko; io = io + 1; }
+        index[io + jo * X + ko * X * Y] = no;
+    }
+}
+
+/* |curl a| times the mask (K:8352-8378): central differences inside, one-sided at the
+ * faces, FP32 as in the reference. */
+void orc_curl(long X, long Y, long Z, float dx, float dy, float dz, const float *au,
+              const float *av, const float *aw, const float *mask, float *curl)
+{
+    for (long k = 0; k < Z; k++)
+        for (long j = 0; j < Y; j++)
+            for (long i = 0; i < X; i++) {
+                long i0 = i - 1 >= 0 ? i - 1 : i, j0 = j - 1 >= 0 ? j - 1 : j, k0 = k - 1 >= 0 ? k - 1 : k;
+                long ie = i + 1 <= X - 1 ? i + 1 : i, je = j + 1 <= Y - 1 ? j + 1 : j, ke = k + 1 <= Z - 1 ? k + 1 : k;
+                long XY = X * Y;
+                float cxv = (aw[i + je * X + k * XY] - aw[i + j0 * X + k * XY]) / (float)(je - j0) / dy;
+                cxv += -(av[i + j * X + ke * XY] - av[i + j * X + k0 * XY]) / (float)(ke - k0) / dz;
+                float cyv = -(aw[ie + j * X + k * XY] - aw[i0 + j * X + k * XY]) / (float)(ie - i0) / dx;
+                cyv += (au[i + j * X + ke * XY] - au[i + j * X + k0 * XY]) / (float)(ke - k0) / dz;
+                float czv = (av[ie + j * X + k * XY] - av[i0 + j * X + k * XY]) / (float)(ie - i0) / dx;
+                czv += -(au[i + je * X + k * XY] - au[i + j0 * X + k * XY]) / (float)(je - j0) / dy;
+                curl[i + j * X + k * XY] = sqrtf(cxv * cxv + cyv * cyv + czv * czv) * mask[i + j * X + k * XY];
+            }
+}
+
+int orc_num_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}

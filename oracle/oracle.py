@@ -1,0 +1,354 @@
+"""ctypes bindings of the CPU oracle and of the reference's own CPU functions.
+
+TEST INFRASTRUCTURE ONLY.  Imported by tests/, ``__graft_entry__.smoke()`` and bench.py's
+CPU-baseline / reference arm, always as the checker or the timed CPU baseline, never by
+the product package.
+
+* ``Oracle`` wraps oracle/omni_oracle.c (built into oracle/_build/liborc.so), the plain-C
+  restatement of the reference's omni path (Omni3D_8.0/Omni3D_8.0/kernel.cu), with an
+  FP32 mode that reproduces the reference's float arithmetic and an FP64 mode on the same
+  discrete line geometry.
+* ``RefLib`` wraps oracle/_ref/libomni_ref.so: the reference's own functions
+  (cross2point, bodyIntegralInner, bodyIntegralInnerSelect, calIndex,
+  omni3dparallellinesESInnerCPU, devidecountInnerCPU, calCurlofMaterialAccCPU, sor3D,
+  calRHS) compiled from its sources by oracle/build_ref.sh.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+ORC_SO = os.path.join(BUILD, "liborc.so")
+REF_SO = os.path.join(HERE, "_ref", "libomni_ref.so")
+REF_STAGED = os.path.join(HERE, "_ref", "src", "ref_kernel_extract.cpp")
+REFERENCE_ROOT = os.environ.get("OMNI3D_REFERENCE_ROOT", "/root/reference")
+
+_f = C.c_float
+_d = C.c_double
+_i = C.c_int
+_l = C.c_long
+_fp = C.POINTER(C.c_float)
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_lp = C.POINTER(C.c_long)
+_bp = C.POINTER(C.c_byte)
+
+
+def build_oracle(force: bool = False) -> str:
+    """Compile the C restatement (one rounding per float operation: no contraction)."""
+    src = os.path.join(HERE, "omni_oracle.c")
+    if force or not os.path.exists(ORC_SO) or os.path.getmtime(ORC_SO) < os.path.getmtime(src):
+        os.makedirs(BUILD, exist_ok=True)
+        tmp = ORC_SO + ".tmp%d" % os.getpid()
+        subprocess.check_call(["gcc", "-O2", "-std=gnu11", "-ffp-contract=off", "-fopenmp", "-fPIC",
+                               "-shared", "-o", tmp, src, "-lm"])
+        os.replace(tmp, ORC_SO)
+    return ORC_SO
+
+
+def build_ref(force: bool = False) -> str | None:
+    """Stage the reference sources (when the reference tree is present) and compile them.
+
+    Returns the library path, or None when neither the reference tree nor a staged copy
+    exists on this machine."""
+    script = os.path.join(HERE, "build_ref.sh")
+    have_tree = os.path.exists(os.path.join(REFERENCE_ROOT, "Omni3D_8.0", "Omni3D_8.0", "kernel.cu"))
+    if have_tree and (force or not os.path.exists(REF_STAGED)):
+        subprocess.check_call(["bash", script, "stage"], env=dict(os.environ, REF_ROOT=REFERENCE_ROOT),
+                              stdout=subprocess.DEVNULL)
+    if not os.path.exists(REF_STAGED):
+        return None
+    deps = [REF_STAGED, os.path.join(HERE, "ref_driver.cpp")]
+    if force or not os.path.exists(REF_SO) or any(os.path.getmtime(REF_SO) < os.path.getmtime(d) for d in deps):
+        subprocess.check_call(["bash", script, "build"], stdout=subprocess.DEVNULL)
+    return REF_SO
+
+
+def _ptr(a: np.ndarray, ct):
+    assert a.flags["C_CONTIGUOUS"], "arrays must be C-contiguous"
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+class OrcProblem(C.Structure):
+    _fields_ = [("X", _l), ("Y", _l), ("Z", _l), ("dx", _f), ("dy", _f), ("dz", _f), ("rho", _f),
+                ("ls", _f), ("thr", _f), ("nv", _i), ("k1", _fp), ("k2", _fp), ("k3", _fp),
+                ("mode", _i), ("geom_cpu_twin", _i)]
+
+
+class Oracle:
+    """The C restatement.  Arrays are numpy, x-fastest ([Z][Y][X] C order)."""
+
+    def __init__(self, path: str | None = None):
+        self.lib = C.CDLL(path or build_oracle())
+        L = self.lib
+        L.orc_nogrid.restype = _i
+        L.orc_nogrid.argtypes = [_l, _l, _l, _f, _i]
+        L.orc_dir_coeffs.argtypes = [_f, _f, _f, _i, _fp]
+        L.orc_line_offset.argtypes = [_i, _i, _f, _fp, _fp]
+        L.orc_cross2point.restype = _i
+        L.orc_cross2point.argtypes = [_l, _l, _l, _f, _f, _f, _f, _f, _f, _ip, _ip]
+        L.orc_line_valid.restype = _i
+        L.orc_line_valid.argtypes = [_l, _l, _l, _ip, _ip]
+        L.orc_walk.restype = _i
+        L.orc_walk.argtypes = [_l, _l, _l, _ip, _ip, _f, _f, _f, _f, _f, _f, _bp, _i]
+        L.orc_trace_direction.restype = _l
+        L.orc_trace_direction.argtypes = [_l, _l, _l, _f, _f, _f, _f, _i, _ip, _ip, _ip, _fp]
+        for s, ptr in (("f32", _fp), ("f64", _dp)):
+            fn = getattr(L, "orc_sweep_" + s)
+            fn.restype = _l
+            fn.argtypes = [C.POINTER(OrcProblem), _fp, _fp, _fp, _fp, ptr, ptr, ptr, _i]
+            fn = getattr(L, "orc_solve_" + s)
+            fn.restype = _l
+            fn.argtypes = [C.POINTER(OrcProblem), _fp, _fp, _fp, _fp, _fp, _i, ptr, ptr, _i]
+            fn = getattr(L, "orc_divide_" + s)
+            fn.argtypes = [_l, ptr, ptr, ptr, _i]
+        L.orc_calindex.argtypes = [_l, _l, _l, _lp]
+        L.orc_curl.argtypes = [_l, _l, _l, _f, _f, _f, _fp, _fp, _fp, _fp, _fp]
+        L.orc_num_threads.restype = _i
+
+    # -- geometry ----------------------------------------------------------------------
+    def nogrid(self, dims, ls, cpu_twin=False) -> int:
+        X, Y, Z = dims
+        return self.lib.orc_nogrid(X, Y, Z, ls, int(cpu_twin))
+
+    def dir_coeffs(self, k, cpu_twin=False) -> np.ndarray:
+        k = np.asarray(k, np.float32)
+        out = np.zeros((len(k), 4), np.float32)
+        for d in range(len(k)):
+            self.lib.orc_dir_coeffs(float(k[d, 0]), float(k[d, 1]), float(k[d, 2]), int(cpu_twin),
+                                    _ptr(out[d], C.c_float))
+        return out
+
+    def trace_direction(self, dims, ls, kd, cpu_twin=False):
+        """Per lattice point: valid flag, (in ijk, out ijk), walk length, offset xyz."""
+        X, Y, Z = dims
+        ng = self.nogrid(dims, ls, cpu_twin)
+        n = ng * ng
+        valid = np.zeros(n, np.int32)
+        inout = np.zeros((n, 6), np.int32)
+        nsteps = np.zeros(n, np.int32)
+        xyz = np.zeros((n, 3), np.float32)
+        self.lib.orc_trace_direction(X, Y, Z, ls, float(kd[0]), float(kd[1]), float(kd[2]), int(cpu_twin),
+                                     _ptr(valid, C.c_int), _ptr(inout, C.c_int), _ptr(nsteps, C.c_int),
+                                     _ptr(xyz, C.c_float))
+        return valid, inout, nsteps, xyz
+
+    def walk(self, dims, inout, xyz, kd) -> np.ndarray:
+        X, Y, Z = dims
+        cap = X + Y + Z + 4
+        ax = np.zeros(cap, np.int8)
+        i = np.ascontiguousarray(inout[:3], np.int32)
+        o = np.ascontiguousarray(inout[3:], np.int32)
+        n = self.lib.orc_walk(X, Y, Z, _ptr(i, C.c_int), _ptr(o, C.c_int), float(xyz[0]), float(xyz[1]),
+                              float(xyz[2]), float(kd[0]), float(kd[1]), float(kd[2]),
+                              _ptr(ax, C.c_byte), cap)
+        if n < 0:
+            raise RuntimeError("walk failed")
+        return ax[:n].copy()
+
+    # -- sweeps ------------------------------------------------------------------------
+    def _problem(self, dims, spacing, rho, ls, thr, k, mode, cpu_twin):
+        k = np.ascontiguousarray(np.asarray(k, np.float32))
+        ks = [np.ascontiguousarray(k[:, a]) for a in range(3)]
+        P = OrcProblem(dims[0], dims[1], dims[2], spacing[0], spacing[1], spacing[2], rho, ls, thr,
+                       len(k), _ptr(ks[0], C.c_float), _ptr(ks[1], C.c_float), _ptr(ks[2], C.c_float),
+                       int(mode), int(cpu_twin))
+        return P, ks
+
+    def solve(self, dims, spacing, k, au, av, aw, p_init, niter, *, rho=1.0, ls=1.0, mode=0, thr=0.0,
+              curl=None, precision="f32", nthreads=1, cpu_twin=False):
+        """The reference iteration: p = pn = p_init, niter x {sweep, p = pn/count}."""
+        P, keep = self._problem(dims, spacing, rho, ls, thr, k, mode, cpu_twin)
+        dt = np.float32 if precision == "f32" else np.float64
+        ct = C.c_float if precision == "f32" else C.c_double
+        V = dims[0] * dims[1] * dims[2]
+        f = lambda a: np.ascontiguousarray(np.asarray(a, np.float32).reshape(-1))
+        au, av, aw, p_init = f(au), f(av), f(aw), f(p_init)
+        curl = f(curl) if curl is not None else np.zeros(V, np.float32)
+        p = np.zeros(V, dt)
+        cnt = np.zeros(V, dt)
+        fn = getattr(self.lib, "orc_solve_" + precision)
+        err = fn(C.byref(P), _ptr(au, C.c_float), _ptr(av, C.c_float), _ptr(aw, C.c_float),
+                 _ptr(curl, C.c_float), _ptr(p_init, C.c_float), int(niter), _ptr(p, ct), _ptr(cnt, ct),
+                 int(nthreads))
+        if err:
+            raise RuntimeError("oracle: %d lines hit the wrong-point branch" % err)
+        return p, cnt
+
+    def sweep(self, dims, spacing, k, au, av, aw, p, *, rho=1.0, ls=1.0, mode=0, thr=0.0, curl=None,
+              precision="f32", nthreads=1, cpu_twin=False):
+        """One sweep from p: returns (pn, count) without normalisation."""
+        P, keep = self._problem(dims, spacing, rho, ls, thr, k, mode, cpu_twin)
+        dt = np.float32 if precision == "f32" else np.float64
+        ct = C.c_float if precision == "f32" else C.c_double
+        V = dims[0] * dims[1] * dims[2]
+        f = lambda a: np.ascontiguousarray(np.asarray(a, np.float32).reshape(-1))
+        au, av, aw = f(au), f(av), f(aw)
+        curl = f(curl) if curl is not None else np.zeros(V, np.float32)
+        p = np.ascontiguousarray(np.asarray(p, dt).reshape(-1))
+        pn = np.zeros(V, dt)
+        cnt = np.zeros(V, dt)
+        fn = getattr(self.lib, "orc_sweep_" + precision)
+        err = fn(C.byref(P), _ptr(au, C.c_float), _ptr(av, C.c_float), _ptr(aw, C.c_float),
+                 _ptr(curl, C.c_float), _ptr(p, ct), _ptr(pn, ct), _ptr(cnt, ct), int(nthreads))
+        if err:
+            raise RuntimeError("oracle: %d lines hit the wrong-point branch" % err)
+        return pn, cnt
+
+    def calindex(self, dims) -> np.ndarray:
+        X, Y, Z = dims
+        idx = np.full(X * Y * Z, -1, np.int64)
+        self.lib.orc_calindex(X, Y, Z, _ptr(idx, C.c_long))
+        return idx
+
+    def curl(self, dims, spacing, au, av, aw, mask) -> np.ndarray:
+        X, Y, Z = dims
+        f = lambda a: np.ascontiguousarray(np.asarray(a, np.float32).reshape(-1))
+        au, av, aw, mask = f(au), f(av), f(aw), f(mask)
+        out = np.zeros(X * Y * Z, np.float32)
+        self.lib.orc_curl(X, Y, Z, spacing[0], spacing[1], spacing[2], _ptr(au, C.c_float),
+                          _ptr(av, C.c_float), _ptr(aw, C.c_float), _ptr(mask, C.c_float),
+                          _ptr(out, C.c_float))
+        return out
+
+    def num_threads(self) -> int:
+        return self.lib.orc_num_threads()
+
+
+class RefLib:
+    """The reference's own functions (see oracle/build_ref.sh)."""
+
+    def __init__(self, path: str | None = None):
+        path = path or build_ref()
+        if path is None:
+            raise FileNotFoundError("reference sources are not staged on this machine")
+        self.lib = C.CDLL(path)
+        L = self.lib
+        L.ref_calindex.argtypes = [_l, _l, _l, _lp]
+        L.ref_cross2point.restype = _i
+        L.ref_cross2point.argtypes = [_l, _l, _l, _f, _f, _f, _f, _f, _f, _ip]
+        common = [_l, _l, _l, _f, _f, _f, _f, _f, _f]
+        L.ref_sweep.restype = C.c_longlong
+        L.ref_sweep.argtypes = common + [_i, _fp, _fp, _fp, _i, _fp, _fp, _fp, _fp, _fp, _fp, _fp, _i]
+        L.ref_sweep_dirs.argtypes = common + [_i, _i, _fp, _fp, _fp, _i, _fp, _fp, _fp, _fp, _fp, _fp, _fp]
+        L.ref_solve.argtypes = common + [_i, _fp, _fp, _fp, _i, _fp, _fp, _fp, _fp, _fp, _i, _fp, _fp, _i]
+        L.ref_cpu_twin_solve.argtypes = [_l, _l, _l, _f, _f, _f, _f, _f, _i, _fp, _fp, _fp, _fp, _fp, _fp,
+                                         _fp, _i, _fp, _fp]
+        L.ref_curl.argtypes = [_l, _l, _l, _f, _f, _f, _fp, _fp, _fp, _fp, _fp]
+        L.ref_sor.argtypes = [_i, _i, _i, _d, _d, _d, _d, _dp, _dp, _dp, _i, _d, _dp]
+        L.ref_calrhs.argtypes = [_i, _i, _i, _d, _d, _d, _d, _dp, _dp, _dp, _dp]
+        L.ref_num_threads.restype = _i
+
+    @staticmethod
+    def _f(a):
+        return np.ascontiguousarray(np.asarray(a, np.float32).reshape(-1))
+
+    def calindex(self, dims):
+        X, Y, Z = dims
+        idx = np.full(X * Y * Z, -1, np.int64)
+        self.lib.ref_calindex(X, Y, Z, _ptr(idx, C.c_long))
+        return idx
+
+    def cross2point(self, dims, xyz, kd):
+        io = np.zeros(6, np.int32)
+        ok = self.lib.ref_cross2point(dims[0], dims[1], dims[2], float(xyz[0]), float(xyz[1]), float(xyz[2]),
+                                      float(kd[0]), float(kd[1]), float(kd[2]), _ptr(io, C.c_int))
+        return ok, io
+
+    def solve(self, dims, spacing, k, au, av, aw, p_init, niter, *, rho=1.0, ls=1.0, mode=0, thr=0.0,
+              curl=None, nthreads=1):
+        X, Y, Z = dims
+        V = X * Y * Z
+        k = np.asarray(k, np.float32)
+        k1, k2, k3 = (np.ascontiguousarray(k[:, a]) for a in range(3))
+        au, av, aw, p_init = self._f(au), self._f(av), self._f(aw), self._f(p_init)
+        curl = self._f(curl) if curl is not None else np.zeros(V, np.float32)
+        p = np.zeros(V, np.float32)
+        cnt = np.zeros(V, np.float32)
+        self.lib.ref_solve(X, Y, Z, spacing[0], spacing[1], spacing[2], rho, ls, thr, len(k),
+                           _ptr(k1, C.c_float), _ptr(k2, C.c_float), _ptr(k3, C.c_float), int(mode),
+                           _ptr(au, C.c_float), _ptr(av, C.c_float), _ptr(aw, C.c_float), _ptr(curl, C.c_float),
+                           _ptr(p_init, C.c_float), int(niter), _ptr(p, C.c_float), _ptr(cnt, C.c_float),
+                           int(nthreads))
+        return p, cnt
+
+    def sweep(self, dims, spacing, k, au, av, aw, p, *, rho=1.0, ls=1.0, mode=0, thr=0.0, curl=None, nthreads=1):
+        """One full-coverage sweep over the given directions; returns (pn, count, units)."""
+        X, Y, Z = dims
+        V = X * Y * Z
+        k = np.asarray(k, np.float32)
+        k1, k2, k3 = (np.ascontiguousarray(k[:, a]) for a in range(3))
+        au, av, aw, p = self._f(au), self._f(av), self._f(aw), self._f(p)
+        curl = self._f(curl) if curl is not None else np.zeros(V, np.float32)
+        pn = np.zeros(V, np.float32)
+        cnt = np.zeros(V, np.float32)
+        units = self.lib.ref_sweep(X, Y, Z, spacing[0], spacing[1], spacing[2], rho, ls, thr, len(k),
+                                   _ptr(k1, C.c_float), _ptr(k2, C.c_float), _ptr(k3, C.c_float), int(mode),
+                                   _ptr(au, C.c_float), _ptr(av, C.c_float), _ptr(aw, C.c_float),
+                                   _ptr(curl, C.c_float), _ptr(p, C.c_float), _ptr(pn, C.c_float),
+                                   _ptr(cnt, C.c_float), int(nthreads))
+        return pn, cnt, int(units)
+
+    def sweep_dirs(self, dims, spacing, k, d0, d1, au, av, aw, p, *, rho=1.0, ls=1.0, mode=0, thr=0.0,
+                   curl=None, pn=None, cnt=None):
+        X, Y, Z = dims
+        V = X * Y * Z
+        k = np.asarray(k, np.float32)
+        k1, k2, k3 = (np.ascontiguousarray(k[:, a]) for a in range(3))
+        curl = curl if curl is not None else np.zeros(V, np.float32)
+        pn = pn if pn is not None else np.zeros(V, np.float32)
+        cnt = cnt if cnt is not None else np.zeros(V, np.float32)
+        self.lib.ref_sweep_dirs(X, Y, Z, spacing[0], spacing[1], spacing[2], rho, ls, thr, int(d0), int(d1),
+                                _ptr(k1, C.c_float), _ptr(k2, C.c_float), _ptr(k3, C.c_float), int(mode),
+                                _ptr(au, C.c_float), _ptr(av, C.c_float), _ptr(aw, C.c_float),
+                                _ptr(curl, C.c_float), _ptr(p, C.c_float), _ptr(pn, C.c_float),
+                                _ptr(cnt, C.c_float))
+        return pn, cnt
+
+    def cpu_twin_solve(self, dims, spacing, k, au, av, aw, p_init, niter, *, rho=1.0, ls=1.0):
+        X, Y, Z = dims
+        V = X * Y * Z
+        k = np.asarray(k, np.float32)
+        k1, k2, k3 = (np.ascontiguousarray(k[:, a]) for a in range(3))
+        au, av, aw, p_init = self._f(au), self._f(av), self._f(aw), self._f(p_init)
+        p = np.zeros(V, np.float32)
+        cnt = np.zeros(V, np.float32)
+        self.lib.ref_cpu_twin_solve(X, Y, Z, spacing[0], spacing[1], spacing[2], rho, ls, len(k),
+                                    _ptr(k1, C.c_float), _ptr(k2, C.c_float), _ptr(k3, C.c_float),
+                                    _ptr(au, C.c_float), _ptr(av, C.c_float), _ptr(aw, C.c_float),
+                                    _ptr(p_init, C.c_float), int(niter), _ptr(p, C.c_float), _ptr(cnt, C.c_float))
+        return p, cnt
+
+    def curl(self, dims, spacing, au, av, aw, mask):
+        X, Y, Z = dims
+        au, av, aw, mask = self._f(au), self._f(av), self._f(aw), self._f(mask)
+        out = np.zeros(X * Y * Z, np.float32)
+        self.lib.ref_curl(X, Y, Z, spacing[0], spacing[1], spacing[2], _ptr(au, C.c_float), _ptr(av, C.c_float),
+                          _ptr(aw, C.c_float), _ptr(mask, C.c_float), _ptr(out, C.c_float))
+        return out
+
+    def sor(self, dims, spacing, au, av, aw, niter, eps, *, rho=1.0):
+        X, Y, Z = dims
+        g = lambda a: np.ascontiguousarray(np.asarray(a, np.float64).reshape(-1))
+        au, av, aw = g(au), g(av), g(aw)
+        p = np.zeros(X * Y * Z, np.float64)
+        self.lib.ref_sor(X, Y, Z, spacing[0], spacing[1], spacing[2], rho, _ptr(au, C.c_double),
+                         _ptr(av, C.c_double), _ptr(aw, C.c_double), int(niter), float(eps), _ptr(p, C.c_double))
+        return p
+
+    def num_threads(self) -> int:
+        return self.lib.ref_num_threads()
+
+
+def load_reference_directions(level_file: str) -> np.ndarray | None:
+    """Direction file of the reference tree (only where the tree is present)."""
+    path = os.path.join(REFERENCE_ROOT, "Omni3D_8.0", "Executable", level_file)
+    if not os.path.exists(path):
+        return None
+    rows = open(path).read().replace("\r", "").strip().split("\n")
+    return np.array([[float(x) for x in r.split()] for r in rows[:-1]], np.float32)

@@ -1,0 +1,584 @@
+// C ABI of libomni3d_gb300: solver contexts, the per-snapshot solve and the diagnostics.
+// The per-file block of the reference main() (K:8794-8863) becomes omni3d_solve(); the
+// per-direction setup of its kernels (K:6175-6191) is evaluated once per direction here on
+// the host and uploaded as a table.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "omni3d_internal.h"
+
+using namespace omni3d;
+
+namespace {
+
+thread_local std::string g_error;
+
+struct DeviceBuf {
+    void *p = nullptr;
+    size_t n = 0;
+    cudaError_t ensure(size_t bytes)
+    {
+        if (bytes <= n) return cudaSuccess;
+        cudaFree(p);
+        p = nullptr;
+        n = 0;
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e == cudaSuccess) n = bytes;
+        return e;
+    }
+    void release()
+    {
+        cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    template <typename T>
+    T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+}  // namespace
+
+namespace omni3d {
+unsigned long long g_kernel_launches = 0;
+void set_global_error(const std::string &msg) { g_error = msg; }
+}  // namespace omni3d
+
+struct omni3d_ctx {
+    omni3d_params prm{};
+    std::vector<float> dirs;
+    std::vector<DirEntry> table;
+    Geometry geo;
+    cudaStream_t st = nullptr;
+    bool own_stream = false;
+    std::string err;
+    double ms_geometry = 0.0;
+    // per-solve buffers
+    DeviceBuf in_ax, in_ay, in_az, in_aux, in_pinit;  // staging of host inputs
+    DeviceBuf f32, b16, curl;
+    DeviceBuf pvol_a, pvol_b, pout, cnt, pncnt, scratch;
+    Anchor anc;
+    cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+};
+
+namespace {
+
+int fail(omni3d_ctx *ctx, int code, const std::string &msg)
+{
+    if (ctx) ctx->err = msg;
+    g_error = msg;
+    return code;
+}
+
+int cuda_fail(omni3d_ctx *ctx, cudaError_t e, const char *what)
+{
+    return fail(ctx, e == cudaErrorMemoryAllocation ? OMNI3D_ERR_NOMEM : OMNI3D_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(ctx, x)                                          \
+    do {                                                    \
+        cudaError_t e_ = (x);                               \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #x); \
+    } while (0)
+
+// Rotation coefficients of one direction (K:6175-6191; libm in place of the intrinsics)
+// and the cross2point branches its components select (K:672, 759, 847, 936, 955, 974,
+// 992; "zero" is the double 1e-7, K:23).
+DirEntry make_dir(float k1, float k2, float k3)
+{
+    DirEntry D{};
+    float theta = acosf(k3);
+    float st = sinf(theta);
+    float phi = 0.0f;
+    if (st != 0.0f) {
+        phi = asinf(k2 / st);
+        if (k1 / st < 0) phi = (float)(-phi + 3.1415926535897932384626433832795);
+    }
+    D.ct = cosf(theta);
+    D.st = st;
+    D.cp = cosf(phi);
+    D.sp = sinf(phi);
+    D.k1 = k1;
+    D.k2 = k2;
+    D.k3 = k3;
+    const double z = 1e-7;
+    double a1 = std::fabs((double)k1), a2 = std::fabs((double)k2), a3 = std::fabs((double)k3);
+    int c = 0;
+    if (k1 == 0 && k2 != 0 && k3 != 0) c |= 1;
+    if (k1 != 0 && k2 == 0 && k3 != 0) c |= 2;
+    if (k1 != 0 && k2 != 0 && k3 == 0) c |= 4;
+    if (a1 < z && a2 < z && a3 >= z) c |= 8;
+    if (a1 < z && a2 >= z && a3 < z) c |= 16;
+    if (a1 >= z && a2 < z && a3 < z) c |= 32;
+    if (a1 >= z && a2 >= z && a3 >= z) c |= 64;
+    D.cas = c;
+    return D;
+}
+
+int check_params(const omni3d_params *p, std::string *why)
+{
+    if (!p) { *why = "params is NULL"; return OMNI3D_ERR_ARG; }
+    if (p->nx < 2 || p->ny < 2 || p->nz < 2) { *why = "grid dimensions must be >= 2"; return OMNI3D_ERR_ARG; }
+    long long V = (long long)p->nx * p->ny * p->nz;
+    if (V >= (1LL << 32) || (long long)p->nx * p->ny >= (1LL << 31)) {
+        *why = "grid too large: voxel indices are 32-bit";
+        return OMNI3D_ERR_RANGE;
+    }
+    if (!(p->line_spacing > 0.0f) || !std::isfinite(p->line_spacing)) { *why = "line_spacing must be > 0"; return OMNI3D_ERR_ARG; }
+    if (p->n_dirs <= 0 || !p->dirs) { *why = "no directions"; return OMNI3D_ERR_ARG; }
+    if (p->max_iter < 0) { *why = "max_iter must be >= 0"; return OMNI3D_ERR_ARG; }
+    if (p->method != OMNI3D_METHOD_PLAIN && p->method != OMNI3D_METHOD_SELECT) { *why = "unknown method"; return OMNI3D_ERR_ARG; }
+    if (p->solver != OMNI3D_SOLVER_ANCHOR && p->solver != OMNI3D_SOLVER_SWEEP) { *why = "unknown solver"; return OMNI3D_ERR_ARG; }
+    if (p->grad_storage != OMNI3D_GRAD_F32 && p->grad_storage != OMNI3D_GRAD_BF16) { *why = "unknown grad_storage"; return OMNI3D_ERR_ARG; }
+    if (p->gauge < OMNI3D_GAUGE_NONE || p->gauge > OMNI3D_GAUGE_MEAN) { *why = "unknown gauge"; return OMNI3D_ERR_ARG; }
+    if (p->gauge == OMNI3D_GAUGE_POINT &&
+        (p->ref_i < 0 || p->ref_i >= p->nx || p->ref_j < 0 || p->ref_j >= p->ny || p->ref_k < 0 || p->ref_k >= p->nz)) {
+        *why = "reference voxel outside the grid";
+        return OMNI3D_ERR_ARG;
+    }
+    if (!(p->tol >= 0.0)) { *why = "tol must be >= 0"; return OMNI3D_ERR_ARG; }
+    double ng = std::max(std::max(p->nx, p->ny), p->nz) * 1.732 / (double)p->line_spacing;
+    if (ng * ng * (double)p->n_dirs / 256.0 > 2.0e9) { *why = "too many lines (lattice x directions)"; return OMNI3D_ERR_RANGE; }
+    return OMNI3D_OK;
+}
+
+float ms_between(cudaEvent_t a, cudaEvent_t b)
+{
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+}
+
+// Upload (host) or adopt (device) one input volume.
+int stage(omni3d_ctx *ctx, const float *src, bool dev, DeviceBuf &buf, long long V, const float **out)
+{
+    if (!src) { *out = nullptr; return OMNI3D_OK; }
+    if (dev) { *out = src; return OMNI3D_OK; }
+    CK(ctx, buf.ensure(sizeof(float) * (size_t)V));
+    CK(ctx, cudaMemcpyAsync(buf.p, src, sizeof(float) * (size_t)V, cudaMemcpyHostToDevice, ctx->st));
+    *out = buf.as<float>();
+    return OMNI3D_OK;
+}
+
+// Build the device field (float4 ax, ay, az, curl; optional bf16 copy; curl array).
+int prepare_field(omni3d_ctx *ctx, const float *ax, const float *ay, const float *az, const float *curl,
+                  const float *mask, bool dev, Field *F)
+{
+    const Grid &g = ctx->geo.grid;
+    const long long V = g.V;
+    const float *dax, *day, *daz, *daux;
+    int rc;
+    if ((rc = stage(ctx, ax, dev, ctx->in_ax, V, &dax))) return rc;
+    if ((rc = stage(ctx, ay, dev, ctx->in_ay, V, &day))) return rc;
+    if ((rc = stage(ctx, az, dev, ctx->in_az, V, &daz))) return rc;
+    const bool select = ctx->prm.method == OMNI3D_METHOD_SELECT;
+    const float *dcurl = nullptr;
+    if (select) {
+        if (curl) {
+            if ((rc = stage(ctx, curl, dev, ctx->in_aux, V, &daux))) return rc;
+            dcurl = daux;
+        } else {
+            if ((rc = stage(ctx, mask, dev, ctx->in_aux, V, &daux))) return rc;
+            CK(ctx, ctx->curl.ensure(sizeof(float) * (size_t)V));
+            CK(ctx, curl_field(g, dax, day, daz, daux, ctx->curl.as<float>(), ctx->st));
+            dcurl = ctx->curl.as<float>();
+        }
+    }
+    const bool bf16 = ctx->prm.grad_storage == OMNI3D_GRAD_BF16;
+    CK(ctx, ctx->f32.ensure(sizeof(float4) * (size_t)V));
+    F->f32 = ctx->f32.as<float4>();
+    if (bf16) {
+        CK(ctx, ctx->b16.ensure(sizeof(uint2) * (size_t)V));
+        F->bf16 = ctx->b16.as<uint2>();
+    }
+    F->curl = const_cast<float *>(dcurl);
+    CK(ctx, pack_field(g, dax, day, daz, dcurl, F, bf16, ctx->st));
+    return OMNI3D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void omni3d_default_params(omni3d_params *p)
+{
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->nx = p->ny = p->nz = 64;             // K:8532-8534
+    p->dx = p->dy = p->dz = 0.006135923151543f;  // K:8533-8535
+    p->density = 1.0f;                      // K:8511
+    p->line_spacing = 1.0f;
+    p->max_iter = 100;                      // K:8526
+    p->threshold = 0.0f;
+    p->method = OMNI3D_METHOD_PLAIN;
+    p->solver = OMNI3D_SOLVER_ANCHOR;
+    p->grad_storage = OMNI3D_GRAD_F32;
+    p->tol = 0.0;
+    p->gauge = OMNI3D_GAUGE_NONE;
+    p->seed_first_iteration = 1;
+    p->device = 0;
+}
+
+const char *omni3d_last_error(const omni3d_ctx *ctx) { return ctx ? ctx->err.c_str() : g_error.c_str(); }
+const char *omni3d_global_error(void) { return g_error.c_str(); }
+
+int omni3d_create(const omni3d_params *params, omni3d_ctx **out)
+{
+    if (!out) return fail(nullptr, OMNI3D_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    std::string why;
+    int rc = check_params(params, &why);
+    if (rc) return fail(nullptr, rc, why);
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return fail(nullptr, OMNI3D_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    if (params->device < 0 || params->device >= ndev) return fail(nullptr, OMNI3D_ERR_ARG, "device ordinal out of range");
+    e = cudaSetDevice(params->device);
+    if (e != cudaSuccess) return fail(nullptr, OMNI3D_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+
+    omni3d_ctx *ctx = new omni3d_ctx();
+    ctx->prm = *params;
+    ctx->dirs.assign(params->dirs, params->dirs + 3 * (size_t)params->n_dirs);
+    ctx->prm.dirs = ctx->dirs.data();
+    for (int d = 0; d < params->n_dirs; d++)
+        ctx->table.push_back(make_dir(ctx->dirs[3 * d], ctx->dirs[3 * d + 1], ctx->dirs[3 * d + 2]));
+
+    Grid &g = ctx->geo.grid;
+    g.X = params->nx;
+    g.Y = params->ny;
+    g.Z = params->nz;
+    g.XY = (long long)g.X * g.Y;
+    g.V = g.XY * g.Z;
+    g.cx = (float)((g.X - 1) / 2.0);
+    g.cy = (float)((g.Y - 1) / 2.0);
+    g.cz = (float)((g.Z - 1) / 2.0);
+    g.dx = params->dx;
+    g.dy = params->dy;
+    g.dz = params->dz;
+    g.rho = params->density;
+    g.ls = params->line_spacing;
+    g.thr = params->threshold;
+    int mx = std::max(std::max(g.X, g.Y), g.Z);
+    g.ng = (int)(mx * 1.732 / (double)params->line_spacing);  // K:6167
+    ctx->geo.nv = params->n_dirs;
+
+    auto bail = [&](cudaError_t ce, const char *what) {
+        int r = cuda_fail(ctx, ce, what);
+        g_error = ctx->err;
+        omni3d_destroy(ctx);
+        return r;
+    };
+    if ((e = cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "cudaStreamCreate");
+    ctx->own_stream = true;
+    for (auto &ev : ctx->ev)
+        if ((e = cudaEventCreate(&ev)) != cudaSuccess) return bail(e, "cudaEventCreate");
+    if ((e = cudaMalloc(&ctx->geo.d_dirs, sizeof(DirEntry) * ctx->table.size())) != cudaSuccess) return bail(e, "cudaMalloc dirs");
+    if ((e = cudaMemcpyAsync(ctx->geo.d_dirs, ctx->table.data(), sizeof(DirEntry) * ctx->table.size(),
+                             cudaMemcpyHostToDevice, ctx->st)) != cudaSuccess)
+        return bail(e, "upload dirs");
+    cudaEventRecord(ctx->ev[0], ctx->st);
+    std::string gerr;
+    e = build_geometry(&ctx->geo, ctx->st, &gerr);
+    if (e != cudaSuccess) {
+        ctx->err = "line tracing: " + gerr;
+        g_error = ctx->err;
+        int r = e == cudaErrorMemoryAllocation ? OMNI3D_ERR_NOMEM : OMNI3D_ERR_CUDA;
+        omni3d_destroy(ctx);
+        return r;
+    }
+    cudaEventRecord(ctx->ev[1], ctx->st);
+    cudaEventSynchronize(ctx->ev[1]);
+    ctx->ms_geometry = ms_between(ctx->ev[0], ctx->ev[1]);
+    *out = ctx;
+    return OMNI3D_OK;
+}
+
+int omni3d_destroy(omni3d_ctx *ctx)
+{
+    if (!ctx) return OMNI3D_OK;
+    cudaSetDevice(ctx->prm.device);
+    if (ctx->st) cudaStreamSynchronize(ctx->st);
+    free_geometry(&ctx->geo);
+    cudaFree(ctx->geo.d_dirs);
+    anchor_free(&ctx->anc);
+    for (DeviceBuf *b : {&ctx->in_ax, &ctx->in_ay, &ctx->in_az, &ctx->in_aux, &ctx->in_pinit, &ctx->f32, &ctx->b16,
+                         &ctx->curl, &ctx->pvol_a, &ctx->pvol_b, &ctx->pout, &ctx->cnt, &ctx->pncnt, &ctx->scratch})
+        b->release();
+    for (auto &ev : ctx->ev)
+        if (ev) cudaEventDestroy(ev);
+    if (ctx->own_stream && ctx->st) cudaStreamDestroy(ctx->st);
+    delete ctx;
+    return OMNI3D_OK;
+}
+
+int omni3d_set_stream(omni3d_ctx *ctx, void *stream)
+{
+    if (!ctx) return fail(nullptr, OMNI3D_ERR_ARG, "ctx is NULL");
+    cudaStreamSynchronize(ctx->st);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->st);
+    ctx->st = (cudaStream_t)stream;
+    ctx->own_stream = false;
+    return OMNI3D_OK;
+}
+
+int omni3d_geometry_info(omni3d_ctx *ctx, long long *n_lines, long long *n_units, long long *walk_errors)
+{
+    if (!ctx) return fail(nullptr, OMNI3D_ERR_ARG, "ctx is NULL");
+    if (n_lines) *n_lines = ctx->geo.n_lines;
+    if (n_units) *n_units = ctx->geo.n_units;
+    if (walk_errors) *walk_errors = ctx->geo.walk_errors;
+    return OMNI3D_OK;
+}
+
+int omni3d_line_table(omni3d_ctx *ctx, int32_t *rows, long long n_max)
+{
+    if (!ctx || !rows || n_max < 0) return fail(ctx, OMNI3D_ERR_ARG, "bad arguments");
+    long long n = std::min(n_max, ctx->geo.n_lines);
+    if (n == 0) return OMNI3D_OK;
+    cudaSetDevice(ctx->prm.device);
+    CK(ctx, cudaMemcpyAsync(rows, ctx->geo.d_lines, sizeof(LineRec) * (size_t)n, cudaMemcpyDeviceToHost, ctx->st));
+    CK(ctx, cudaStreamSynchronize(ctx->st));
+    return OMNI3D_OK;
+}
+
+int omni3d_line_steps(omni3d_ctx *ctx, long long line, int8_t *axes, int cap)
+{
+    if (!ctx || !axes || line < 0 || line >= ctx->geo.n_lines) return fail(ctx, OMNI3D_ERR_ARG, "bad arguments");
+    cudaSetDevice(ctx->prm.device);
+    LineRec r;
+    uint32_t gb;
+    CK(ctx, cudaMemcpyAsync(&r, ctx->geo.d_lines + line, sizeof(r), cudaMemcpyDeviceToHost, ctx->st));
+    CK(ctx, cudaMemcpyAsync(&gb, ctx->geo.d_gbase + (line >> 5), sizeof(gb), cudaMemcpyDeviceToHost, ctx->st));
+    CK(ctx, cudaStreamSynchronize(ctx->st));
+    if (r.m > cap) return fail(ctx, OMNI3D_ERR_RANGE, "cap smaller than the line's step count");
+    int nw = (r.m + 15) / 16;
+    std::vector<uint32_t> words((size_t)std::max(nw, 1));
+    for (int w = 0; w < nw; w++)
+        CK(ctx, cudaMemcpyAsync(&words[w], ctx->geo.d_desc + 32ull * gb + 32ull * w + (line & 31), sizeof(uint32_t),
+                                cudaMemcpyDeviceToHost, ctx->st));
+    CK(ctx, cudaStreamSynchronize(ctx->st));
+    for (int s = 0; s < r.m; s++) axes[s] = (int8_t)((words[s >> 4] >> (2 * (s & 15))) & 3u);
+    return r.m;
+}
+
+int omni3d_curl(omni3d_ctx *ctx, const float *ax, const float *ay, const float *az, const float *mask, float *curl_out,
+                int device_ptrs)
+{
+    if (!ctx || !ax || !ay || !az || !curl_out) return fail(ctx, OMNI3D_ERR_ARG, "NULL argument");
+    cudaSetDevice(ctx->prm.device);
+    const long long V = ctx->geo.grid.V;
+    const bool dev = device_ptrs != 0;
+    const float *dax, *day, *daz, *dmask;
+    int rc;
+    if ((rc = stage(ctx, ax, dev, ctx->in_ax, V, &dax))) return rc;
+    if ((rc = stage(ctx, ay, dev, ctx->in_ay, V, &day))) return rc;
+    if ((rc = stage(ctx, az, dev, ctx->in_az, V, &daz))) return rc;
+    if ((rc = stage(ctx, mask, dev, ctx->in_aux, V, &dmask))) return rc;
+    float *dout = curl_out;
+    if (!dev) {
+        CK(ctx, ctx->curl.ensure(sizeof(float) * (size_t)V));
+        dout = ctx->curl.as<float>();
+    }
+    CK(ctx, curl_field(ctx->geo.grid, dax, day, daz, dmask, dout, ctx->st));
+    if (!dev) CK(ctx, cudaMemcpyAsync(curl_out, dout, sizeof(float) * (size_t)V, cudaMemcpyDeviceToHost, ctx->st));
+    CK(ctx, cudaStreamSynchronize(ctx->st));
+    return OMNI3D_OK;
+}
+
+int omni3d_sweep(omni3d_ctx *ctx, const float *ax, const float *ay, const float *az, const float *curl, const float *p,
+                 float *pn, float *count, int device_ptrs)
+{
+    if (!ctx || !ax || !ay || !az || !p || !pn || !count) return fail(ctx, OMNI3D_ERR_ARG, "NULL argument");
+    if (ctx->prm.method == OMNI3D_METHOD_SELECT && !curl) return fail(ctx, OMNI3D_ERR_ARG, "select method needs curl");
+    cudaSetDevice(ctx->prm.device);
+    const long long V = ctx->geo.grid.V;
+    const bool dev = device_ptrs != 0;
+    Field F;
+    int rc = prepare_field(ctx, ax, ay, az, curl, nullptr, dev, &F);
+    if (rc) return rc;
+    const float *dp;
+    if ((rc = stage(ctx, p, dev, ctx->in_pinit, V, &dp))) return rc;
+    CK(ctx, ctx->pncnt.ensure(sizeof(float2) * (size_t)V));
+    float2 *acc = ctx->pncnt.as<float2>();
+    CK(ctx, init_accum(V, nullptr, false, acc, ctx->st));
+    CK(ctx, sweep_full(ctx->geo, F, ctx->prm.method, ctx->prm.grad_storage == OMNI3D_GRAD_BF16, dp, acc, ctx->st));
+    // add (pn, count) to the caller's arrays
+    float *dpn = pn, *dcount = count;
+    if (!dev) {
+        CK(ctx, ctx->pvol_a.ensure(sizeof(float) * (size_t)V));
+        CK(ctx, ctx->pvol_b.ensure(sizeof(float) * (size_t)V));
+        dpn = ctx->pvol_a.as<float>();
+        dcount = ctx->pvol_b.as<float>();
+        CK(ctx, cudaMemcpyAsync(dpn, pn, sizeof(float) * (size_t)V, cudaMemcpyHostToDevice, ctx->st));
+        CK(ctx, cudaMemcpyAsync(dcount, count, sizeof(float) * (size_t)V, cudaMemcpyHostToDevice, ctx->st));
+    }
+    CK(ctx, accum_split(V, acc, dpn, dcount, ctx->st));
+    if (!dev) {
+        CK(ctx, cudaMemcpyAsync(pn, dpn, sizeof(float) * (size_t)V, cudaMemcpyDeviceToHost, ctx->st));
+        CK(ctx, cudaMemcpyAsync(count, dcount, sizeof(float) * (size_t)V, cudaMemcpyDeviceToHost, ctx->st));
+    }
+    CK(ctx, cudaStreamSynchronize(ctx->st));
+    return OMNI3D_OK;
+}
+
+int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float *az, const float *curl,
+                 const float *mask, const float *p_init, float *p_out, float *count_out, int device_ptrs,
+                 omni3d_stats *stats)
+{
+    if (!ctx || !ax || !ay || !az || !p_out) return fail(ctx, OMNI3D_ERR_ARG, "NULL argument");
+    cudaSetDevice(ctx->prm.device);
+    const omni3d_params &P = ctx->prm;
+    const Grid &g = ctx->geo.grid;
+    const long long V = g.V;
+    const bool dev = device_ptrs != 0;
+    const bool bf16 = P.grad_storage == OMNI3D_GRAD_BF16;
+    cudaStream_t st = ctx->st;
+    long long ref = (long long)P.ref_i + (long long)P.ref_j * g.X + (long long)P.ref_k * g.XY;
+
+    const unsigned long long launches0 = __atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED);
+    cudaEventRecord(ctx->ev[0], st);
+    Field F;
+    int rc = prepare_field(ctx, ax, ay, az, curl, mask, dev, &F);
+    if (rc) return rc;
+    // initial pressure (zero when not given)
+    const float *dpinit;
+    if (p_init) {
+        if ((rc = stage(ctx, p_init, dev, ctx->in_pinit, V, &dpinit))) return rc;
+    } else {
+        CK(ctx, ctx->in_pinit.ensure(sizeof(float) * (size_t)V));
+        CK(ctx, cudaMemsetAsync(ctx->in_pinit.p, 0, sizeof(float) * (size_t)V, st));
+        dpinit = ctx->in_pinit.as<float>();
+    }
+    CK(ctx, ctx->pncnt.ensure(sizeof(float2) * (size_t)V));
+    CK(ctx, ctx->pout.ensure(sizeof(float) * (size_t)V));
+    CK(ctx, ctx->cnt.ensure(sizeof(float) * (size_t)V));
+    CK(ctx, ctx->pvol_a.ensure(sizeof(float) * (size_t)V));
+    CK(ctx, ctx->scratch.ensure(sizeof(double) * std::max(change_scratch_doubles(), gauge_scratch_doubles()) + 64));
+    float2 *acc = ctx->pncnt.as<float2>();
+    float *dout = ctx->pout.as<float>(), *dcnt = ctx->cnt.as<float>();
+    double *scratch = ctx->scratch.as<double>();
+    double *red2 = scratch;  // 2 doubles, then the reduction scratch
+    double *rscratch = scratch + 4;
+
+    const int K = P.max_iter;
+    const bool seed = P.seed_first_iteration != 0;
+    int done = 0;
+    double rel = 0.0;
+    double hred[2];
+    long long n_anchor = 0, n_links = 0;
+
+    if (K == 0) {
+        cudaEventRecord(ctx->ev[5], st);
+        cudaEventRecord(ctx->ev[6], st);
+        CK(ctx, cudaMemcpyAsync(dout, dpinit, sizeof(float) * (size_t)V, cudaMemcpyDeviceToDevice, st));
+        CK(ctx, cudaMemsetAsync(dcnt, 0, sizeof(float) * (size_t)V, st));
+        cudaEventRecord(ctx->ev[1], st);
+        cudaEventRecord(ctx->ev[2], st);
+    } else if (P.solver == OMNI3D_SOLVER_SWEEP) {
+        // the reference loop: NoItr x {sweep, devidecountInner}
+        CK(ctx, ctx->pvol_b.ensure(sizeof(float) * (size_t)V));
+        float *pc = ctx->pvol_a.as<float>(), *pn = ctx->pvol_b.as<float>();
+        CK(ctx, cudaMemcpyAsync(pc, dpinit, sizeof(float) * (size_t)V, cudaMemcpyDeviceToDevice, st));
+        cudaEventRecord(ctx->ev[1], st);
+        for (int it = 1; it <= K; it++) {
+            CK(ctx, init_accum(V, dpinit, seed && it == 1, acc, st));
+            cudaEventRecord(ctx->ev[5], st);
+            CK(ctx, sweep_full(ctx->geo, F, P.method, bf16, pc, acc, st));
+            cudaEventRecord(ctx->ev[6], st);
+            CK(ctx, normalize(V, acc, pc, pn, dcnt, st));
+            done = it;
+            if (P.tol > 0.0) {
+                CK(ctx, change_sums(V, pc, pn, P.gauge, P.gauge == OMNI3D_GAUGE_POINT ? ref : -1, rscratch, red2, st));
+                CK(ctx, cudaMemcpyAsync(hred, red2, sizeof(hred), cudaMemcpyDeviceToHost, st));
+                CK(ctx, cudaStreamSynchronize(st));
+                rel = hred[1] > 0 ? std::sqrt(hred[0] / hred[1]) : 0.0;
+            }
+            std::swap(pc, pn);
+            if (P.tol > 0.0 && rel < P.tol) break;
+        }
+        cudaEventRecord(ctx->ev[2], st);
+        CK(ctx, cudaMemcpyAsync(dout, pc, sizeof(float) * (size_t)V, cudaMemcpyDeviceToDevice, st));
+    } else {
+        // anchor form: iterate the anchors, then one full sweep
+        std::string aerr;
+        cudaError_t e = anchor_build(ctx->geo, F, P.method, bf16, P.gauge == OMNI3D_GAUGE_POINT ? ref : -1, &ctx->anc,
+                                     st, &aerr);
+        if (e != cudaSuccess) return fail(ctx, e == cudaErrorMemoryAllocation ? OMNI3D_ERR_NOMEM : OMNI3D_ERR_CUDA,
+                                          "anchor operator: " + aerr);
+        Anchor &A = ctx->anc;
+        n_anchor = A.n;
+        n_links = A.nnz;
+        long long ref_anchor = -1;
+        if (P.gauge == OMNI3D_GAUGE_POINT) {
+            int32_t ra = -1;
+            CK(ctx, cudaMemcpyAsync(&ra, A.id + ref, sizeof(ra), cudaMemcpyDeviceToHost, st));
+            CK(ctx, cudaStreamSynchronize(st));
+            ref_anchor = ra;
+        }
+        CK(ctx, anchor_gather(A, dpinit, A.pa, st));
+        cudaEventRecord(ctx->ev[1], st);
+        float *pc = A.pa, *pn = A.pb;
+        int its = 0;
+        for (int it = 1; it <= K - 1; it++) {
+            CK(ctx, anchor_step(A, dpinit, seed && it == 1, P.gauge, ref_anchor, pc, pn, P.tol > 0.0 ? red2 : nullptr, st));
+            its = it;
+            std::swap(pc, pn);
+            if (P.tol > 0.0) {
+                CK(ctx, cudaMemcpyAsync(hred, red2, sizeof(hred), cudaMemcpyDeviceToHost, st));
+                CK(ctx, cudaStreamSynchronize(st));
+                rel = hred[1] > 0 ? std::sqrt(hred[0] / hred[1]) : 0.0;
+                if (rel < P.tol) break;
+            }
+        }
+        cudaEventRecord(ctx->ev[2], st);
+        float *vol = ctx->pvol_a.as<float>();
+        CK(ctx, cudaMemcpyAsync(vol, dpinit, sizeof(float) * (size_t)V, cudaMemcpyDeviceToDevice, st));
+        CK(ctx, anchor_scatter(A, pc, vol, st));
+        CK(ctx, init_accum(V, dpinit, seed && its == 0, acc, st));
+        cudaEventRecord(ctx->ev[5], st);
+        CK(ctx, sweep_full(ctx->geo, F, P.method, bf16, vol, acc, st));
+        cudaEventRecord(ctx->ev[6], st);
+        CK(ctx, normalize(V, acc, dpinit, dout, dcnt, st));
+        done = its + 1;
+    }
+    CK(ctx, apply_gauge(V, P.gauge, ref, dcnt, dout, rscratch, st));
+    cudaEventRecord(ctx->ev[3], st);
+    if (dev) {
+        CK(ctx, cudaMemcpyAsync(p_out, dout, sizeof(float) * (size_t)V, cudaMemcpyDeviceToDevice, st));
+        if (count_out) CK(ctx, cudaMemcpyAsync(count_out, dcnt, sizeof(float) * (size_t)V, cudaMemcpyDeviceToDevice, st));
+    } else {
+        CK(ctx, cudaMemcpyAsync(p_out, dout, sizeof(float) * (size_t)V, cudaMemcpyDeviceToHost, st));
+        if (count_out) CK(ctx, cudaMemcpyAsync(count_out, dcnt, sizeof(float) * (size_t)V, cudaMemcpyDeviceToHost, st));
+    }
+    cudaEventRecord(ctx->ev[4], st);
+    CK(ctx, cudaStreamSynchronize(st));
+    CK(ctx, cudaGetLastError());
+    if (stats) {
+        stats->iterations = done;
+        stats->rel_change = rel;
+        stats->n_lines = ctx->geo.n_lines;
+        stats->n_units = ctx->geo.n_units;
+        stats->walk_errors = ctx->geo.walk_errors;
+        stats->n_anchors = n_anchor;
+        stats->n_links = n_links;
+        stats->ms_geometry = ctx->ms_geometry;
+        stats->ms_setup = ms_between(ctx->ev[0], ctx->ev[1]);
+        stats->ms_iterate = ms_between(ctx->ev[1], ctx->ev[2]);
+        stats->ms_final = ms_between(ctx->ev[2], ctx->ev[3]);
+        stats->ms_total = ms_between(ctx->ev[0], ctx->ev[4]);
+        stats->ms_sweep = ms_between(ctx->ev[5], ctx->ev[6]);
+        stats->kernel_launches = (long long)(__atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED) - launches0);
+    }
+    if (ctx->geo.walk_errors) return fail(ctx, OMNI3D_ERR_NUMERIC, "line walk hit the wrong-point branch");
+    return OMNI3D_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,523 @@
+// Anchor operator: the reference iteration restricted to the voxels whose values feed back.
+//
+// In one iteration of the reference (K:8840-8861) a voxel v receives, from every line
+// segment through it, w * (p[start] + I(v)) in pn and w in count (w = 1 for the plain
+// method; the start is the line entry, K:1760-1761; for the selected method the start is
+// the voxel where the segment began or restarted, K:2301-2411, and w = n / sum(curl/1e4)).
+// I(v) and w depend only on the gradient field, so
+//     p_new(v) = (b(v) + sum_j w_j p_old(start_j)) / c(v),  b = sum w I,  c = sum w.
+// Only the start voxels ("anchors") are ever read, so the iteration closes on the anchors:
+// iterate p_a <- (b_a + M p_a) / c_a on them alone, then evaluate every voxel once from
+// the final anchor values with one full sweep.  This gives the reference's iterate exactly
+// (up to the order of floating-point sums) at a fraction of the cost.
+//
+// The operator is built from the same line descriptors as the sweep: a marking pass finds
+// the anchors, a counting pass sizes each anchor's row, a filling pass writes
+// (column = start anchor, weight) pairs and accumulates b and c.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+
+#include "omni3d_internal.h"
+
+namespace omni3d {
+
+namespace {
+
+__device__ __forceinline__ float bf_lo(uint32_t u) { return __uint_as_float(u << 16); }
+__device__ __forceinline__ float bf_hi(uint32_t u) { return __uint_as_float(u & 0xffff0000u); }
+
+template <bool BF16>
+__device__ __forceinline__ float4 load_grad(const float4 *f32, const uint2 *b16, long long v)
+{
+    if (BF16) {
+        uint2 u = __ldg(b16 + v);
+        return make_float4(bf_lo(u.x), bf_hi(u.x), bf_lo(u.y), 0.0f);
+    }
+    return __ldg(f32 + v);
+}
+
+__device__ __forceinline__ float sel3(int a, float x, float y, float z)
+{
+    return a == 0 ? x : (a == 1 ? y : z);
+}
+
+__device__ __forceinline__ void kahan_add(float &s, float &c, float x)
+{
+    float y = x - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+__device__ __forceinline__ bool is_anchor(const uint32_t *bits, long long v)
+{
+    return (__ldg(bits + (v >> 5)) >> (v & 31)) & 1u;
+}
+
+enum Pass { kMark = 0, kCount = 1, kFill = 2 };
+
+struct Sink {
+    const uint32_t *bits;
+    const int32_t *id;
+    uint8_t *flag;
+    uint32_t *rowcnt;
+    const unsigned long long *rowptr;
+    uint32_t *cursor;
+    uint32_t *col;
+    float *w;
+    float *b;
+    float *c;
+};
+
+// Record one contribution of weight wt and integral I into voxel v from the segment that
+// started at voxel `start`.
+template <int PASS>
+__device__ __forceinline__ void emit(const Sink &S, long long v, long long start, float wt, float I)
+{
+    if (PASS == kMark) return;
+    if (!is_anchor(S.bits, v)) return;
+    int row = __ldg(S.id + v);
+    if (PASS == kCount) {
+        atomicAdd(S.rowcnt + row, 1u);
+    } else {
+        unsigned long long slot = S.rowptr[row] + atomicAdd(S.cursor + row, 1u);
+        S.col[slot] = (uint32_t)__ldg(S.id + start);
+        S.w[slot] = wt;
+        atomicAdd(S.b + row, wt * I);
+        atomicAdd(S.c + row, wt);
+    }
+}
+
+struct Walk {
+    long long v;
+    int d0, d1, d2;
+    float h0, h1, h2;
+    int m;
+    const uint32_t *dp;
+    __device__ __forceinline__ void init(const Grid &g, const LineRec &r, const uint32_t *gbase,
+                                         const uint32_t *desc, long long li)
+    {
+        int ie = (int)(r.e % (uint32_t)g.X), je = (int)((r.e / (uint32_t)g.X) % (uint32_t)g.Y),
+            ke = (int)(r.e / (uint32_t)g.XY);
+        int ix = (int)(r.x % (uint32_t)g.X), jx = (int)((r.x / (uint32_t)g.X) % (uint32_t)g.Y),
+            kx = (int)(r.x / (uint32_t)g.XY);
+        int si = ix > ie ? 1 : -1, sj = jx > je ? 1 : -1, sk = kx > ke ? 1 : -1;
+        d0 = si;
+        d1 = sj * g.X;
+        d2 = sk * (int)g.XY;
+        h0 = __fmul_rn(-g.rho * (float)si, g.dx) * 0.5f;
+        h1 = __fmul_rn(-g.rho * (float)sj, g.dy) * 0.5f;
+        h2 = __fmul_rn(-g.rho * (float)sk, g.dz) * 0.5f;
+        v = r.e;
+        m = r.m;
+        dp = desc + 32ull * gbase[li >> 5] + (li & 31);
+    }
+};
+
+// Plain method: anchors are the entries; every voxel of a line takes (p[entry] + I, 1).
+template <int PASS, bool BF16>
+__global__ void __launch_bounds__(256) k_anchor_plain(Grid g, const LineRec *__restrict__ lines,
+                                                      const uint32_t *__restrict__ gbase,
+                                                      const uint32_t *__restrict__ desc, long long n_lines,
+                                                      const float4 *__restrict__ f32,
+                                                      const uint2 *__restrict__ b16, Sink S)
+{
+    long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= n_lines) return;
+    LineRec r = lines[li];
+    if (PASS == kMark) {
+        S.flag[r.e] = 1;
+        return;
+    }
+    Walk L;
+    L.init(g, r, gbase, desc, li);
+    const long long e = r.e;
+    emit<PASS>(S, e, e, 1.0f, 0.0f);
+    float4 gl = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (PASS == kFill) gl = load_grad<BF16>(f32, b16, e);
+    float I = 0.0f, comp = 0.0f;
+    for (int s0 = 0; s0 < L.m; s0 += 16) {
+        uint32_t w = __ldg(L.dp + 32 * (s0 >> 4));
+        int n = min(16, L.m - s0);
+        for (int t = 0; t < n; t++, w >>= 2) {
+            int a = (int)(w & 3u);
+            L.v += a == 0 ? L.d0 : (a == 1 ? L.d1 : L.d2);
+            if (PASS == kFill) {
+                float4 gv = load_grad<BF16>(f32, b16, L.v);
+                kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
+                gl = gv;
+            }
+            emit<PASS>(S, L.v, e, 1.0f, I);
+        }
+    }
+}
+
+// Selected method: the state machine of k_sweep_select (K:2280-2537); anchors are the
+// segment starts.
+template <int PASS, bool BF16>
+__global__ void __launch_bounds__(256) k_anchor_select(Grid g, const LineRec *__restrict__ lines,
+                                                       const uint32_t *__restrict__ gbase,
+                                                       const uint32_t *__restrict__ desc, long long n_lines,
+                                                       const float4 *__restrict__ f32,
+                                                       const uint2 *__restrict__ b16,
+                                                       const float *__restrict__ curl, Sink S)
+{
+    long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= n_lines) return;
+    LineRec r = lines[li];
+    Walk L;
+    L.init(g, r, gbase, desc, li);
+    const float thr = g.thr;
+    float4 gl = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (PASS == kFill) gl = load_grad<BF16>(f32, b16, L.v);
+    float ce = __ldg(curl + L.v);
+    bool started = !(ce == 0.0f || ce > thr);
+    bool paused = false;
+    long long start = L.v;
+    if (PASS == kMark && started) S.flag[start] = 1;
+    float I = 0.0f, comp = 0.0f, csum = 0.0f, nseg = 0.0f;
+    for (int s0 = 0; s0 < L.m; s0 += 16) {
+        uint32_t w = __ldg(L.dp + 32 * (s0 >> 4));
+        int n = min(16, L.m - s0);
+        for (int t = 0; t < n; t++, w >>= 2) {
+            int a = (int)(w & 3u);
+            L.v += a == 0 ? L.d0 : (a == 1 ? L.d1 : L.d2);
+            float4 gv = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (PASS == kFill) gv = load_grad<BF16>(f32, b16, L.v);
+            float cn = __ldg(curl + L.v);
+            if (!started) {
+                bool ok = (a == 0) ? (cn != 0.0f && cn < thr) : (cn != 0.0f);
+                if (ok) {
+                    start = L.v;
+                    if (PASS == kMark) S.flag[start] = 1;
+                    started = true;
+                    I = 0.0f; comp = 0.0f; nseg = 0.0f; csum = 0.0f;
+                }
+            } else {
+                bool good = cn < thr && cn != 0.0f;
+                if (!paused && good) {
+                    if (PASS == kFill)
+                        kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
+                    csum += __fdiv_rn(cn, 10000.0f);
+                    nseg += 1.0f;
+                    emit<PASS>(S, L.v, start, __fdiv_rn(1.0f, csum) * nseg, I);
+                }
+                bool enter_bad = (a == 0) ? ((!paused && cn >= thr) || cn == 0.0f) : (!paused && cn >= thr);
+                if (enter_bad) paused = true;
+                if (paused && good) {
+                    start = L.v;
+                    if (PASS == kMark) S.flag[start] = 1;
+                    I = 0.0f; comp = 0.0f;
+                    paused = false;
+                    if (a != 2) { nseg = 0.0f; csum = 0.0f; }
+                }
+            }
+            gl = gv;
+        }
+    }
+}
+
+__global__ void k_flag_to_u32(long long V, const uint8_t *flag, uint32_t *out)
+{
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x)
+        out[v] = flag[v];
+}
+
+// id[v] = position among anchors or -1; vox[id] = v; bits = one bit per voxel.
+__global__ void k_assign_ids(long long V, const uint8_t *flag, const uint32_t *pos, int32_t *id, uint32_t *vox,
+                             uint32_t *bits)
+{
+    long long nthr = ((V + 31) / 32) * 32;
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < nthr;
+         v += (long long)gridDim.x * blockDim.x) {
+        bool f = v < V && flag[v];
+        unsigned b = __ballot_sync(0xffffffffu, f);
+        if (v < V) {
+            id[v] = f ? (int32_t)pos[v] : -1;
+            if (f) vox[pos[v]] = (uint32_t)v;
+        }
+        if ((threadIdx.x & 31) == 0) bits[v >> 5] = b;
+    }
+}
+
+__global__ void k_u32_to_u64(long long n, const uint32_t *in, unsigned long long *out)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = in[i];
+}
+
+// One anchor iteration, a warp per row.
+__global__ void __launch_bounds__(256) k_anchor_spmv(long long n, const unsigned long long *__restrict__ rowptr,
+                                                     const uint32_t *__restrict__ col, const float *__restrict__ w,
+                                                     const float *__restrict__ b, const float *__restrict__ c,
+                                                     const uint32_t *__restrict__ vox, const float *__restrict__ p_init,
+                                                     int seed, const float *__restrict__ pc, float *__restrict__ pn)
+{
+    long long row = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (row >= n) return;  // whole warps
+    unsigned long long j0 = rowptr[row], j1 = rowptr[row + 1];
+    float s = 0.0f;
+    for (unsigned long long j = j0 + lane; j < j1; j += 32) s += __ldg(w + j) * __ldg(pc + __ldg(col + j));
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+        float cc = c[row];
+        float numer = b[row] + s;
+        if (seed && p_init) numer += p_init[vox[row]];
+        pn[row] = cc > 0.0f ? __fdiv_rn(numer, cc) : pc[row];
+    }
+}
+
+constexpr int kRedBlocks = 256, kRedThreads = 256;
+
+__device__ __forceinline__ double block_sum(double x, double *sh)
+{
+    for (int o = 16; o; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = x;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += sh[i];
+    __syncthreads();
+    return s;
+}
+
+// Sums of (d, p) over the anchors (for the mean gauge).
+__global__ void k_sum_dp(long long n, const float *pc, const float *pn, double *part)
+{
+    __shared__ double sh[32];
+    double sd = 0.0, sp = 0.0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        sd += (double)pn[i] - (double)pc[i];
+        sp += (double)pn[i];
+    }
+    double a = block_sum(sd, sh), bb = block_sum(sp, sh);
+    if (threadIdx.x == 0) { part[2 * blockIdx.x] = a; part[2 * blockIdx.x + 1] = bb; }
+}
+
+__global__ void k_finish(const double *part, int nblk, int width, double *out, double scale)
+{
+    if ((int)threadIdx.x < width) {
+        double s = 0.0;
+        for (int i = 0; i < nblk; i++) s += part[width * i + threadIdx.x];
+        out[threadIdx.x] = s * scale;
+    }
+}
+
+// Gauged squared change and squared norm: sum (d - sd)^2, sum (p - sp)^2.  The shifts are
+// the reference anchor's change and value (point gauge), the means (mean gauge) or 0.
+__global__ void k_change(long long n, const float *pc, const float *pn, int gauge, long long ref,
+                         const double *means, double *part)
+{
+    __shared__ double sh[32];
+    double sd = 0.0, sp = 0.0;
+    if (gauge == OMNI3D_GAUGE_POINT && ref >= 0) {
+        sp = (double)pn[ref];
+        sd = sp - (double)pc[ref];
+    } else if (gauge == OMNI3D_GAUGE_MEAN) {
+        sd = means[0];
+        sp = means[1];
+    }
+    double a = 0.0, bb = 0.0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        double d = (double)pn[i] - (double)pc[i] - sd;
+        double q = (double)pn[i] - sp;
+        a += d * d;
+        bb += q * q;
+    }
+    double ta = block_sum(a, sh), tb = block_sum(bb, sh);
+    if (threadIdx.x == 0) { part[2 * blockIdx.x] = ta; part[2 * blockIdx.x + 1] = tb; }
+}
+
+__global__ void k_scatter(long long n, const uint32_t *vox, const float *pa, float *vol)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        vol[vox[i]] = pa[i];
+}
+
+__global__ void k_gather(long long n, const uint32_t *vox, const float *vol, float *pa)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        pa[i] = vol[vox[i]];
+}
+
+unsigned grid_for(long long n, int threads = 256)
+{
+    long long b = (n + threads - 1) / threads;
+    if (b > 152LL * 64) b = 152LL * 64;
+    if (b < 1) b = 1;
+    return (unsigned)b;
+}
+
+template <int PASS>
+cudaError_t run_pass(const Geometry &geo, const Field &f, int method, bool bf16, const Sink &S, cudaStream_t st)
+{
+    if (geo.n_lines == 0) return cudaSuccess;
+    unsigned blocks = (unsigned)((geo.n_lines + 255) / 256);
+    const Grid &g = geo.grid;
+    if (method == OMNI3D_METHOD_SELECT) {
+        if (bf16)
+            k_anchor_select<PASS, true><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
+                                                                f.f32, f.bf16, f.curl, S);
+        else
+            k_anchor_select<PASS, false><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
+                                                                 f.f32, f.bf16, f.curl, S);
+        OM_COUNT_LAUNCH();
+    } else {
+        if (bf16)
+            k_anchor_plain<PASS, true><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
+                                                               f.f32, f.bf16, S);
+        else
+            k_anchor_plain<PASS, false><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
+                                                                f.f32, f.bf16, S);
+        OM_COUNT_LAUNCH();
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+#define AN_TRY(x)                                                              \
+    do {                                                                       \
+        cudaError_t e_ = (x);                                                  \
+        if (e_ != cudaSuccess) {                                               \
+            if (err) *err = std::string(#x) + ": " + cudaGetErrorString(e_);   \
+            return e_;                                                         \
+        }                                                                      \
+    } while (0)
+
+void anchor_free(Anchor *A)
+{
+    cudaFree(A->flag); cudaFree(A->bits); cudaFree(A->id); cudaFree(A->vox); cudaFree(A->rowptr);
+    cudaFree(A->col); cudaFree(A->w); cudaFree(A->b); cudaFree(A->c); cudaFree(A->pa); cudaFree(A->pb);
+    cudaFree(A->red);
+    *A = Anchor();
+}
+
+cudaError_t anchor_build(const Geometry &geo, const Field &f, int method, bool bf16, long long ref_voxel,
+                         Anchor *A, cudaStream_t st, std::string *err)
+{
+    anchor_free(A);
+    const long long V = geo.grid.V;
+    AN_TRY(cudaMalloc(&A->flag, (size_t)V));
+    AN_TRY(cudaMalloc(&A->bits, sizeof(uint32_t) * (size_t)((V + 31) / 32)));
+    AN_TRY(cudaMalloc(&A->id, sizeof(int32_t) * (size_t)V));
+    AN_TRY(cudaMemsetAsync(A->flag, 0, (size_t)V, st));
+    Sink S{};
+    S.flag = A->flag;
+    AN_TRY(run_pass<kMark>(geo, f, method, bf16, S, st));
+    if (ref_voxel >= 0 && ref_voxel < V) AN_TRY(cudaMemsetAsync(A->flag + ref_voxel, 1, 1, st));
+
+    uint32_t *u = nullptr, *pos = nullptr, *tmp = nullptr;
+    AN_TRY(cudaMalloc(&u, sizeof(uint32_t) * (size_t)V));
+    AN_TRY(cudaMalloc(&pos, sizeof(uint32_t) * (size_t)(V + 1)));
+    AN_TRY(cudaMalloc(&tmp, sizeof(uint32_t) * scan_tmp_elems(V)));
+    k_flag_to_u32<<<grid_for(V), 256, 0, st>>>(V, A->flag, u);
+    OM_COUNT_LAUNCH();
+    AN_TRY(cudaGetLastError());
+    AN_TRY(exclusive_scan_u32(u, pos, V, tmp, st));
+    uint32_t n = 0;
+    AN_TRY(cudaMemcpyAsync(&n, pos + V, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    AN_TRY(cudaStreamSynchronize(st));
+    A->n = n;
+    AN_TRY(cudaMalloc(&A->vox, sizeof(uint32_t) * (size_t)std::max<long long>(n, 1)));
+    k_assign_ids<<<grid_for(V), 256, 0, st>>>(V, A->flag, pos, A->id, A->vox, A->bits);
+    OM_COUNT_LAUNCH();
+    AN_TRY(cudaGetLastError());
+
+    // rows
+    uint32_t *rowcnt = u;  // reuse: n <= V
+    AN_TRY(cudaMemsetAsync(rowcnt, 0, sizeof(uint32_t) * (size_t)std::max<long long>(n, 1), st));
+    S.bits = A->bits;
+    S.id = A->id;
+    S.rowcnt = rowcnt;
+    AN_TRY(run_pass<kCount>(geo, f, method, bf16, S, st));
+    unsigned long long *cnt64 = nullptr, *tmp64 = nullptr;
+    AN_TRY(cudaMalloc(&cnt64, sizeof(unsigned long long) * (size_t)std::max<long long>(n, 1)));
+    AN_TRY(cudaMalloc(&tmp64, sizeof(unsigned long long) * scan_tmp_elems(n)));
+    AN_TRY(cudaMalloc(&A->rowptr, sizeof(unsigned long long) * (size_t)(n + 1)));
+    k_u32_to_u64<<<grid_for(n), 256, 0, st>>>(n, rowcnt, cnt64);
+    OM_COUNT_LAUNCH();
+    AN_TRY(cudaGetLastError());
+    AN_TRY(exclusive_scan_u64(cnt64, A->rowptr, n, tmp64, st));
+    unsigned long long nnz = 0;
+    AN_TRY(cudaMemcpyAsync(&nnz, A->rowptr + n, sizeof(nnz), cudaMemcpyDeviceToHost, st));
+    AN_TRY(cudaStreamSynchronize(st));
+    A->nnz = (long long)nnz;
+    cudaFree(cnt64);
+    cudaFree(tmp64);
+    cudaFree(pos);
+    cudaFree(tmp);
+
+    AN_TRY(cudaMalloc(&A->col, sizeof(uint32_t) * (size_t)std::max<unsigned long long>(nnz, 1)));
+    AN_TRY(cudaMalloc(&A->w, sizeof(float) * (size_t)std::max<unsigned long long>(nnz, 1)));
+    AN_TRY(cudaMalloc(&A->b, sizeof(float) * (size_t)std::max<long long>(n, 1)));
+    AN_TRY(cudaMalloc(&A->c, sizeof(float) * (size_t)std::max<long long>(n, 1)));
+    AN_TRY(cudaMalloc(&A->pa, sizeof(float) * (size_t)std::max<long long>(n, 1)));
+    AN_TRY(cudaMalloc(&A->pb, sizeof(float) * (size_t)std::max<long long>(n, 1)));
+    AN_TRY(cudaMalloc(&A->red, sizeof(double) * (size_t)(8 + 2 * kRedBlocks)));
+    uint32_t *cursor = rowcnt;
+    AN_TRY(cudaMemsetAsync(cursor, 0, sizeof(uint32_t) * (size_t)std::max<long long>(n, 1), st));
+    AN_TRY(cudaMemsetAsync(A->b, 0, sizeof(float) * (size_t)std::max<long long>(n, 1), st));
+    AN_TRY(cudaMemsetAsync(A->c, 0, sizeof(float) * (size_t)std::max<long long>(n, 1), st));
+    S.rowptr = A->rowptr;
+    S.cursor = cursor;
+    S.col = A->col;
+    S.w = A->w;
+    S.b = A->b;
+    S.c = A->c;
+    AN_TRY(run_pass<kFill>(geo, f, method, bf16, S, st));
+    AN_TRY(cudaStreamSynchronize(st));
+    cudaFree(u);
+    return cudaSuccess;
+}
+
+size_t change_scratch_doubles() { return 8 + 2 * kRedBlocks; }
+
+cudaError_t change_sums(long long n, const float *pc, const float *pn, int gauge, long long ref, double *scratch,
+                        double *out2, cudaStream_t st)
+{
+    double *part = scratch + 8;
+    if (gauge == OMNI3D_GAUGE_MEAN) {
+        k_sum_dp<<<kRedBlocks, kRedThreads, 0, st>>>(n, pc, pn, part);
+        OM_COUNT_LAUNCH();
+        k_finish<<<1, 32, 0, st>>>(part, kRedBlocks, 2, scratch + 4, 1.0 / (double)std::max(n, 1LL));
+        OM_COUNT_LAUNCH();
+    }
+    k_change<<<kRedBlocks, kRedThreads, 0, st>>>(n, pc, pn, gauge, ref, scratch + 4, part);
+    OM_COUNT_LAUNCH();
+    k_finish<<<1, 32, 0, st>>>(part, kRedBlocks, 2, out2, 1.0);
+    OM_COUNT_LAUNCH();
+    return cudaGetLastError();
+}
+
+cudaError_t anchor_step(const Anchor &A, const float *p_init, bool seed, int gauge, long long ref_anchor,
+                        const float *p_cur, float *p_next, double *red2, cudaStream_t st)
+{
+    if (A.n == 0) return cudaSuccess;
+    long long threads = A.n * 32;
+    k_anchor_spmv<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(A.n, A.rowptr, A.col, A.w, A.b, A.c, A.vox,
+                                                                      p_init, seed ? 1 : 0, p_cur, p_next);
+    OM_COUNT_LAUNCH();
+    if (red2) return change_sums(A.n, p_cur, p_next, gauge, ref_anchor, A.red, red2, st);
+    return cudaGetLastError();
+}
+
+cudaError_t anchor_scatter(const Anchor &A, const float *pa, float *vol, cudaStream_t st)
+{
+    if (A.n == 0) return cudaSuccess;
+    k_scatter<<<grid_for(A.n), 256, 0, st>>>(A.n, A.vox, pa, vol);
+    OM_COUNT_LAUNCH();
+    return cudaGetLastError();
+}
+
+cudaError_t anchor_gather(const Anchor &A, const float *vol, float *pa, cudaStream_t st)
+{
+    if (A.n == 0) return cudaSuccess;
+    k_gather<<<grid_for(A.n), 256, 0, st>>>(A.n, A.vox, vol, pa);
+    OM_COUNT_LAUNCH();
+    return cudaGetLastError();
+}
+
+}  // namespace omni3d

@@ -1,0 +1,385 @@
+// Omni sweep over the traced lines: the accumulation half of bodyIntegralInner
+// (K:1743-1863) and bodyIntegralInnerSelect (K:2280-2537), the normalisation
+// devidecountInner (K:6746-6759), the curl indicator (K:8352-8378) and the gauge.
+//
+// One thread walks one line by decoding its 2-bit staircase; a warp holds 32 neighbouring
+// lines of one direction, whose step words are interleaved so that every word load is one
+// coalesced 128-byte transaction.  The gradient of each visited voxel is one 16-byte
+// (FP32) or 8-byte (BF16) gather; contributions go to an interleaved (pn, count) pair with
+// one vector reduction (red.global.add.v2.f32) per visited voxel.  The trapezoid prefix
+// integral along the line is a compensated (Kahan) FP32 sum.
+#include <cuda_bf16.h>
+
+#include "omni3d_internal.h"
+
+namespace omni3d {
+
+namespace {
+
+__device__ __forceinline__ float bf_lo(uint32_t u) { return __uint_as_float(u << 16); }
+__device__ __forceinline__ float bf_hi(uint32_t u) { return __uint_as_float(u & 0xffff0000u); }
+
+template <bool BF16>
+__device__ __forceinline__ float4 load_grad(const float4 *f32, const uint2 *b16, long long v)
+{
+    if (BF16) {
+        uint2 u = __ldg(b16 + v);
+        return make_float4(bf_lo(u.x), bf_hi(u.x), bf_lo(u.y), 0.0f);
+    } else {
+        return __ldg(f32 + v);
+    }
+}
+
+__device__ __forceinline__ float sel3(int a, float x, float y, float z)
+{
+    return a == 0 ? x : (a == 1 ? y : z);
+}
+
+// Per-line constants of the accumulation walk.
+struct LineWalk {
+    long long v;          // current voxel
+    int d0, d1, d2;       // signed strides of a step along x, y, z
+    float h0, h1, h2;     // -rho * sign * spacing / 2 per axis (K:1816, 1825, 1834)
+    int m;
+    const uint32_t *dp;   // this lane's first step word
+
+    __device__ __forceinline__ void init(const Grid &g, const LineRec &r, const uint32_t *gbase,
+                                         const uint32_t *desc, long long li)
+    {
+        int ie = (int)(r.e % (uint32_t)g.X), je = (int)((r.e / (uint32_t)g.X) % (uint32_t)g.Y),
+            ke = (int)(r.e / (uint32_t)g.XY);
+        int ix = (int)(r.x % (uint32_t)g.X), jx = (int)((r.x / (uint32_t)g.X) % (uint32_t)g.Y),
+            kx = (int)(r.x / (uint32_t)g.XY);
+        int si = ix > ie ? 1 : -1, sj = jx > je ? 1 : -1, sk = kx > ke ? 1 : -1;
+        d0 = si;
+        d1 = sj * g.X;
+        d2 = sk * (int)g.XY;
+        // the reference forms -rho*s*dl in float and halves it in double (exact)
+        h0 = __fmul_rn(-g.rho * (float)si, g.dx) * 0.5f;
+        h1 = __fmul_rn(-g.rho * (float)sj, g.dy) * 0.5f;
+        h2 = __fmul_rn(-g.rho * (float)sk, g.dz) * 0.5f;
+        v = r.e;
+        m = r.m;
+        dp = desc + 32ull * gbase[li >> 5] + (li & 31);
+    }
+};
+
+__device__ __forceinline__ void kahan_add(float &s, float &c, float x)
+{
+    float y = x - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+// Plain method: every voxel of the line, the entry included, receives p[entry] + I(v).
+template <bool BF16>
+__global__ void __launch_bounds__(256) k_sweep_plain(Grid g, const LineRec *__restrict__ lines,
+                                                     const uint32_t *__restrict__ gbase,
+                                                     const uint32_t *__restrict__ desc, long long n_lines,
+                                                     const float4 *__restrict__ f32,
+                                                     const uint2 *__restrict__ b16,
+                                                     const float *__restrict__ p, float2 *pncnt)
+{
+    long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= n_lines) return;
+    LineRec r = lines[li];
+    LineWalk L;
+    L.init(g, r, gbase, desc, li);
+    const float pe = __ldg(p + r.e);
+    atomicAdd(pncnt + r.e, make_float2(pe, 1.0f));
+    float4 gl = load_grad<BF16>(f32, b16, L.v);
+    float I = 0.0f, comp = 0.0f;
+    for (int s0 = 0; s0 < L.m; s0 += 16) {
+        uint32_t w = __ldg(L.dp + 32 * (s0 >> 4));
+        int n = min(16, L.m - s0);
+        for (int t = 0; t < n; t++, w >>= 2) {
+            int a = (int)(w & 3u);
+            L.v += a == 0 ? L.d0 : (a == 1 ? L.d1 : L.d2);
+            float4 gv = load_grad<BF16>(f32, b16, L.v);
+            float term = sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z));
+            kahan_add(I, comp, term);
+            atomicAdd(pncnt + L.v, make_float2(pe + I, 1.0f));
+            gl = gv;
+        }
+    }
+}
+
+// Selected method (K:2280-2537), state machine and asymmetries included: the entry is a
+// segment start when 0 < curl <= thr; before the first start an x step needs
+// 0 < curl < thr, a y/z step only curl != 0; a bad voxel pauses the segment (an x step
+// also pauses on curl == 0, a y/z step walks through it without adding that step's
+// increment); a good voxel after a pause restarts the segment at that voxel; the z
+// branch keeps the running curl/count sums on restart.
+template <bool BF16>
+__global__ void __launch_bounds__(256) k_sweep_select(Grid g, const LineRec *__restrict__ lines,
+                                                      const uint32_t *__restrict__ gbase,
+                                                      const uint32_t *__restrict__ desc, long long n_lines,
+                                                      const float4 *__restrict__ f32,
+                                                      const uint2 *__restrict__ b16,
+                                                      const float *__restrict__ curl,
+                                                      const float *__restrict__ p, float2 *pncnt)
+{
+    long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= n_lines) return;
+    LineRec r = lines[li];
+    LineWalk L;
+    L.init(g, r, gbase, desc, li);
+    const float thr = g.thr;
+    float4 gl = load_grad<BF16>(f32, b16, L.v);
+    float ce = BF16 ? __ldg(curl + L.v) : gl.w;
+    bool started = !(ce == 0.0f || ce > thr);
+    bool paused = false;
+    float p0 = started ? __ldg(p + L.v) : 0.0f;
+    float I = 0.0f, comp = 0.0f, csum = 0.0f, nseg = 0.0f;
+    for (int s0 = 0; s0 < L.m; s0 += 16) {
+        uint32_t w = __ldg(L.dp + 32 * (s0 >> 4));
+        int n = min(16, L.m - s0);
+        for (int t = 0; t < n; t++, w >>= 2) {
+            int a = (int)(w & 3u);
+            L.v += a == 0 ? L.d0 : (a == 1 ? L.d1 : L.d2);
+            float4 gv = load_grad<BF16>(f32, b16, L.v);
+            float cn = BF16 ? __ldg(curl + L.v) : gv.w;
+            if (!started) {
+                bool ok = (a == 0) ? (cn != 0.0f && cn < thr) : (cn != 0.0f);
+                if (ok) {
+                    p0 = __ldg(p + L.v);
+                    started = true;
+                    I = 0.0f; comp = 0.0f; nseg = 0.0f; csum = 0.0f;
+                }
+            } else {
+                bool good = cn < thr && cn != 0.0f;
+                if (!paused && good) {
+                    float term = sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z));
+                    kahan_add(I, comp, term);
+                    csum += __fdiv_rn(cn, 10000.0f);
+                    nseg += 1.0f;
+                    float wp = __fdiv_rn(p0 + I, csum) * nseg;
+                    float wc = __fdiv_rn(1.0f, csum) * nseg;
+                    atomicAdd(pncnt + L.v, make_float2(wp, wc));
+                }
+                bool enter_bad = (a == 0) ? ((!paused && cn >= thr) || cn == 0.0f) : (!paused && cn >= thr);
+                if (enter_bad) paused = true;
+                if (paused && good) {
+                    p0 = __ldg(p + L.v);
+                    I = 0.0f; comp = 0.0f;
+                    paused = false;
+                    if (a != 2) { nseg = 0.0f; csum = 0.0f; }
+                }
+            }
+            gl = gv;
+        }
+    }
+}
+
+__global__ void k_normalize(long long V, const float2 *__restrict__ pncnt, const float *__restrict__ p_keep,
+                            float *p_out, float *cnt_out)
+{
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < V;
+         v += (long long)gridDim.x * blockDim.x) {
+        float2 a = pncnt[v];
+        float pk = p_keep ? p_keep[v] : 0.0f;
+        if (p_out) p_out[v] = a.y > 0.0f ? __fdiv_rn(a.x, a.y) : pk;
+        if (cnt_out) cnt_out[v] = a.y;
+    }
+}
+
+__global__ void k_accum_split(long long V, const float2 *__restrict__ acc, float *pn, float *cnt)
+{
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < V;
+         v += (long long)gridDim.x * blockDim.x) {
+        float2 a = acc[v];
+        pn[v] += a.x;
+        cnt[v] += a.y;
+    }
+}
+
+__global__ void k_init_accum(long long V, const float *__restrict__ p_init, int seed, float2 *pncnt)
+{
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < V;
+         v += (long long)gridDim.x * blockDim.x)
+        pncnt[v] = make_float2(seed && p_init ? p_init[v] : 0.0f, 0.0f);
+}
+
+__device__ __forceinline__ uint32_t to_bf16(float x)
+{
+    return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(x));
+}
+
+__global__ void k_pack(long long V, const float *__restrict__ ax, const float *__restrict__ ay,
+                       const float *__restrict__ az, const float *__restrict__ curl, float4 *f32,
+                       uint2 *b16)
+{
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < V;
+         v += (long long)gridDim.x * blockDim.x) {
+        float x = ax[v], y = ay[v], z = az[v];
+        f32[v] = make_float4(x, y, z, curl ? curl[v] : 0.0f);
+        if (b16) b16[v] = make_uint2(to_bf16(x) | (to_bf16(y) << 16), to_bf16(z));
+    }
+}
+
+// |curl a| x mask with the reference's stencil and evaluation order (K:8352-8378).
+__global__ void k_curl(Grid g, const float *__restrict__ au, const float *__restrict__ av,
+                       const float *__restrict__ aw, const float *__restrict__ mask, float *out)
+{
+    const long long X = g.X, Y = g.Y, Z = g.Z, XY = g.XY;
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < g.V;
+         v += (long long)gridDim.x * blockDim.x) {
+        long long i = v % X, j = (v / X) % Y, k = v / XY;
+        long long i0 = i - 1 >= 0 ? i - 1 : i, j0 = j - 1 >= 0 ? j - 1 : j, k0 = k - 1 >= 0 ? k - 1 : k;
+        long long ie = i + 1 <= X - 1 ? i + 1 : i, je = j + 1 <= Y - 1 ? j + 1 : j, ke = k + 1 <= Z - 1 ? k + 1 : k;
+        float dj = (float)(je - j0), dk = (float)(ke - k0), di = (float)(ie - i0);
+        float cx = __fdiv_rn(__fdiv_rn(__fsub_rn(aw[i + je * X + k * XY], aw[i + j0 * X + k * XY]), dj), g.dy);
+        cx = __fadd_rn(cx, __fdiv_rn(__fdiv_rn(-__fsub_rn(av[i + j * X + ke * XY], av[i + j * X + k0 * XY]), dk), g.dz));
+        float cy = __fdiv_rn(__fdiv_rn(-__fsub_rn(aw[ie + j * X + k * XY], aw[i0 + j * X + k * XY]), di), g.dx);
+        cy = __fadd_rn(cy, __fdiv_rn(__fdiv_rn(__fsub_rn(au[i + j * X + ke * XY], au[i + j * X + k0 * XY]), dk), g.dz));
+        float cz = __fdiv_rn(__fdiv_rn(__fsub_rn(av[ie + j * X + k * XY], av[i0 + j * X + k * XY]), di), g.dx);
+        cz = __fadd_rn(cz, __fdiv_rn(__fdiv_rn(-__fsub_rn(au[i + je * X + k * XY], au[i + j0 * X + k * XY]), dj), g.dy));
+        float s = __fadd_rn(__fadd_rn(__fmul_rn(cx, cx), __fmul_rn(cy, cy)), __fmul_rn(cz, cz));
+        out[v] = __fmul_rn(__fsqrt_rn(s), mask ? mask[v] : 1.0f);
+    }
+}
+
+// Deterministic FP64 sums: fixed grid, per-block partials, one block adds them in order.
+constexpr int kRedBlocks = 256, kRedThreads = 256;
+
+__device__ __forceinline__ double block_sum(double x, double *sh)
+{
+    for (int o = 16; o; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = x;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += sh[w];
+    __syncthreads();
+    return s;
+}
+
+__global__ void k_masked_sum(long long V, const float *__restrict__ p, const float *__restrict__ cnt,
+                             double *part)
+{
+    __shared__ double sh[32];
+    double s = 0.0, n = 0.0;
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < V;
+         v += (long long)gridDim.x * blockDim.x) {
+        if (cnt[v] > 0.0f) { s += (double)p[v]; n += 1.0; }
+    }
+    double bs = block_sum(s, sh);
+    double bn = block_sum(n, sh);
+    if (threadIdx.x == 0) { part[2 * blockIdx.x] = bs; part[2 * blockIdx.x + 1] = bn; }
+}
+
+__global__ void k_finish_sums(const double *part, int nblk, int width, double *out)
+{
+    if (threadIdx.x < width) {
+        double s = 0.0;
+        for (int b = 0; b < nblk; b++) s += part[width * b + threadIdx.x];
+        out[threadIdx.x] = s;
+    }
+}
+
+// p -= sums[0] / sums[1] (the mean, or the reference value with sums[1] = 1).
+__global__ void k_shift(long long V, const double *sums, float *p)
+{
+    const double sub = sums[1] > 0 ? sums[0] / sums[1] : 0.0;
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < V;
+         v += (long long)gridDim.x * blockDim.x)
+        p[v] = (float)((double)p[v] - sub);
+}
+
+__global__ void k_read_point(const float *p, long long ref, double *out) { out[0] = (double)p[ref]; out[1] = 1.0; }
+
+unsigned grid_for(long long n, int threads = 256)
+{
+    long long b = (n + threads - 1) / threads;
+    if (b > 152LL * 64) b = 152LL * 64;
+    if (b < 1) b = 1;
+    return (unsigned)b;
+}
+
+}  // namespace
+
+cudaError_t sweep_full(const Geometry &geo, const Field &f, int method, bool bf16, const float *p,
+                       float2 *pncnt, cudaStream_t st)
+{
+    if (geo.n_lines == 0) return cudaSuccess;
+    unsigned blocks = (unsigned)((geo.n_lines + 255) / 256);
+    if (method == OMNI3D_METHOD_SELECT) {
+        if (bf16)
+            k_sweep_select<true><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
+                                                         f.f32, f.bf16, f.curl, p, pncnt);
+        else
+            k_sweep_select<false><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
+                                                          f.f32, f.bf16, f.curl, p, pncnt);
+        OM_COUNT_LAUNCH();
+    } else {
+        if (bf16)
+            k_sweep_plain<true><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
+                                                        f.f32, f.bf16, p, pncnt);
+        else
+            k_sweep_plain<false><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
+                                                         f.f32, f.bf16, p, pncnt);
+        OM_COUNT_LAUNCH();
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t normalize(long long V, const float2 *pncnt, const float *p_keep, float *p_out, float *cnt_out,
+                      cudaStream_t st)
+{
+    k_normalize<<<grid_for(V), 256, 0, st>>>(V, pncnt, p_keep, p_out, cnt_out);
+    OM_COUNT_LAUNCH();
+    return cudaGetLastError();
+}
+
+cudaError_t accum_split(long long V, const float2 *acc, float *pn, float *cnt, cudaStream_t st)
+{
+    k_accum_split<<<grid_for(V), 256, 0, st>>>(V, acc, pn, cnt);
+    OM_COUNT_LAUNCH();
+    return cudaGetLastError();
+}
+
+cudaError_t init_accum(long long V, const float *p_init, bool seed, float2 *pncnt, cudaStream_t st)
+{
+    k_init_accum<<<grid_for(V), 256, 0, st>>>(V, p_init, seed ? 1 : 0, pncnt);
+    OM_COUNT_LAUNCH();
+    return cudaGetLastError();
+}
+
+cudaError_t pack_field(const Grid &g, const float *ax, const float *ay, const float *az, const float *curl,
+                       Field *f, bool make_bf16, cudaStream_t st)
+{
+    k_pack<<<grid_for(g.V), 256, 0, st>>>(g.V, ax, ay, az, curl, f->f32, make_bf16 ? f->bf16 : nullptr);
+    OM_COUNT_LAUNCH();
+    return cudaGetLastError();
+}
+
+cudaError_t curl_field(const Grid &g, const float *ax, const float *ay, const float *az, const float *mask,
+                       float *out, cudaStream_t st)
+{
+    k_curl<<<grid_for(g.V), 256, 0, st>>>(g, ax, ay, az, mask, out);
+    OM_COUNT_LAUNCH();
+    return cudaGetLastError();
+}
+
+cudaError_t apply_gauge(long long V, int gauge, long long ref, const float *cnt, float *p, double *scratch,
+                        cudaStream_t st)
+{
+    if (gauge == OMNI3D_GAUGE_NONE) return cudaSuccess;
+    if (gauge == OMNI3D_GAUGE_MEAN) {
+        k_masked_sum<<<kRedBlocks, kRedThreads, 0, st>>>(V, p, cnt, scratch + 2);
+        OM_COUNT_LAUNCH();
+        k_finish_sums<<<1, 32, 0, st>>>(scratch + 2, kRedBlocks, 2, scratch);
+        OM_COUNT_LAUNCH();
+    } else {
+        k_read_point<<<1, 1, 0, st>>>(p, ref, scratch);
+        OM_COUNT_LAUNCH();
+    }
+    k_shift<<<grid_for(V), 256, 0, st>>>(V, scratch, p);
+    OM_COUNT_LAUNCH();
+    return cudaGetLastError();
+}
+
+size_t gauge_scratch_doubles() { return 2 + 2 * kRedBlocks; }
+
+}  // namespace omni3d

@@ -1,0 +1,342 @@
+// Line tracing: every (direction, lattice point) pair -> line records -> staircase step
+// descriptors.  Replaces the per-thread line setup at the top of the reference's omni
+// kernels (K:6153-6206) and the walk of bodyIntegralInner (K:1762-1861), done once per
+// geometry instead of once per line per iteration.
+#include <algorithm>
+#include <cstdio>
+#include <vector>
+
+#include "geometry.cuh"
+#include "omni3d_internal.h"
+
+namespace omni3d {
+
+namespace {
+
+constexpr int kTraceBlock = 256;
+constexpr int kScanBlock = 1024;
+constexpr int kScanItems = 4;  // items per thread
+constexpr long long kScanTile = (long long)kScanBlock * kScanItems;
+
+__device__ __forceinline__ bool trace_candidate(const Grid &g, const DirEntry *dirs, long long ng2,
+                                                long long c, int in[3], int out[3], float o[3],
+                                                int *dir)
+{
+    int d = (int)(c / ng2);
+    long long pt = c - (long long)d * ng2;
+    DirEntry D = dirs[d];
+    om_line_offset(pt, g.ng, g.ls, D, o[0], o[1], o[2]);
+    om_cross2point(g, o[0], o[1], o[2], D.k1, D.k2, D.k3, D.cas, in, out);
+    *dir = d;
+    return om_line_valid(g, in, out);
+}
+
+// Pass 1: number of valid lines per block of candidates.
+__global__ void __launch_bounds__(kTraceBlock) k_trace_count(Grid g, const DirEntry *dirs,
+                                                             long long ncand, long long ng2,
+                                                             uint32_t *blk_cnt)
+{
+    __shared__ uint32_t warp_cnt[kTraceBlock / 32];
+    long long c = (long long)blockIdx.x * kTraceBlock + threadIdx.x;
+    bool valid = false;
+    if (c < ncand) {
+        int in[3], out[3], d;
+        float o[3];
+        valid = trace_candidate(g, dirs, ng2, c, in, out, o, &d);
+    }
+    unsigned b = __ballot_sync(0xffffffffu, valid);
+    if ((threadIdx.x & 31) == 0) warp_cnt[threadIdx.x >> 5] = __popc(b);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t s = 0;
+        for (int w = 0; w < kTraceBlock / 32; w++) s += warp_cnt[w];
+        blk_cnt[blockIdx.x] = s;
+    }
+}
+
+// Pass 2: write the valid lines of each block at its offset, in candidate order.
+__global__ void __launch_bounds__(kTraceBlock) k_trace_emit(Grid g, const DirEntry *dirs,
+                                                            long long ncand, long long ng2,
+                                                            const uint32_t *blk_off,
+                                                            LineRec *lines, float4 *off)
+{
+    __shared__ uint32_t warp_cnt[kTraceBlock / 32];
+    long long c = (long long)blockIdx.x * kTraceBlock + threadIdx.x;
+    bool valid = false;
+    int in[3], out[3], d = 0;
+    float o[3];
+    if (c < ncand) valid = trace_candidate(g, dirs, ng2, c, in, out, o, &d);
+    unsigned b = __ballot_sync(0xffffffffu, valid);
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) warp_cnt[warp] = __popc(b);
+    __syncthreads();
+    if (!valid) return;
+    uint32_t base = blk_off[blockIdx.x];
+    for (int w = 0; w < warp; w++) base += warp_cnt[w];
+    base += __popc(b & ((1u << lane) - 1u));
+    LineRec r;
+    r.e = (uint32_t)(in[0] + (long long)in[1] * g.X + (long long)in[2] * g.XY);
+    r.x = (uint32_t)(out[0] + (long long)out[1] * g.X + (long long)out[2] * g.XY);
+    r.dir = d;
+    r.m = abs(out[0] - in[0]) + abs(out[1] - in[1]) + abs(out[2] - in[2]);
+    lines[base] = r;
+    off[base] = make_float4(o[0], o[1], o[2], 0.0f);
+}
+
+// Words per lane of every group of 32 lines: ceil(max steps / 16).
+__global__ void k_group_words(const LineRec *lines, long long n_lines, long long n_groups,
+                              uint32_t *gw)
+{
+    long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if ((li >> 5) >= n_groups) return;  // whole warps only (blockDim is a multiple of 32)
+    int m = li < n_lines ? lines[li].m : 0;
+    int mx = __reduce_max_sync(0xffffffffu, m);
+    if ((threadIdx.x & 31) == 0) gw[li >> 5] = (uint32_t)((mx + 15) >> 4);
+}
+
+// Walk every line once (K:1762-1861) and store its staircase, 2 bits per step.
+__global__ void __launch_bounds__(256) k_walk(Grid g, const DirEntry *dirs, LineRec *lines,
+                                              const float4 *off, const uint32_t *gbase,
+                                              uint32_t *desc, long long n_lines,
+                                              unsigned long long *counters)
+{
+    long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned mask = __ballot_sync(0xffffffffu, li < n_lines);
+    if (li >= n_lines) return;  // the tail of the last warp only
+    LineRec r = lines[li];
+    float4 o = off[li];
+    DirEntry D = dirs[r.dir];
+    int ie = (int)(r.e % g.X), je = (int)((r.e / g.X) % g.Y), ke = (int)(r.e / g.XY);
+    int ix = (int)(r.x % g.X), jx = (int)((r.x / g.X) % g.Y), kx = (int)(r.x / g.XY);
+    OmWalker w;
+    w.init(g, o.x, o.y, o.z, D.k1, D.k2, D.k3, ie, je, ke, ix, jx, kx);
+    uint32_t *dp = desc + 32ull * gbase[li >> 5] + (li & 31);
+    uint32_t word = 0;
+    int s = 0;
+    for (; s < r.m; s++) {
+        int a = w.step();
+        if (a < 0) break;
+        word |= (uint32_t)a << (2 * (s & 15));
+        if ((s & 15) == 15) { dp[32 * (s >> 4)] = word; word = 0; }
+    }
+    if (s & 15) dp[32 * (s >> 4)] = word;
+    if (s != r.m) {
+        lines[li].m = s;  // the reference keeps the contributions of the steps taken
+        atomicAdd(&counters[0], 1ull);
+    }
+    // voxel-direction updates: entry + one per step
+    unsigned u = __reduce_add_sync(mask, (unsigned)(s + 1));
+    if ((threadIdx.x & 31) == (__ffs(mask) - 1)) atomicAdd(&counters[1], (unsigned long long)u);
+}
+
+// ---------------------------------------------------------------- scan
+template <typename T>
+__device__ __forceinline__ T block_exclusive_scan(T v, T *sh, T *total)
+{
+    // sh: kScanBlock / 32 + 1 entries
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    T x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        T y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sh[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        T s = lane < kScanBlock / 32 ? sh[lane] : T(0);
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            T y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < kScanBlock / 32) sh[lane] = s;
+    }
+    __syncthreads();
+    T warp_excl = warp ? sh[warp - 1] : T(0);
+    if (total) *total = sh[kScanBlock / 32 - 1];
+    __syncthreads();
+    return warp_excl + x - v;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kScanBlock) k_scan_reduce(const T *in, long long n, T *part)
+{
+    __shared__ T sh[kScanBlock / 32 + 1];
+    long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems;
+    T s = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++)
+        if (base + i < n) s += in[base + i];
+    T tot;
+    block_exclusive_scan<T>(s, sh, &tot);
+    if (threadIdx.x == 0) part[blockIdx.x] = tot;
+}
+
+// Scan of the partial sums in one block (sequential over tiles of kScanBlock items).
+template <typename T>
+__global__ void __launch_bounds__(kScanBlock) k_scan_partials(T *part, long long np)
+{
+    __shared__ T sh[kScanBlock / 32 + 1];
+    T carry = 0;
+    for (long long t0 = 0; t0 < np; t0 += kScanBlock) {
+        long long i = t0 + threadIdx.x;
+        T v = i < np ? part[i] : T(0);
+        T tot;
+        T ex = block_exclusive_scan<T>(v, sh, &tot);
+        if (i < np) part[i] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) part[np] = carry;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kScanBlock) k_scan_apply(const T *in, long long n, const T *part,
+                                                           T *out)
+{
+    __shared__ T sh[kScanBlock / 32 + 1];
+    long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems;
+    T v[kScanItems];
+    T s = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++) {
+        v[i] = base + i < n ? in[base + i] : T(0);
+        s += v[i];
+    }
+    T ex = block_exclusive_scan<T>(s, sh, nullptr) + part[blockIdx.x];
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++) {
+        if (base + i < n) out[base + i] = ex;
+        ex += v[i];
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = part[gridDim.x];
+}
+
+template <typename T>
+cudaError_t exclusive_scan(const T *in, T *out, long long n, T *tmp, cudaStream_t st)
+{
+    long long nb = (n + kScanTile - 1) / kScanTile;
+    if (nb == 0) {
+        return cudaMemsetAsync(out, 0, sizeof(T), st);
+    }
+    k_scan_reduce<T><<<(unsigned)nb, kScanBlock, 0, st>>>(in, n, tmp);
+    OM_COUNT_LAUNCH();
+    k_scan_partials<T><<<1, kScanBlock, 0, st>>>(tmp, nb);
+    OM_COUNT_LAUNCH();
+    k_scan_apply<T><<<(unsigned)nb, kScanBlock, 0, st>>>(in, n, tmp, out);
+    OM_COUNT_LAUNCH();
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t scan_tmp_elems(long long n) { return (size_t)((n + kScanTile - 1) / kScanTile) + 2; }
+
+cudaError_t exclusive_scan_u32(const uint32_t *in, uint32_t *out, long long n, uint32_t *tmp,
+                               cudaStream_t st)
+{
+    return exclusive_scan<uint32_t>(in, out, n, tmp, st);
+}
+cudaError_t exclusive_scan_u64(const unsigned long long *in, unsigned long long *out, long long n,
+                               unsigned long long *tmp, cudaStream_t st)
+{
+    return exclusive_scan<unsigned long long>(in, out, n, tmp, st);
+}
+
+#define OM_TRY(x)                                                         \
+    do {                                                                  \
+        cudaError_t e_ = (x);                                             \
+        if (e_ != cudaSuccess) {                                          \
+            if (err) *err = std::string(#x) + ": " + cudaGetErrorString(e_); \
+            return e_;                                                    \
+        }                                                                 \
+    } while (0)
+
+void free_geometry(Geometry *g)
+{
+    cudaFree(g->d_off);
+    cudaFree(g->d_lines);
+    cudaFree(g->d_gbase);
+    cudaFree(g->d_desc);
+    g->d_off = nullptr;
+    g->d_lines = nullptr;
+    g->d_gbase = nullptr;
+    g->d_desc = nullptr;
+    g->n_lines = g->n_groups = g->n_words = g->n_units = g->walk_errors = 0;
+}
+
+cudaError_t build_geometry(Geometry *g, cudaStream_t st, std::string *err)
+{
+    const Grid &G = g->grid;
+    long long ng2 = (long long)G.ng * G.ng;
+    long long ncand = ng2 * g->nv;
+    long long nblk = (ncand + kTraceBlock - 1) / kTraceBlock;
+    if (nblk > 0x7fffffffLL) {
+        if (err) *err = "too many lattice candidates";
+        return cudaErrorInvalidValue;
+    }
+    uint32_t *blk = nullptr, *tmp = nullptr;
+    OM_TRY(cudaMalloc(&blk, sizeof(uint32_t) * (size_t)(2 * nblk + 1)));
+    OM_TRY(cudaMalloc(&tmp, sizeof(uint32_t) * scan_tmp_elems(nblk)));
+    uint32_t *blk_off = blk + nblk;
+    k_trace_count<<<(unsigned)nblk, kTraceBlock, 0, st>>>(G, g->d_dirs, ncand, ng2, blk);
+    OM_COUNT_LAUNCH();
+    OM_TRY(cudaGetLastError());
+    OM_TRY(exclusive_scan_u32(blk, blk_off, nblk, tmp, st));
+    uint32_t total = 0;
+    OM_TRY(cudaMemcpyAsync(&total, blk_off + nblk, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    OM_TRY(cudaStreamSynchronize(st));
+    g->n_lines = total;
+    g->n_groups = (total + 31) / 32;
+    if (total == 0) {
+        cudaFree(blk);
+        cudaFree(tmp);
+        g->n_words = 0;
+        g->n_units = 0;
+        return cudaSuccess;
+    }
+    OM_TRY(cudaMalloc(&g->d_lines, sizeof(LineRec) * (size_t)total));
+    OM_TRY(cudaMalloc(&g->d_off, sizeof(float4) * (size_t)total));
+    k_trace_emit<<<(unsigned)nblk, kTraceBlock, 0, st>>>(G, g->d_dirs, ncand, ng2, blk_off, g->d_lines,
+                                                         g->d_off);
+    OM_COUNT_LAUNCH();
+    OM_TRY(cudaGetLastError());
+    cudaFree(blk);
+    cudaFree(tmp);
+
+    // words per group -> prefix offsets
+    uint32_t *gw = nullptr, *gtmp = nullptr;
+    OM_TRY(cudaMalloc(&gw, sizeof(uint32_t) * (size_t)g->n_groups));
+    OM_TRY(cudaMalloc(&g->d_gbase, sizeof(uint32_t) * (size_t)(g->n_groups + 1)));
+    OM_TRY(cudaMalloc(&gtmp, sizeof(uint32_t) * scan_tmp_elems(g->n_groups)));
+    long long nthr = g->n_groups * 32;
+    k_group_words<<<(unsigned)((nthr + 255) / 256), 256, 0, st>>>(g->d_lines, g->n_lines, g->n_groups, gw);
+    OM_COUNT_LAUNCH();
+    OM_TRY(cudaGetLastError());
+    OM_TRY(exclusive_scan_u32(gw, g->d_gbase, g->n_groups, gtmp, st));
+    uint32_t words_per_lane_total = 0;
+    OM_TRY(cudaMemcpyAsync(&words_per_lane_total, g->d_gbase + g->n_groups, sizeof(uint32_t),
+                           cudaMemcpyDeviceToHost, st));
+    OM_TRY(cudaStreamSynchronize(st));
+    cudaFree(gw);
+    cudaFree(gtmp);
+    g->n_words = 32LL * words_per_lane_total;
+    OM_TRY(cudaMalloc(&g->d_desc, sizeof(uint32_t) * (size_t)std::max(g->n_words, 1LL)));
+
+    unsigned long long *d_err = nullptr;
+    OM_TRY(cudaMalloc(&d_err, 2 * sizeof(unsigned long long)));
+    OM_TRY(cudaMemsetAsync(d_err, 0, 2 * sizeof(unsigned long long), st));
+    k_walk<<<(unsigned)((g->n_lines + 255) / 256), 256, 0, st>>>(G, g->d_dirs, g->d_lines, g->d_off,
+                                                                 g->d_gbase, g->d_desc, g->n_lines, d_err);
+    OM_COUNT_LAUNCH();
+    OM_TRY(cudaGetLastError());
+    unsigned long long herr[2] = {0, 0};
+    OM_TRY(cudaMemcpyAsync(herr, d_err, sizeof(herr), cudaMemcpyDeviceToHost, st));
+    OM_TRY(cudaStreamSynchronize(st));
+    cudaFree(d_err);
+    g->walk_errors = (long long)herr[0];
+    g->n_units = (long long)herr[1];
+    return cudaSuccess;
+}
+
+}  // namespace omni3d

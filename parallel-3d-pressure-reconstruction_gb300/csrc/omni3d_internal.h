@@ -1,0 +1,145 @@
+// Internal declarations shared by the CUDA translation units of libomni3d_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "omni3d.h"
+
+namespace omni3d {
+
+// Number of kernels this library has launched (process-wide, all contexts).
+extern unsigned long long g_kernel_launches;
+#define OM_COUNT_LAUNCH() (__atomic_fetch_add(&omni3d::g_kernel_launches, 1ull, __ATOMIC_RELAXED))
+
+// Per-direction constants, computed once on the host (exact libm evaluation of the
+// rotation of K:6175-6191) and read by the tracing kernels.
+struct DirEntry {
+    float ct, st, cp, sp;  // cos/sin of theta and phi
+    float k1, k2, k3;      // the direction as read from the direction file
+    int cas;               // which branch of cross2point (K:663-1113) applies: 1..7, 0 none
+};
+
+// Grid constants passed by value to every kernel.
+struct Grid {
+    int X, Y, Z;
+    long long XY, V;
+    float cx, cy, cz;       // (N-1)/2 in float, K:665-667
+    float dx, dy, dz, rho;  // spacing and density
+    float ls;               // line spacing
+    float thr;              // select threshold
+    int ng;                 // lattice points per row, K:6159-6167
+};
+
+// One traced line (16 bytes): entry voxel, exit voxel (linear indices), direction and
+// number of staircase steps.  The sign of every axis step is fixed per line: toward the
+// exit.
+struct LineRec {
+    uint32_t e, x;
+    int32_t dir;
+    int32_t m;
+};
+
+// Device-resident geometry of one (grid, direction set, line spacing) triple.  Lines are
+// grouped 32 per warp; group g's step words are interleaved lane by lane:
+// word w of lane l lives at desc[32 * gbase[g] + 32 * w + l], 16 steps (2 bits each) per
+// word.
+struct Geometry {
+    Grid grid;
+    int nv = 0;
+    DirEntry *d_dirs = nullptr;
+    float4 *d_off = nullptr;        // per line: centred offset (x, y, z) of its lattice point
+    LineRec *d_lines = nullptr;
+    uint32_t *d_gbase = nullptr;    // n_groups + 1 prefix sums of words per lane
+    uint32_t *d_desc = nullptr;
+    long long n_lines = 0, n_groups = 0, n_words = 0;
+    long long n_units = 0;          // sum over lines of (steps + 1)
+    long long walk_errors = 0;
+};
+
+// ---------------------------------------------------------------- launchers (kernels_*.cu)
+// All launchers are asynchronous on `st` and return the launch status.
+
+// Lines of every (direction, lattice point) pair, in that order.  Allocates and fills
+// g->d_off, g->d_lines, g->d_gbase, g->d_desc; walks every line.  Synchronises `st`.
+cudaError_t build_geometry(Geometry *g, cudaStream_t st, std::string *err);
+void free_geometry(Geometry *g);
+
+// Exclusive scans (out has n + 1 entries; out[n] = total).  tmp must hold
+// scan_tmp_elems(n) elements.
+size_t scan_tmp_elems(long long n);
+cudaError_t exclusive_scan_u32(const uint32_t *in, uint32_t *out, long long n, uint32_t *tmp,
+                               cudaStream_t st);
+cudaError_t exclusive_scan_u64(const unsigned long long *in, unsigned long long *out,
+                               long long n, unsigned long long *tmp, cudaStream_t st);
+
+// Gradient field on the device: float4 (ax, ay, az, curl) per voxel, or its bf16 copy.
+struct Field {
+    float4 *f32 = nullptr;          // always present
+    uint2 *bf16 = nullptr;          // (ax, ay, az, 0) as bf16 when grad_storage is BF16
+    float *curl = nullptr;          // curl (select method), also in f32[v].w
+};
+
+// Pack three component arrays (+ optional curl) into the interleaved field.
+cudaError_t pack_field(const Grid &g, const float *ax, const float *ay, const float *az,
+                       const float *curl, Field *f, bool make_bf16, cudaStream_t st);
+// |curl a| x mask into out (and into field .w when f is given).
+cudaError_t curl_field(const Grid &g, const float *ax, const float *ay, const float *az,
+                       const float *mask, float *out, cudaStream_t st);
+
+// One full sweep: pncnt[v] += (sum of contributions, sum of weights) over all lines.
+// method: OMNI3D_METHOD_*; p is read at line entries / segment starts.
+cudaError_t sweep_full(const Geometry &geo, const Field &f, int method, bool bf16,
+                       const float *p, float2 *pncnt, cudaStream_t st);
+
+// p_out[v] = cnt > 0 ? pn / cnt : p_keep[v]; cnt_out[v] = cnt (either may be null).
+cudaError_t normalize(long long V, const float2 *pncnt, const float *p_keep, float *p_out,
+                      float *cnt_out, cudaStream_t st);
+// pn[v] += acc[v].x, cnt[v] += acc[v].y
+cudaError_t accum_split(long long V, const float2 *acc, float *pn, float *cnt, cudaStream_t st);
+// pncnt = (seed ? p_init : 0, 0)
+cudaError_t init_accum(long long V, const float *p_init, bool seed, float2 *pncnt,
+                       cudaStream_t st);
+
+// Anchor operator (kernels_anchor.cu).
+struct Anchor {
+    long long n = 0, nnz = 0;
+    uint8_t *flag = nullptr;        // V bytes: voxel is an anchor
+    uint32_t *bits = nullptr;       // V bits
+    int32_t *id = nullptr;          // V: anchor id or -1
+    uint32_t *vox = nullptr;        // n: voxel of anchor
+    unsigned long long *rowptr = nullptr;  // n + 1
+    uint32_t *col = nullptr;        // nnz
+    float *w = nullptr;             // nnz
+    float *b = nullptr;             // n: sum of w * I
+    float *c = nullptr;             // n: sum of w
+    float *pa = nullptr, *pb = nullptr;  // iterates
+    double *red = nullptr;          // reduction scratch
+};
+cudaError_t anchor_build(const Geometry &geo, const Field &f, int method, bool bf16,
+                         long long ref_voxel, Anchor *A, cudaStream_t st, std::string *err);
+void anchor_free(Anchor *A);
+// One iteration p_next = (b + seed * p_init_a + M p_cur) / c; accumulates the gauged
+// change / norm sums into red[0..1] for the relative change.
+cudaError_t anchor_step(const Anchor &A, const float *p_init, bool seed, int gauge,
+                        long long ref_anchor, const float *p_cur, float *p_next, double *red2,
+                        cudaStream_t st);
+// Gauged relative-change sums over n values: out2 = {sum (d - d_ref)^2, sum (p - p_ref)^2}
+// with d = pn - pc; the shift is the value at `ref` (point gauge), the mean (mean gauge)
+// or zero.  Deterministic FP64 reduction; scratch holds change_scratch_doubles().
+size_t change_scratch_doubles();
+cudaError_t change_sums(long long n, const float *pc, const float *pn, int gauge, long long ref,
+                        double *scratch, double *out2, cudaStream_t st);
+// Scatter anchor values into a volume.
+cudaError_t anchor_scatter(const Anchor &A, const float *pa, float *vol, cudaStream_t st);
+// Gather anchor values from a volume.
+cudaError_t anchor_gather(const Anchor &A, const float *vol, float *pa, cudaStream_t st);
+
+// Gauge: subtract p[ref] (mode POINT) or the mean over count > 0 (MEAN), FP64 reduction.
+cudaError_t apply_gauge(long long V, int gauge, long long ref, const float *cnt, float *p,
+                        double *scratch, cudaStream_t st);
+size_t gauge_scratch_doubles();
+
+}  // namespace omni3d

@@ -1,0 +1,241 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle.
+
+Bit-exact: the traced lines (entry, exit, direction, step count), every staircase, the
+plain-method counts and the curl indicator.  Floating point: p after the iterations
+within a stated relative L2 of the oracle's FP64 evaluation of the same discrete method
+(the FP32 GPU path differs only in the order and precision of sums).
+"""
+import numpy as np
+import pytest
+
+from omni3d import synthetic
+
+pytestmark = pytest.mark.gpu
+
+# tolerances (relative L2 after removing the mean)
+TOL_P_PLAIN = 2e-5     # FP32 + Kahan line scans vs FP64, a few iterations
+TOL_P_SELECT = 1e-4    # curl-weighted averages amplify rounding a little
+TOL_PN = 1e-5          # one sweep, accumulated sums
+
+
+def _field(dims, seed=0, noise=0.05, sphere=None):
+    n = max(dims)
+    f = synthetic.blobs(dims=dims, count=3, sigma_range=(2.0, 5.0), noise=noise, seed=seed, spacing=1e-3,
+                        sphere_radius=sphere)
+    return f
+
+
+def _pinit(dims, seed=1):
+    """Bernoulli-like nonzero j = 0 face, exercising the first-iteration seeding (K:8811)."""
+    nx, ny, nz = dims
+    rng = np.random.default_rng(seed)
+    p = np.zeros((nz, ny, nx), np.float32)
+    p[:, 0, :] = rng.normal(0, 0.5, (nz, nx)).astype(np.float32)
+    return p
+
+
+def _lines_oracle(orc, dims, ls, dirs):
+    rows = []
+    for d in range(len(dirs)):
+        valid, inout, nsteps, xyz = orc.trace_direction(dims, ls, dirs[d])
+        X, Y, Z = dims
+        for pt in np.nonzero(valid)[0]:
+            i = inout[pt]
+            e = i[0] + i[1] * X + i[2] * X * Y
+            x = i[3] + i[4] * X + i[5] * X * Y
+            rows.append((e, x, d, nsteps[pt]))
+    return np.array(rows, np.int64).reshape(-1, 4)
+
+
+@pytest.mark.parametrize("dims,ls,level", [((20, 17, 13), 1.0, 3), ((16, 16, 16), 0.7, 3), ((12, 9, 15), 1.0, 2)])
+def test_line_table_bit_exact(omni, orc, dims, ls, level):
+    dirs = omni.icosphere(level)
+    with omni.Omni3D(dims, 1e-3, dirs, line_spacing=ls, max_iter=1) as s:
+        info = s.geometry_info()
+        assert info["walk_errors"] == 0
+        got = s.line_table().astype(np.int64)
+        got[:, 0] &= 0xFFFFFFFF
+        got[:, 1] &= 0xFFFFFFFF
+        exp = _lines_oracle(orc, dims, ls, dirs)
+        assert got.shape == exp.shape
+        np.testing.assert_array_equal(got, exp)
+        assert info["n_units"] == int((exp[:, 3] + 1).sum())
+        # staircases of a sample of lines
+        X, Y, Z = dims
+        for li in range(0, len(exp), max(1, len(exp) // 40)):
+            e, x, d, m = exp[li]
+            inout = np.array([e % X, (e // X) % Y, e // (X * Y), x % X, (x // X) % Y, x // (X * Y)], np.int32)
+            # the oracle walk needs the lattice offset: recover it from the trace
+            valid, io, ns, xyz = orc.trace_direction(dims, ls, dirs[d])
+            pts = np.nonzero(valid)[0]
+            hit = [pt for pt in pts if (io[pt] == inout).all()]
+            assert hit, "line not found in the oracle trace"
+            ax = orc.walk(dims, io[hit[0]], xyz[hit[0]], dirs[d])
+            np.testing.assert_array_equal(s.line_steps(li), ax)
+
+
+def test_curl_bit_exact(omni, orc):
+    dims = (14, 11, 9)
+    f = _field(dims, sphere=3.0)
+    dirs = omni.icosphere(2)
+    with omni.Omni3D(dims, f["spacing"], dirs, max_iter=1) as s:
+        got = s.curl(f["ax"], f["ay"], f["az"], f["mask"]).reshape(-1)
+    exp = orc.curl(dims, f["spacing"], f["ax"], f["ay"], f["az"], f["mask"])
+    np.testing.assert_array_equal(got.view(np.uint32), exp.view(np.uint32))
+
+
+def test_plain_sweep_matches_oracle(omni, orc):
+    dims = (18, 15, 12)
+    f = _field(dims, seed=3)
+    dirs = omni.icosphere(3)
+    p = _pinit(dims)
+    with omni.Omni3D(dims, f["spacing"], dirs, max_iter=1) as s:
+        pn, cnt = s.sweep(f["ax"], f["ay"], f["az"], p)
+    epn, ecnt = orc.sweep(dims, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p, precision="f64")
+    np.testing.assert_array_equal(cnt.reshape(-1), ecnt.astype(np.float32))
+    assert synthetic.relative_l2(pn, epn, gauge="none") < TOL_PN
+
+
+@pytest.mark.parametrize("solver", ["sweep", "anchor"])
+@pytest.mark.parametrize("niter", [1, 2, 5])
+def test_plain_solve_matches_oracle(omni, orc, solver, niter):
+    dims = (20, 16, 14)
+    f = _field(dims, seed=4)
+    dirs = omni.icosphere(3)
+    p0 = _pinit(dims)
+    with omni.Omni3D(dims, f["spacing"], dirs, max_iter=niter, solver=solver) as s:
+        r = s.solve(f["ax"], f["ay"], f["az"], p_init=p0)
+    ep, ecnt = orc.solve(dims, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p0, niter, precision="f64")
+    np.testing.assert_array_equal(r.count.reshape(-1), ecnt.astype(np.float32))
+    assert r.stats["iterations"] == niter
+    assert synthetic.relative_l2(r.p, ep, gauge="none") < TOL_P_PLAIN
+    # also against the reference's own float arithmetic
+    fp, fcnt = orc.solve(dims, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p0, niter, precision="f32")
+    np.testing.assert_array_equal(r.count.reshape(-1), fcnt)
+    assert synthetic.relative_l2(r.p, fp, gauge="none") < TOL_P_PLAIN
+
+
+@pytest.mark.parametrize("solver", ["sweep", "anchor"])
+def test_select_solve_matches_oracle(omni, orc, solver):
+    dims = (20, 18, 16)
+    f = _field(dims, seed=5, noise=0.1, sphere=4.0)
+    dirs = omni.icosphere(3)
+    p0 = _pinit(dims, seed=2)
+    curl = orc.curl(dims, f["spacing"], f["ax"], f["ay"], f["az"], f["mask"])
+    thr = float(np.percentile(curl[curl > 0], 85))
+    niter = 4
+    with omni.Omni3D(dims, f["spacing"], dirs, max_iter=niter, solver=solver, method="select", threshold=thr) as s:
+        r = s.solve(f["ax"], f["ay"], f["az"], mask=f["mask"], p_init=p0)
+    ep, ecnt = orc.solve(dims, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p0, niter, mode=1, thr=thr, curl=curl,
+                         precision="f64")
+    # weights are curl-dependent floats: compare within tolerance, zero pattern exactly
+    np.testing.assert_array_equal(r.count.reshape(-1) > 0, ecnt > 0)
+    assert synthetic.relative_l2(r.count, ecnt, gauge="none") < 1e-5
+    assert synthetic.relative_l2(r.p, ep, gauge="none") < TOL_P_SELECT
+
+
+def test_select_without_threshold_splits_at_mask(omni, orc):
+    """Config-3 form: threshold above every curl, so only the masked voxels are excluded."""
+    dims = (18, 18, 18)
+    f = _field(dims, seed=6, sphere=5.0)
+    dirs = omni.icosphere(2)
+    curl = orc.curl(dims, f["spacing"], f["ax"], f["ay"], f["az"], f["mask"])
+    thr = float(np.finfo(np.float32).max)
+    with omni.Omni3D(dims, f["spacing"], dirs, max_iter=3, method="select", threshold=thr) as s:
+        r = s.solve(f["ax"], f["ay"], f["az"], curl=curl)
+    ep, ecnt = orc.solve(dims, f["spacing"], dirs, f["ax"], f["ay"], f["az"], np.zeros(curl.size, np.float32), 3,
+                         mode=1, thr=thr, curl=curl, precision="f64")
+    inside = (f["mask"].reshape(-1) == 0)
+    assert (r.count.reshape(-1)[inside] == 0).all()
+    assert synthetic.relative_l2(r.p, ep, gauge="none") < TOL_P_SELECT
+
+
+def test_iteration_edge_cases(omni, orc):
+    dims = (10, 9, 8)
+    f = _field(dims, seed=7)
+    dirs = omni.icosphere(2)
+    p0 = _pinit(dims)
+    with omni.Omni3D(dims, f["spacing"], dirs, max_iter=0) as s:
+        r = s.solve(f["ax"], f["ay"], f["az"], p_init=p0)
+        np.testing.assert_array_equal(r.p.reshape(-1), p0.reshape(-1))
+        assert (r.count == 0).all()
+    # seeding off: the first sweep starts from zero
+    with omni.Omni3D(dims, f["spacing"], dirs, max_iter=1, seed_first_iteration=False) as s:
+        r = s.solve(f["ax"], f["ay"], f["az"], p_init=p0)
+    pn, cnt = orc.sweep(dims, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p0, precision="f64")
+    exp = np.where(cnt > 0, pn / np.maximum(cnt, 1), p0.reshape(-1))
+    assert synthetic.relative_l2(r.p, exp, gauge="none") < TOL_P_PLAIN
+
+
+def test_minimal_grid_and_pole_directions(omni, orc):
+    """2x2x2 grid and a direction set holding only the poles and the axes."""
+    dirs = np.array([[0, 0, 1], [0, 0, -1], [1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0]], np.float32)
+    for dims in [(2, 2, 2), (3, 5, 4)]:
+        f = _field(dims, seed=8)
+        with omni.Omni3D(dims, f["spacing"], dirs, max_iter=2) as s:
+            r = s.solve(f["ax"], f["ay"], f["az"])
+        ep, ecnt = orc.solve(dims, f["spacing"], dirs, f["ax"], f["ay"], f["az"], np.zeros(np.prod(dims), np.float32),
+                             2, precision="f64")
+        np.testing.assert_array_equal(r.count.reshape(-1), ecnt.astype(np.float32))
+        assert synthetic.relative_l2(r.p, ep, gauge="none") < TOL_P_PLAIN
+
+
+def test_gauges_and_tolerance(omni, orc):
+    dims = (16, 16, 16)
+    f = _field(dims, seed=9)
+    dirs = omni.icosphere(3)
+    with omni.Omni3D(dims, f["spacing"], dirs, max_iter=6) as s:
+        r0 = s.solve(f["ax"], f["ay"], f["az"])
+    with omni.Omni3D(dims, f["spacing"], dirs, max_iter=6, gauge="point", ref=(0, 0, 0)) as s:
+        r1 = s.solve(f["ax"], f["ay"], f["az"])
+    assert r1.p.reshape(-1)[0] == 0.0
+    np.testing.assert_allclose(r1.p, r0.p - r0.p.reshape(-1)[0], atol=1e-5 * np.abs(r0.p).max())
+    with omni.Omni3D(dims, f["spacing"], dirs, max_iter=6, gauge="mean") as s:
+        r2 = s.solve(f["ax"], f["ay"], f["az"])
+    sel = r2.count > 0
+    assert abs(float(r2.p[sel].mean())) < 1e-5 * np.abs(r2.p).max()
+    # tolerance-driven stop: both solvers stop at the same iteration
+    its = []
+    for solver in ("sweep", "anchor"):
+        with omni.Omni3D(dims, f["spacing"], dirs, max_iter=200, tol=1e-4, gauge="point", solver=solver) as s:
+            r = s.solve(f["ax"], f["ay"], f["az"])
+            its.append(r.stats["iterations"])
+            assert r.stats["rel_change"] < 1e-4
+    assert abs(its[0] - its[1]) <= 1
+
+
+def test_bf16_gradient_storage(omni):
+    dims = (24, 24, 24)
+    f = _field(dims, seed=10)
+    dirs = omni.icosphere(3)
+    out = {}
+    for g in ("f32", "bf16"):
+        with omni.Omni3D(dims, f["spacing"], dirs, max_iter=4, grad=g) as s:
+            out[g] = s.solve(f["ax"], f["ay"], f["az"])
+    np.testing.assert_array_equal(out["f32"].count, out["bf16"].count)
+    err = synthetic.relative_l2(out["bf16"].p, out["f32"].p)
+    assert 0 < err < 1e-2
+
+
+def test_device_pointers_match_host(omni):
+    torch = pytest.importorskip("torch")
+    dims = (16, 14, 12)
+    f = _field(dims, seed=11)
+    dirs = omni.icosphere(3)
+    with omni.Omni3D(dims, f["spacing"], dirs, max_iter=3) as s:
+        rh = s.solve(f["ax"], f["ay"], f["az"])
+        t = [torch.from_numpy(f[k].reshape(-1)).cuda() for k in ("ax", "ay", "az")]
+        rd = s.solve(*t)
+    np.testing.assert_array_equal(rd.count.cpu().numpy(), rh.count)
+    assert synthetic.relative_l2(rd.p.cpu().numpy(), rh.p, gauge="none") < 1e-6
+
+
+def test_counts_deterministic(omni):
+    dims = (20, 20, 20)
+    f = _field(dims, seed=12)
+    dirs = omni.icosphere(3)
+    with omni.Omni3D(dims, f["spacing"], dirs, max_iter=2) as s:
+        a = s.solve(f["ax"], f["ay"], f["az"])
+        b = s.solve(f["ax"], f["ay"], f["az"])
+    np.testing.assert_array_equal(a.count, b.count)
+    assert synthetic.relative_l2(a.p, b.p, gauge="none") < 1e-6
