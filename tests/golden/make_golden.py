@@ -1,0 +1,93 @@
+"""Generate tests/golden/reference_small.npz from the reference's own CPU functions.
+
+Run in a tree where the reference sources are available (oracle/build_ref.sh stages and
+compiles them into oracle/_ref/libomni_ref.so):
+
+    python tests/golden/make_golden.py
+
+Each case stores its inputs (so the fixture does not depend on the generator) and the
+outputs of the reference functions:
+  plain    12x10x8 grid, 42 directions, 2 iterations of cross2point + bodyIntegralInner
+           over every (direction, lattice point) pair with the GPU kernel's geometry, then
+           the GPU normalisation (count > 0), starting from a nonzero j = 0 face
+  select   14x12x10 grid with a masked sphere, 42 directions, 3 iterations of
+           bodyIntegralInnerSelect, threshold at the 80th percentile of the curl
+  ls07     10x9x8 grid, 42 directions, line spacing 0.7, 2 plain iterations
+  cputwin  10x10x10 grid, 42 directions, 2 iterations of the reference's own CPU loop
+           omni3dparallellinesESInnerCPU + devidecountInnerCPU (no pole guard, count > 1)
+  curl     the curl indicator calCurlofMaterialAccCPU of the select case
+Directions are the 42-vertex icosphere (the vertex set of GridIcosahedronDivide2.dat).
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+sys.path.insert(0, os.path.join(REPO, "parallel-3d-pressure-reconstruction_gb300"))
+
+import oracle  # noqa: E402
+from omni3d import synthetic  # noqa: E402
+from omni3d.solver import icosphere  # noqa: E402
+
+
+def field(dims, seed, sphere=None):
+    f = synthetic.blobs(dims=dims, count=3, sigma_range=(2.0, 4.0), noise=0.05, seed=seed, sphere_radius=sphere)
+    return f
+
+
+def pinit(dims, seed):
+    nx, ny, nz = dims
+    rng = np.random.default_rng(seed)
+    p = np.zeros((nz, ny, nx), np.float32)
+    p[:, 0, :] = rng.normal(0, 0.5, (nz, nx)).astype(np.float32)
+    return p.reshape(-1)
+
+
+def main():
+    R = oracle.RefLib()
+    dirs = icosphere(2)
+    out = {"dirs": dirs}
+    # plain
+    d = (12, 10, 8)
+    f = field(d, 1)
+    p0 = pinit(d, 2)
+    p, c = R.solve(d, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p0, 2)
+    out.update({"plain_dims": np.array(d), "plain_spacing": np.array(f["spacing"], np.float32),
+                "plain_ax": f["ax"].reshape(-1), "plain_ay": f["ay"].reshape(-1), "plain_az": f["az"].reshape(-1),
+                "plain_p0": p0, "plain_p": p, "plain_count": c})
+    # select
+    d = (14, 12, 10)
+    f = field(d, 3, sphere=3.0)
+    p0 = pinit(d, 4)
+    curl = R.curl(d, f["spacing"], f["ax"], f["ay"], f["az"], f["mask"])
+    thr = np.float32(np.percentile(curl[curl > 0], 80))
+    p, c = R.solve(d, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p0, 3, mode=1, thr=float(thr), curl=curl)
+    out.update({"select_dims": np.array(d), "select_spacing": np.array(f["spacing"], np.float32),
+                "select_ax": f["ax"].reshape(-1), "select_ay": f["ay"].reshape(-1), "select_az": f["az"].reshape(-1),
+                "select_mask": f["mask"].reshape(-1), "select_curl": curl, "select_thr": np.array(thr),
+                "select_p0": p0, "select_p": p, "select_count": c})
+    # line spacing 0.7
+    d = (10, 9, 8)
+    f = field(d, 5)
+    p0 = np.zeros(np.prod(d), np.float32)
+    p, c = R.solve(d, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p0, 2, ls=0.7)
+    out.update({"ls07_dims": np.array(d), "ls07_spacing": np.array(f["spacing"], np.float32),
+                "ls07_ax": f["ax"].reshape(-1), "ls07_ay": f["ay"].reshape(-1), "ls07_az": f["az"].reshape(-1),
+                "ls07_p": p, "ls07_count": c})
+    # the reference's own CPU loop
+    d = (10, 10, 10)
+    f = field(d, 6)
+    p0 = np.zeros(np.prod(d), np.float32)
+    p, c = R.cpu_twin_solve(d, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p0, 2)
+    out.update({"cputwin_dims": np.array(d), "cputwin_spacing": np.array(f["spacing"], np.float32),
+                "cputwin_ax": f["ax"].reshape(-1), "cputwin_ay": f["ay"].reshape(-1),
+                "cputwin_az": f["az"].reshape(-1), "cputwin_p": p, "cputwin_count": c})
+    np.savez_compressed(os.path.join(HERE, "reference_small.npz"), **out)
+    print("wrote", os.path.join(HERE, "reference_small.npz"))
+
+
+if __name__ == "__main__":
+    main()

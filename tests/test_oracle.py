@@ -1,0 +1,175 @@
+"""The oracle pinned against the reference: its own functions compiled from source
+(oracle/_ref, where the sources are staged) and the committed golden fixtures made from
+them (tests/golden/make_golden.py).  CPU only."""
+import os
+
+import numpy as np
+import pytest
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "reference_small.npz")
+
+
+def _bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return np.load(GOLD)
+
+
+def _dims(g, c):
+    return tuple(int(x) for x in g[c + "_dims"])
+
+
+def _sp(g, c):
+    return tuple(float(x) for x in g[c + "_spacing"])
+
+
+def test_golden_plain_bit_exact(orc, gold):
+    g = gold
+    p, c = orc.solve(_dims(g, "plain"), _sp(g, "plain"), g["dirs"], g["plain_ax"], g["plain_ay"], g["plain_az"],
+                     g["plain_p0"], 2)
+    np.testing.assert_array_equal(_bits(c), _bits(g["plain_count"]))
+    np.testing.assert_array_equal(_bits(p), _bits(g["plain_p"]))
+
+
+def test_golden_select_bit_exact(orc, gold):
+    g = gold
+    d = _dims(g, "select")
+    curl = orc.curl(d, _sp(g, "select"), g["select_ax"], g["select_ay"], g["select_az"], g["select_mask"])
+    np.testing.assert_array_equal(_bits(curl), _bits(g["select_curl"]))
+    p, c = orc.solve(d, _sp(g, "select"), g["dirs"], g["select_ax"], g["select_ay"], g["select_az"], g["select_p0"], 3,
+                     mode=1, thr=float(g["select_thr"]), curl=curl)
+    np.testing.assert_array_equal(_bits(c), _bits(g["select_count"]))
+    np.testing.assert_array_equal(_bits(p), _bits(g["select_p"]))
+
+
+def test_golden_line_spacing(orc, gold):
+    g = gold
+    d = _dims(g, "ls07")
+    p, c = orc.solve(d, _sp(g, "ls07"), g["dirs"], g["ls07_ax"], g["ls07_ay"], g["ls07_az"],
+                     np.zeros(np.prod(d), np.float32), 2, ls=0.7)
+    np.testing.assert_array_equal(_bits(c), _bits(g["ls07_count"]))
+    np.testing.assert_array_equal(_bits(p), _bits(g["ls07_p"]))
+
+
+def test_golden_cpu_twin_loop(orc, gold):
+    """The reference's own CPU loop: no pole guard (poles give NaN offsets and are skipped),
+    lattice without the line-spacing division, normalisation where count > 1."""
+    g = gold
+    d = _dims(g, "cputwin")
+    V = int(np.prod(d))
+    p = np.zeros(V, np.float32)
+    pn = np.zeros(V, np.float32)
+    cnt = np.zeros(V, np.float32)
+    for _ in range(2):
+        cnt[:] = 0
+        spn, scnt = orc.sweep(d, _sp(g, "cputwin"), g["dirs"], g["cputwin_ax"], g["cputwin_ay"], g["cputwin_az"], p,
+                              cpu_twin=True)
+        pn += spn
+        cnt += scnt
+        m = cnt > 1
+        p[m] = (pn[m] / cnt[m]).astype(np.float32)
+        pn[m] = 0
+    np.testing.assert_array_equal(_bits(cnt), _bits(g["cputwin_count"]))
+    np.testing.assert_array_equal(_bits(p), _bits(g["cputwin_p"]))
+
+
+def test_oracle_matches_reference_functions(orc, reflib):
+    """Direct comparison with the reference functions on a non-cubic grid, both methods."""
+    from omni3d import synthetic
+    from omni3d.solver import icosphere
+
+    dims = (17, 13, 11)
+    dirs = icosphere(3)
+    f = synthetic.blobs(dims=dims, count=3, sigma_range=(2.0, 4.0), noise=0.05, seed=11, sphere_radius=3.0)
+    p0 = np.zeros(np.prod(dims), np.float32)
+    p0[: dims[0]] = 0.25
+    a, ca = orc.solve(dims, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p0, 2)
+    b, cb = reflib.solve(dims, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p0, 2)
+    np.testing.assert_array_equal(_bits(ca), _bits(cb))
+    np.testing.assert_array_equal(_bits(a), _bits(b))
+    curl = orc.curl(dims, f["spacing"], f["ax"], f["ay"], f["az"], f["mask"])
+    thr = float(np.percentile(curl[curl > 0], 70))
+    a, ca = orc.solve(dims, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p0, 2, mode=1, thr=thr, curl=curl)
+    b, cb = reflib.solve(dims, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p0, 2, mode=1, thr=thr, curl=curl)
+    np.testing.assert_array_equal(_bits(ca), _bits(cb))
+    np.testing.assert_array_equal(_bits(a), _bits(b))
+
+
+def test_cross2point_matches_reference(orc, reflib):
+    """Random offsets and directions, including exact-zero components (cases 1-6)."""
+    rng = np.random.default_rng(0)
+    dims = (13, 9, 11)
+    dirs = [rng.normal(size=3) for _ in range(60)]
+    dirs += [np.array(v, float) for v in ([0, 1, 1], [1, 0, 1], [1, 1, 0], [0, 0, 1], [0, 1, 0], [1, 0, 0],
+                                          [0, -1, 2], [-2, 0, 1], [3, -1, 0], [0, 0, -1], [0, -1, 0], [-1, 0, 0])]
+    n = 0
+    for k in dirs:
+        k = (k / np.linalg.norm(k)).astype(np.float32)
+        for _ in range(40):
+            xyz = rng.uniform(-9, 9, 3).astype(np.float32)
+            i = np.zeros(3, np.int32)
+            o = np.zeros(3, np.int32)
+            import ctypes as C
+
+            ra = orc.lib.orc_cross2point(*dims, float(xyz[0]), float(xyz[1]), float(xyz[2]), float(k[0]),
+                                         float(k[1]), float(k[2]), i.ctypes.data_as(C.POINTER(C.c_int)),
+                                         o.ctypes.data_as(C.POINTER(C.c_int)))
+            rb, io = reflib.cross2point(dims, xyz, k)
+            assert ra == rb
+            np.testing.assert_array_equal(np.concatenate([i, o]), io)
+            n += 1
+    assert n == len(dirs) * 40
+
+
+def test_calindex_is_bijection_on_boundary(orc, reflib):
+    """The reference's boundary numbering is a bijection on the boundary voxels, so its
+    `nin != nout` test equals `entry voxel != exit voxel`."""
+    for dims in [(12, 10, 8), (5, 7, 3), (32, 32, 32)]:
+        a = orc.calindex(dims)
+        b = reflib.calindex(dims)
+        np.testing.assert_array_equal(a, b)
+        X, Y, Z = dims
+        v = np.arange(X * Y * Z)
+        i, j, k = v % X, (v // X) % Y, v // (X * Y)
+        surf = (i == 0) | (i == X - 1) | (j == 0) | (j == Y - 1) | (k == 0) | (k == Z - 1)
+        assert len(np.unique(a[surf])) == surf.sum()
+        assert (a[~surf] == -1).all()
+
+
+def test_fp64_oracle_close_to_fp32(orc, gold):
+    """The FP64 oracle follows the same discrete geometry: counts equal, values close."""
+    g = gold
+    d = _dims(g, "plain")
+    p32, c32 = orc.solve(d, _sp(g, "plain"), g["dirs"], g["plain_ax"], g["plain_ay"], g["plain_az"], g["plain_p0"], 2)
+    p64, c64 = orc.solve(d, _sp(g, "plain"), g["dirs"], g["plain_ax"], g["plain_ay"], g["plain_az"], g["plain_p0"], 2,
+                         precision="f64")
+    np.testing.assert_array_equal(c32, c64.astype(np.float32))
+    assert np.linalg.norm(p32 - p64) / np.linalg.norm(p64) < 1e-5
+
+
+def test_oracle_threads_change_only_sum_order(orc, gold):
+    g = gold
+    d = _dims(g, "plain")
+    a, ca = orc.solve(d, _sp(g, "plain"), g["dirs"], g["plain_ax"], g["plain_ay"], g["plain_az"], g["plain_p0"], 2)
+    b, cb = orc.solve(d, _sp(g, "plain"), g["dirs"], g["plain_ax"], g["plain_ay"], g["plain_az"], g["plain_p0"], 2,
+                      nthreads=3)
+    np.testing.assert_array_equal(ca, cb)
+    assert np.linalg.norm(a - b) / np.linalg.norm(a) < 1e-5
+
+
+def test_oracle_converges_toward_analytic(orc):
+    """Config-1 shape at reduced size: the iteration approaches the analytic field."""
+    from omni3d import synthetic
+    from omni3d.solver import icosphere
+
+    f = synthetic.gaussian(n=16, sigma_cells=3.0, noise=0.0)
+    dirs = icosphere(3)
+    errs = []
+    for k in (1, 4):
+        p, c = orc.solve(f["dims"], f["spacing"], dirs, f["ax"], f["ay"], f["az"], np.zeros(16 ** 3, np.float32), k,
+                         precision="f64")
+        errs.append(synthetic.relative_l2(p, f["p_true"]))
+    assert errs[1] < errs[0] and errs[1] < 0.1
