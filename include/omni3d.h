@@ -130,6 +130,14 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
 int omni3d_sweep(omni3d_ctx *ctx, const float *ax, const float *ay, const float *az,
                  const float *curl, const float *p, float *pn, float *count, int device_ptrs);
 
+/* Remove the constant mode of a pressure field in place: p -= p[ref] (OMNI3D_GAUGE_POINT,
+ * ref = i + j*nx + k*nx*ny) or p -= mean of p over voxels with count > 0
+ * (OMNI3D_GAUGE_MEAN), with an FP64 reduction.  The reference's mean removal over the
+ * measured voxels is commented out in its main() (K:8879-8915); omni3d_solve applies the
+ * same operation when params.gauge is set.  n must equal the context's voxel count. */
+int omni3d_gauge(omni3d_ctx *ctx, float *p, const float *count, long long n, int gauge,
+                 long long ref, int device_ptrs);
+
 /* |curl a| x mask: calCurlofMaterialAccCPU, K:8352-8378 (GPU twin K:6863-6888). */
 int omni3d_curl(omni3d_ctx *ctx, const float *ax, const float *ay, const float *az,
                 const float *mask, float *curl_out, int device_ptrs);

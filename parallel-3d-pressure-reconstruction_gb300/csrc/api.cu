@@ -369,6 +369,35 @@ int omni3d_line_steps(omni3d_ctx *ctx, long long line, int8_t *axes, int cap)
     return r.m;
 }
 
+int omni3d_gauge(omni3d_ctx *ctx, float *p, const float *count, long long n, int gauge, long long ref,
+                 int device_ptrs)
+{
+    if (!ctx || !p) return fail(ctx, OMNI3D_ERR_ARG, "NULL argument");
+    const long long V = ctx->geo.grid.V;
+    if (n != V) return fail(ctx, OMNI3D_ERR_ARG, "n differs from the context's voxel count");
+    if (gauge < OMNI3D_GAUGE_NONE || gauge > OMNI3D_GAUGE_MEAN) return fail(ctx, OMNI3D_ERR_ARG, "unknown gauge");
+    if (gauge == OMNI3D_GAUGE_POINT && (ref < 0 || ref >= V)) return fail(ctx, OMNI3D_ERR_ARG, "ref outside the grid");
+    if (gauge == OMNI3D_GAUGE_MEAN && !count) return fail(ctx, OMNI3D_ERR_ARG, "the mean gauge needs count");
+    cudaSetDevice(ctx->prm.device);
+    const bool dev = device_ptrs != 0;
+    float *dp = p;
+    const float *dc = count;
+    if (!dev) {
+        CK(ctx, ctx->pout.ensure(sizeof(float) * (size_t)V));
+        dp = ctx->pout.as<float>();
+        CK(ctx, cudaMemcpyAsync(dp, p, sizeof(float) * (size_t)V, cudaMemcpyHostToDevice, ctx->st));
+        if (count) {
+            int rc = stage(ctx, count, false, ctx->in_aux, V, &dc);
+            if (rc) return rc;
+        }
+    }
+    CK(ctx, ctx->scratch.ensure(sizeof(double) * std::max(change_scratch_doubles(), gauge_scratch_doubles()) + 64));
+    CK(ctx, apply_gauge(V, gauge, ref, dc, dp, ctx->scratch.as<double>() + 4, ctx->st));
+    if (!dev) CK(ctx, cudaMemcpyAsync(p, dp, sizeof(float) * (size_t)V, cudaMemcpyDeviceToHost, ctx->st));
+    CK(ctx, cudaStreamSynchronize(ctx->st));
+    return OMNI3D_OK;
+}
+
 int omni3d_curl(omni3d_ctx *ctx, const float *ax, const float *ay, const float *az, const float *mask, float *curl_out,
                 int device_ptrs)
 {

@@ -174,6 +174,24 @@ class Omni3D:
         shape = self.dims[::-1]
         return pn.reshape(shape), cnt.reshape(shape)
 
+    def gauge(self, p, count=None, mode="mean", ref=0):
+        """Remove the constant mode of p (returns a gauged copy): p - p[ref] or p - mean(p)
+        over count > 0."""
+        if _is_cuda_tensor(p):
+            out = p.reshape(-1).clone().contiguous()
+            c = None if count is None else count.reshape(-1).contiguous()
+            import torch
+
+            torch.cuda.current_stream().synchronize()
+            check(lib().omni3d_gauge(self._h, out.data_ptr(), None if c is None else c.data_ptr(), self.V,
+                                     _GAUGES[mode], int(ref), 1), self._h)
+        else:
+            out = _as_host(p, self.V).copy()
+            c = None if count is None else _as_host(count, self.V)
+            check(lib().omni3d_gauge(self._h, out.ctypes.data, None if c is None else c.ctypes.data, self.V,
+                                     _GAUGES[mode], int(ref), 0), self._h)
+        return out.reshape(self.dims[::-1])
+
     def curl(self, ax, ay, az, mask=None):
         dev, keep, ptrs = self._ptrs([ax, ay, az, mask])
         if dev:

@@ -35,7 +35,9 @@ def _pinit(dims, seed=1):
 
 
 def _lines_oracle(orc, dims, ls, dirs):
-    rows = []
+    """Valid lines in (direction, lattice point) order: table rows and, per line, the
+    (entry/exit, offset) the oracle walk needs."""
+    rows, geo = [], []
     for d in range(len(dirs)):
         valid, inout, nsteps, xyz = orc.trace_direction(dims, ls, dirs[d])
         X, Y, Z = dims
@@ -44,7 +46,8 @@ def _lines_oracle(orc, dims, ls, dirs):
             e = i[0] + i[1] * X + i[2] * X * Y
             x = i[3] + i[4] * X + i[5] * X * Y
             rows.append((e, x, d, nsteps[pt]))
-    return np.array(rows, np.int64).reshape(-1, 4)
+            geo.append((inout[pt].copy(), xyz[pt].copy()))
+    return np.array(rows, np.int64).reshape(-1, 4), geo
 
 
 @pytest.mark.parametrize("dims,ls,level", [((20, 17, 13), 1.0, 3), ((16, 16, 16), 0.7, 3), ((12, 9, 15), 1.0, 2)])
@@ -56,21 +59,14 @@ def test_line_table_bit_exact(omni, orc, dims, ls, level):
         got = s.line_table().astype(np.int64)
         got[:, 0] &= 0xFFFFFFFF
         got[:, 1] &= 0xFFFFFFFF
-        exp = _lines_oracle(orc, dims, ls, dirs)
+        exp, geo = _lines_oracle(orc, dims, ls, dirs)
         assert got.shape == exp.shape
         np.testing.assert_array_equal(got, exp)
         assert info["n_units"] == int((exp[:, 3] + 1).sum())
         # staircases of a sample of lines
-        X, Y, Z = dims
-        for li in range(0, len(exp), max(1, len(exp) // 40)):
-            e, x, d, m = exp[li]
-            inout = np.array([e % X, (e // X) % Y, e // (X * Y), x % X, (x // X) % Y, x // (X * Y)], np.int32)
-            # the oracle walk needs the lattice offset: recover it from the trace
-            valid, io, ns, xyz = orc.trace_direction(dims, ls, dirs[d])
-            pts = np.nonzero(valid)[0]
-            hit = [pt for pt in pts if (io[pt] == inout).all()]
-            assert hit, "line not found in the oracle trace"
-            ax = orc.walk(dims, io[hit[0]], xyz[hit[0]], dirs[d])
+        for li in range(0, len(exp), max(1, len(exp) // 60)):
+            io, xyz = geo[li]
+            ax = orc.walk(dims, io, xyz, dirs[exp[li, 2]])
             np.testing.assert_array_equal(s.line_steps(li), ax)
 
 
