@@ -62,8 +62,9 @@ struct omni3d_ctx {
     // per-solve buffers
     DeviceBuf in_ax, in_ay, in_az, in_aux, in_pinit;  // staging of host inputs
     DeviceBuf f32, b16, curl;
-    DeviceBuf pvol_a, pvol_b, pout, cnt, pncnt, scratch;
+    DeviceBuf pvol_a, pvol_b, pout, cnt, pncnt, scratch, flags;
     Anchor anc;
+    bool anc_cached = false;  // plain method: operator structure built for this geometry
     cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 };
 
@@ -310,7 +311,8 @@ int omni3d_destroy(omni3d_ctx *ctx)
     cudaFree(ctx->geo.d_dirs);
     anchor_free(&ctx->anc);
     for (DeviceBuf *b : {&ctx->in_ax, &ctx->in_ay, &ctx->in_az, &ctx->in_aux, &ctx->in_pinit, &ctx->f32, &ctx->b16,
-                         &ctx->curl, &ctx->pvol_a, &ctx->pvol_b, &ctx->pout, &ctx->cnt, &ctx->pncnt, &ctx->scratch})
+                         &ctx->curl, &ctx->pvol_a, &ctx->pvol_b, &ctx->pout, &ctx->cnt, &ctx->pncnt, &ctx->scratch,
+                         &ctx->flags})
         b->release();
     for (auto &ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
@@ -516,6 +518,13 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
         CK(ctx, ctx->pvol_b.ensure(sizeof(float) * (size_t)V));
         float *pc = ctx->pvol_a.as<float>(), *pn = ctx->pvol_b.as<float>();
         CK(ctx, cudaMemcpyAsync(pc, dpinit, sizeof(float) * (size_t)V, cudaMemcpyDeviceToDevice, st));
+        // the convergence test runs over the anchor voxels, as in the anchor solver
+        uint8_t *amask = nullptr;
+        if (P.tol > 0.0) {
+            CK(ctx, ctx->flags.ensure((size_t)V));
+            amask = ctx->flags.as<uint8_t>();
+            CK(ctx, anchor_mark(ctx->geo, F, P.method, bf16, P.gauge == OMNI3D_GAUGE_POINT ? ref : -1, amask, st));
+        }
         cudaEventRecord(ctx->ev[1], st);
         for (int it = 1; it <= K; it++) {
             CK(ctx, init_accum(V, dpinit, seed && it == 1, acc, st));
@@ -525,7 +534,8 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
             CK(ctx, normalize(V, acc, pc, pn, dcnt, st));
             done = it;
             if (P.tol > 0.0) {
-                CK(ctx, change_sums(V, pc, pn, P.gauge, P.gauge == OMNI3D_GAUGE_POINT ? ref : -1, rscratch, red2, st));
+                CK(ctx, change_sums(V, pc, pn, P.gauge, P.gauge == OMNI3D_GAUGE_POINT ? ref : -1, rscratch, red2, st,
+                                    amask));
                 CK(ctx, cudaMemcpyAsync(hred, red2, sizeof(hred), cudaMemcpyDeviceToHost, st));
                 CK(ctx, cudaStreamSynchronize(st));
                 rel = hred[1] > 0 ? std::sqrt(hred[0] / hred[1]) : 0.0;
@@ -538,8 +548,16 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
     } else {
         // anchor form: iterate the anchors, then one full sweep
         std::string aerr;
-        cudaError_t e = anchor_build(ctx->geo, F, P.method, bf16, P.gauge == OMNI3D_GAUGE_POINT ? ref : -1, &ctx->anc,
-                                     st, &aerr);
+        cudaError_t e;
+        if (P.method == OMNI3D_METHOD_PLAIN && ctx->anc_cached) {
+            e = anchor_refresh_rhs(ctx->geo, F, bf16, &ctx->anc, st);
+            aerr = cudaGetErrorString(e);
+        } else {
+            ctx->anc_cached = false;
+            e = anchor_build(ctx->geo, F, P.method, bf16, P.gauge == OMNI3D_GAUGE_POINT ? ref : -1, &ctx->anc, st,
+                             &aerr);
+            ctx->anc_cached = e == cudaSuccess && P.method == OMNI3D_METHOD_PLAIN;
+        }
         if (e != cudaSuccess) return fail(ctx, e == cudaErrorMemoryAllocation ? OMNI3D_ERR_NOMEM : OMNI3D_ERR_CUDA,
                                           "anchor operator: " + aerr);
         Anchor &A = ctx->anc;

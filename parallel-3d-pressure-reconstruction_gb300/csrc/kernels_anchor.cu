@@ -55,7 +55,7 @@ __device__ __forceinline__ bool is_anchor(const uint32_t *bits, long long v)
     return (__ldg(bits + (v >> 5)) >> (v & 31)) & 1u;
 }
 
-enum Pass { kMark = 0, kCount = 1, kFill = 2 };
+enum Pass { kMark = 0, kCount = 1, kFill = 2, kRhs = 3 };
 
 struct Sink {
     const uint32_t *bits;
@@ -78,6 +78,10 @@ __device__ __forceinline__ void emit(const Sink &S, long long v, long long start
     if (PASS == kMark) return;
     if (!is_anchor(S.bits, v)) return;
     int row = __ldg(S.id + v);
+    if (PASS == kRhs) {  // plain method, operator cached: only b = sum I is field-dependent
+        atomicAdd(S.b + row, I);
+        return;
+    }
     if (PASS == kCount) {
         atomicAdd(S.rowcnt + row, 1u);
     } else {
@@ -134,8 +138,9 @@ __global__ void __launch_bounds__(256) k_anchor_plain(Grid g, const LineRec *__r
     L.init(g, r, gbase, desc, li);
     const long long e = r.e;
     emit<PASS>(S, e, e, 1.0f, 0.0f);
+    constexpr bool kGrad = PASS == kFill || PASS == kRhs;
     float4 gl = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (PASS == kFill) gl = load_grad<BF16>(f32, b16, e);
+    if (kGrad) gl = load_grad<BF16>(f32, b16, e);
     float I = 0.0f, comp = 0.0f;
     for (int s0 = 0; s0 < L.m; s0 += 16) {
         uint32_t w = __ldg(L.dp + 32 * (s0 >> 4));
@@ -143,7 +148,7 @@ __global__ void __launch_bounds__(256) k_anchor_plain(Grid g, const LineRec *__r
         for (int t = 0; t < n; t++, w >>= 2) {
             int a = (int)(w & 3u);
             L.v += a == 0 ? L.d0 : (a == 1 ? L.d1 : L.d2);
-            if (PASS == kFill) {
+            if (kGrad) {
                 float4 gv = load_grad<BF16>(f32, b16, L.v);
                 kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
                 gl = gv;
@@ -269,6 +274,28 @@ __global__ void __launch_bounds__(256) k_anchor_spmv(long long n, const unsigned
     }
 }
 
+// Plain method: every weight is 1, so a row is a plain sum of gathered anchor values.
+__global__ void __launch_bounds__(256) k_anchor_spmv_unit(long long n, const unsigned long long *__restrict__ rowptr,
+                                                          const uint32_t *__restrict__ col, const float *__restrict__ b,
+                                                          const float *__restrict__ c, const uint32_t *__restrict__ vox,
+                                                          const float *__restrict__ p_init, int seed,
+                                                          const float *__restrict__ pc, float *__restrict__ pn)
+{
+    long long row = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (row >= n) return;  // whole warps
+    unsigned long long j0 = rowptr[row], j1 = rowptr[row + 1];
+    float s = 0.0f;
+    for (unsigned long long j = j0 + lane; j < j1; j += 32) s += __ldg(pc + __ldg(col + j));
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+        float cc = c[row];
+        float numer = b[row] + s;
+        if (seed && p_init) numer += p_init[vox[row]];
+        pn[row] = cc > 0.0f ? __fdiv_rn(numer, cc) : pc[row];
+    }
+}
+
 constexpr int kRedBlocks = 256, kRedThreads = 256;
 
 __device__ __forceinline__ double block_sum(double x, double *sh)
@@ -283,44 +310,52 @@ __device__ __forceinline__ double block_sum(double x, double *sh)
     return s;
 }
 
-// Sums of (d, p) over the anchors (for the mean gauge).
-__global__ void k_sum_dp(long long n, const float *pc, const float *pn, double *part)
+// Sums of (d, p, 1) over the selected entries (for the mean gauge).
+__global__ void k_sum_dp(long long n, const float *pc, const float *pn, const uint8_t *mask, double *part)
 {
     __shared__ double sh[32];
-    double sd = 0.0, sp = 0.0;
+    double sd = 0.0, sp = 0.0, cn = 0.0;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        if (mask && !mask[i]) continue;
         sd += (double)pn[i] - (double)pc[i];
         sp += (double)pn[i];
+        cn += 1.0;
     }
-    double a = block_sum(sd, sh), bb = block_sum(sp, sh);
-    if (threadIdx.x == 0) { part[2 * blockIdx.x] = a; part[2 * blockIdx.x + 1] = bb; }
+    double a = block_sum(sd, sh), bb = block_sum(sp, sh), cc = block_sum(cn, sh);
+    if (threadIdx.x == 0) {
+        part[3 * blockIdx.x] = a;
+        part[3 * blockIdx.x + 1] = bb;
+        part[3 * blockIdx.x + 2] = cc;
+    }
 }
 
-__global__ void k_finish(const double *part, int nblk, int width, double *out, double scale)
+__global__ void k_finish(const double *part, int nblk, int width, double *out)
 {
     if ((int)threadIdx.x < width) {
         double s = 0.0;
         for (int i = 0; i < nblk; i++) s += part[width * i + threadIdx.x];
-        out[threadIdx.x] = s * scale;
+        out[threadIdx.x] = s;
     }
 }
 
-// Gauged squared change and squared norm: sum (d - sd)^2, sum (p - sp)^2.  The shifts are
-// the reference anchor's change and value (point gauge), the means (mean gauge) or 0.
-__global__ void k_change(long long n, const float *pc, const float *pn, int gauge, long long ref,
-                         const double *means, double *part)
+// Gauged squared change and squared norm over the selected entries: sum (d - sd)^2 and
+// sum (p - sp)^2.  The shifts are the reference entry's change and value (point gauge),
+// the means (mean gauge: sums[0..2] = sum d, sum p, count) or 0.
+__global__ void k_change(long long n, const float *pc, const float *pn, const uint8_t *mask, int gauge,
+                         long long ref, const double *sums, double *part)
 {
     __shared__ double sh[32];
     double sd = 0.0, sp = 0.0;
     if (gauge == OMNI3D_GAUGE_POINT && ref >= 0) {
         sp = (double)pn[ref];
         sd = sp - (double)pc[ref];
-    } else if (gauge == OMNI3D_GAUGE_MEAN) {
-        sd = means[0];
-        sp = means[1];
+    } else if (gauge == OMNI3D_GAUGE_MEAN && sums[2] > 0) {
+        sd = sums[0] / sums[2];
+        sp = sums[1] / sums[2];
     }
     double a = 0.0, bb = 0.0;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        if (mask && !mask[i]) continue;
         double d = (double)pn[i] - (double)pc[i] - sd;
         double q = (double)pn[i] - sp;
         a += d * d;
@@ -387,76 +422,86 @@ cudaError_t run_pass(const Geometry &geo, const Field &f, int method, bool bf16,
         }                                                                      \
     } while (0)
 
+size_t change_scratch_doubles();
+
+// Grow-only device buffer: reallocates only when `bytes` exceeds the recorded capacity.
+template <typename T>
+cudaError_t grow(T *&p, size_t &cap, size_t bytes)
+{
+    if (bytes == 0) bytes = 1;
+    if (bytes <= cap && p) return cudaSuccess;
+    cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e == cudaSuccess) cap = bytes;
+    return e;
+}
+
 void anchor_free(Anchor *A)
 {
     cudaFree(A->flag); cudaFree(A->bits); cudaFree(A->id); cudaFree(A->vox); cudaFree(A->rowptr);
     cudaFree(A->col); cudaFree(A->w); cudaFree(A->b); cudaFree(A->c); cudaFree(A->pa); cudaFree(A->pb);
-    cudaFree(A->red);
+    cudaFree(A->red); cudaFree(A->u); cudaFree(A->pos); cudaFree(A->tmp); cudaFree(A->cnt64); cudaFree(A->tmp64);
     *A = Anchor();
 }
 
 cudaError_t anchor_build(const Geometry &geo, const Field &f, int method, bool bf16, long long ref_voxel,
                          Anchor *A, cudaStream_t st, std::string *err)
 {
-    anchor_free(A);
     const long long V = geo.grid.V;
-    AN_TRY(cudaMalloc(&A->flag, (size_t)V));
-    AN_TRY(cudaMalloc(&A->bits, sizeof(uint32_t) * (size_t)((V + 31) / 32)));
-    AN_TRY(cudaMalloc(&A->id, sizeof(int32_t) * (size_t)V));
+    size_t *cap = A->cap;
+    AN_TRY(grow(A->flag, cap[0], (size_t)V));
+    AN_TRY(grow(A->bits, cap[1], sizeof(uint32_t) * (size_t)((V + 31) / 32)));
+    AN_TRY(grow(A->id, cap[2], sizeof(int32_t) * (size_t)V));
+    AN_TRY(grow(A->u, cap[3], sizeof(uint32_t) * (size_t)V));
+    AN_TRY(grow(A->pos, cap[4], sizeof(uint32_t) * (size_t)(V + 1)));
+    AN_TRY(grow(A->tmp, cap[5], sizeof(uint32_t) * scan_tmp_elems(V)));
+    AN_TRY(grow(A->red, cap[6], sizeof(double) * change_scratch_doubles()));
     AN_TRY(cudaMemsetAsync(A->flag, 0, (size_t)V, st));
     Sink S{};
     S.flag = A->flag;
     AN_TRY(run_pass<kMark>(geo, f, method, bf16, S, st));
     if (ref_voxel >= 0 && ref_voxel < V) AN_TRY(cudaMemsetAsync(A->flag + ref_voxel, 1, 1, st));
 
-    uint32_t *u = nullptr, *pos = nullptr, *tmp = nullptr;
-    AN_TRY(cudaMalloc(&u, sizeof(uint32_t) * (size_t)V));
-    AN_TRY(cudaMalloc(&pos, sizeof(uint32_t) * (size_t)(V + 1)));
-    AN_TRY(cudaMalloc(&tmp, sizeof(uint32_t) * scan_tmp_elems(V)));
-    k_flag_to_u32<<<grid_for(V), 256, 0, st>>>(V, A->flag, u);
+    k_flag_to_u32<<<grid_for(V), 256, 0, st>>>(V, A->flag, A->u);
     OM_COUNT_LAUNCH();
     AN_TRY(cudaGetLastError());
-    AN_TRY(exclusive_scan_u32(u, pos, V, tmp, st));
+    AN_TRY(exclusive_scan_u32(A->u, A->pos, V, A->tmp, st));
     uint32_t n = 0;
-    AN_TRY(cudaMemcpyAsync(&n, pos + V, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    AN_TRY(cudaMemcpyAsync(&n, A->pos + V, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     AN_TRY(cudaStreamSynchronize(st));
     A->n = n;
-    AN_TRY(cudaMalloc(&A->vox, sizeof(uint32_t) * (size_t)std::max<long long>(n, 1)));
-    k_assign_ids<<<grid_for(V), 256, 0, st>>>(V, A->flag, pos, A->id, A->vox, A->bits);
+    AN_TRY(grow(A->vox, cap[7], sizeof(uint32_t) * (size_t)n));
+    k_assign_ids<<<grid_for(V), 256, 0, st>>>(V, A->flag, A->pos, A->id, A->vox, A->bits);
     OM_COUNT_LAUNCH();
     AN_TRY(cudaGetLastError());
 
     // rows
-    uint32_t *rowcnt = u;  // reuse: n <= V
+    uint32_t *rowcnt = A->u;  // reuse: n <= V
     AN_TRY(cudaMemsetAsync(rowcnt, 0, sizeof(uint32_t) * (size_t)std::max<long long>(n, 1), st));
     S.bits = A->bits;
     S.id = A->id;
     S.rowcnt = rowcnt;
     AN_TRY(run_pass<kCount>(geo, f, method, bf16, S, st));
-    unsigned long long *cnt64 = nullptr, *tmp64 = nullptr;
-    AN_TRY(cudaMalloc(&cnt64, sizeof(unsigned long long) * (size_t)std::max<long long>(n, 1)));
-    AN_TRY(cudaMalloc(&tmp64, sizeof(unsigned long long) * scan_tmp_elems(n)));
-    AN_TRY(cudaMalloc(&A->rowptr, sizeof(unsigned long long) * (size_t)(n + 1)));
-    k_u32_to_u64<<<grid_for(n), 256, 0, st>>>(n, rowcnt, cnt64);
+    AN_TRY(grow(A->cnt64, cap[8], sizeof(unsigned long long) * (size_t)n));
+    AN_TRY(grow(A->tmp64, cap[9], sizeof(unsigned long long) * scan_tmp_elems(n)));
+    AN_TRY(grow(A->rowptr, cap[10], sizeof(unsigned long long) * (size_t)(n + 1)));
+    k_u32_to_u64<<<grid_for(n), 256, 0, st>>>(n, rowcnt, A->cnt64);
     OM_COUNT_LAUNCH();
     AN_TRY(cudaGetLastError());
-    AN_TRY(exclusive_scan_u64(cnt64, A->rowptr, n, tmp64, st));
+    AN_TRY(exclusive_scan_u64(A->cnt64, A->rowptr, n, A->tmp64, st));
     unsigned long long nnz = 0;
     AN_TRY(cudaMemcpyAsync(&nnz, A->rowptr + n, sizeof(nnz), cudaMemcpyDeviceToHost, st));
     AN_TRY(cudaStreamSynchronize(st));
     A->nnz = (long long)nnz;
-    cudaFree(cnt64);
-    cudaFree(tmp64);
-    cudaFree(pos);
-    cudaFree(tmp);
 
-    AN_TRY(cudaMalloc(&A->col, sizeof(uint32_t) * (size_t)std::max<unsigned long long>(nnz, 1)));
-    AN_TRY(cudaMalloc(&A->w, sizeof(float) * (size_t)std::max<unsigned long long>(nnz, 1)));
-    AN_TRY(cudaMalloc(&A->b, sizeof(float) * (size_t)std::max<long long>(n, 1)));
-    AN_TRY(cudaMalloc(&A->c, sizeof(float) * (size_t)std::max<long long>(n, 1)));
-    AN_TRY(cudaMalloc(&A->pa, sizeof(float) * (size_t)std::max<long long>(n, 1)));
-    AN_TRY(cudaMalloc(&A->pb, sizeof(float) * (size_t)std::max<long long>(n, 1)));
-    AN_TRY(cudaMalloc(&A->red, sizeof(double) * (size_t)(8 + 2 * kRedBlocks)));
+    AN_TRY(grow(A->col, cap[11], sizeof(uint32_t) * (size_t)nnz));
+    AN_TRY(grow(A->w, cap[12], sizeof(float) * (size_t)nnz));
+    AN_TRY(grow(A->b, cap[13], sizeof(float) * (size_t)n));
+    AN_TRY(grow(A->c, cap[14], sizeof(float) * (size_t)n));
+    AN_TRY(grow(A->pa, cap[15], sizeof(float) * (size_t)n));
+    AN_TRY(grow(A->pb, cap[16], sizeof(float) * (size_t)n));
     uint32_t *cursor = rowcnt;
     AN_TRY(cudaMemsetAsync(cursor, 0, sizeof(uint32_t) * (size_t)std::max<long long>(n, 1), st));
     AN_TRY(cudaMemsetAsync(A->b, 0, sizeof(float) * (size_t)std::max<long long>(n, 1), st));
@@ -468,28 +513,40 @@ cudaError_t anchor_build(const Geometry &geo, const Field &f, int method, bool b
     S.b = A->b;
     S.c = A->c;
     AN_TRY(run_pass<kFill>(geo, f, method, bf16, S, st));
-    AN_TRY(cudaStreamSynchronize(st));
-    cudaFree(u);
-    return cudaSuccess;
+    A->unit_weights = method == OMNI3D_METHOD_PLAIN;
+    return cudaGetLastError();
 }
 
-size_t change_scratch_doubles() { return 8 + 2 * kRedBlocks; }
+size_t change_scratch_doubles() { return 8 + 3 * kRedBlocks; }
 
 cudaError_t change_sums(long long n, const float *pc, const float *pn, int gauge, long long ref, double *scratch,
-                        double *out2, cudaStream_t st)
+                        double *out2, cudaStream_t st, const uint8_t *mask)
 {
     double *part = scratch + 8;
     if (gauge == OMNI3D_GAUGE_MEAN) {
-        k_sum_dp<<<kRedBlocks, kRedThreads, 0, st>>>(n, pc, pn, part);
+        k_sum_dp<<<kRedBlocks, kRedThreads, 0, st>>>(n, pc, pn, mask, part);
         OM_COUNT_LAUNCH();
-        k_finish<<<1, 32, 0, st>>>(part, kRedBlocks, 2, scratch + 4, 1.0 / (double)std::max(n, 1LL));
+        k_finish<<<1, 32, 0, st>>>(part, kRedBlocks, 3, scratch + 4);
         OM_COUNT_LAUNCH();
     }
-    k_change<<<kRedBlocks, kRedThreads, 0, st>>>(n, pc, pn, gauge, ref, scratch + 4, part);
+    k_change<<<kRedBlocks, kRedThreads, 0, st>>>(n, pc, pn, mask, gauge, ref, scratch + 4, part);
     OM_COUNT_LAUNCH();
-    k_finish<<<1, 32, 0, st>>>(part, kRedBlocks, 2, out2, 1.0);
+    k_finish<<<1, 32, 0, st>>>(part, kRedBlocks, 2, out2);
     OM_COUNT_LAUNCH();
     return cudaGetLastError();
+}
+
+cudaError_t anchor_mark(const Geometry &geo, const Field &f, int method, bool bf16, long long ref_voxel,
+                        uint8_t *flag, cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(flag, 0, (size_t)geo.grid.V, st);
+    if (e != cudaSuccess) return e;
+    Sink S{};
+    S.flag = flag;
+    e = run_pass<kMark>(geo, f, method, bf16, S, st);
+    if (e != cudaSuccess) return e;
+    if (ref_voxel >= 0 && ref_voxel < geo.grid.V) e = cudaMemsetAsync(flag + ref_voxel, 1, 1, st);
+    return e;
 }
 
 cudaError_t anchor_step(const Anchor &A, const float *p_init, bool seed, int gauge, long long ref_anchor,
@@ -497,11 +554,27 @@ cudaError_t anchor_step(const Anchor &A, const float *p_init, bool seed, int gau
 {
     if (A.n == 0) return cudaSuccess;
     long long threads = A.n * 32;
-    k_anchor_spmv<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(A.n, A.rowptr, A.col, A.w, A.b, A.c, A.vox,
-                                                                      p_init, seed ? 1 : 0, p_cur, p_next);
+    if (A.unit_weights)
+        k_anchor_spmv_unit<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(A.n, A.rowptr, A.col, A.b, A.c, A.vox,
+                                                                               p_init, seed ? 1 : 0, p_cur, p_next);
+    else
+        k_anchor_spmv<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(A.n, A.rowptr, A.col, A.w, A.b, A.c,
+                                                                          A.vox, p_init, seed ? 1 : 0, p_cur, p_next);
     OM_COUNT_LAUNCH();
-    if (red2) return change_sums(A.n, p_cur, p_next, gauge, ref_anchor, A.red, red2, st);
+    if (red2) return change_sums(A.n, p_cur, p_next, gauge, ref_anchor, A.red, red2, st, nullptr);
     return cudaGetLastError();
+}
+
+cudaError_t anchor_refresh_rhs(const Geometry &geo, const Field &f, bool bf16, Anchor *A, cudaStream_t st)
+{
+    if (A->n == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(A->b, 0, sizeof(float) * (size_t)A->n, st);
+    if (e != cudaSuccess) return e;
+    Sink S{};
+    S.bits = A->bits;
+    S.id = A->id;
+    S.b = A->b;
+    return run_pass<kRhs>(geo, f, OMNI3D_METHOD_PLAIN, bf16, S, st);
 }
 
 cudaError_t anchor_scatter(const Anchor &A, const float *pa, float *vol, cudaStream_t st)

@@ -117,21 +117,37 @@ struct Anchor {
     float *c = nullptr;             // n: sum of w
     float *pa = nullptr, *pb = nullptr;  // iterates
     double *red = nullptr;          // reduction scratch
+    bool unit_weights = false;      // plain method: every w is 1 (the w array is unused)
+    // build scratch (kept between builds)
+    uint32_t *u = nullptr, *pos = nullptr, *tmp = nullptr;
+    unsigned long long *cnt64 = nullptr, *tmp64 = nullptr;
+    // capacities in bytes, one per buffer above, so that rebuilding for a new field of the
+    // same geometry allocates nothing
+    size_t cap[20] = {};
 };
 cudaError_t anchor_build(const Geometry &geo, const Field &f, int method, bool bf16,
                          long long ref_voxel, Anchor *A, cudaStream_t st, std::string *err);
 void anchor_free(Anchor *A);
+// Plain method: recompute only b (the field-dependent part) of an operator built by
+// anchor_build for the same geometry; rows, columns and c depend on the geometry alone.
+cudaError_t anchor_refresh_rhs(const Geometry &geo, const Field &f, bool bf16, Anchor *A,
+                               cudaStream_t st);
 // One iteration p_next = (b + seed * p_init_a + M p_cur) / c; accumulates the gauged
 // change / norm sums into red[0..1] for the relative change.
 cudaError_t anchor_step(const Anchor &A, const float *p_init, bool seed, int gauge,
                         long long ref_anchor, const float *p_cur, float *p_next, double *red2,
                         cudaStream_t st);
-// Gauged relative-change sums over n values: out2 = {sum (d - d_ref)^2, sum (p - p_ref)^2}
-// with d = pn - pc; the shift is the value at `ref` (point gauge), the mean (mean gauge)
-// or zero.  Deterministic FP64 reduction; scratch holds change_scratch_doubles().
+// Gauged relative-change sums over the n values selected by mask (all when mask is null):
+// out2 = {sum (d - d_ref)^2, sum (p - p_ref)^2} with d = pn - pc; the shift is the value at
+// `ref` (point gauge), the mean (mean gauge) or zero.  Deterministic FP64 reduction;
+// scratch holds change_scratch_doubles().
 size_t change_scratch_doubles();
 cudaError_t change_sums(long long n, const float *pc, const float *pn, int gauge, long long ref,
-                        double *scratch, double *out2, cudaStream_t st);
+                        double *scratch, double *out2, cudaStream_t st, const uint8_t *mask);
+// Flag the anchor voxels (line entries, or segment starts of the selected method, plus
+// ref_voxel when >= 0) into a V-byte array.
+cudaError_t anchor_mark(const Geometry &geo, const Field &f, int method, bool bf16,
+                        long long ref_voxel, uint8_t *flag, cudaStream_t st);
 // Scatter anchor values into a volume.
 cudaError_t anchor_scatter(const Anchor &A, const float *pa, float *vol, cudaStream_t st);
 // Gather anchor values from a volume.
