@@ -93,6 +93,9 @@ typedef struct {
     double ms_total;           /* device time of the whole solve */
     double ms_sweep;           /* device time of the final full sweep kernel alone */
     long long kernel_launches; /* CUDA kernels this library launched during the call */
+    int solver_used;           /* OMNI3D_SOLVER_*: the anchor solver falls back to the sweep
+                                  solver when its operator would cost more than a quarter of a
+                                  sweep per iteration (many scattered segment starts) */
 } omni3d_stats;
 
 /* Fill *p with the reference's defaults (K:8512-8535) and this implementation's. */
@@ -147,7 +150,9 @@ int omni3d_geometry_info(omni3d_ctx *ctx, long long *n_lines, long long *n_units
                          long long *walk_errors);
 
 /* Copy the line table to host memory: per line {entry voxel, exit voxel, direction, steps}
- * (4 x int32) in (direction, lattice point) order; n_max rows at most. */
+ * (4 x int32), n_max rows at most.  Lines are stored direction by direction in the
+ * library's processing order (neighbouring directions adjacent) and, within a direction,
+ * in lattice-point order; the direction column is the index in the caller's list. */
 int omni3d_line_table(omni3d_ctx *ctx, int32_t *rows, long long n_max);
 
 /* Copy the staircase of line `line` (one axis code 0/1/2 per step) to host memory. */

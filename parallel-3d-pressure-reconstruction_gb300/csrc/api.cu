@@ -123,6 +123,31 @@ DirEntry make_dir(float k1, float k2, float k3)
     return D;
 }
 
+// Processing order of the directions: serpentine bands of polar angle, each band ordered
+// by azimuth, so that consecutive directions are neighbours on the sphere.  Lines are
+// traced and swept in this order; the few directions in flight at a time then sweep nearly
+// coincident sheets of the volume and share the gradient and accumulator lines in L2.
+std::vector<int> sphere_order(const std::vector<float> &dirs)
+{
+    const int n = (int)(dirs.size() / 3);
+    const double PI = 3.14159265358979323846;
+    int nb = std::max(1, (int)std::lround(std::sqrt(n / 2.0)));
+    std::vector<std::pair<std::pair<int, double>, int>> key;
+    key.reserve(n);
+    for (int d = 0; d < n; d++) {
+        double k1 = dirs[3 * d], k2 = dirs[3 * d + 1], k3 = dirs[3 * d + 2];
+        double r = std::sqrt(k1 * k1 + k2 * k2 + k3 * k3);
+        double th = std::acos(std::max(-1.0, std::min(1.0, r > 0 ? k3 / r : 1.0)));
+        double ph = std::atan2(k2, k1);
+        int b = std::min(nb - 1, (int)(th / PI * nb));
+        key.push_back({{b, (b & 1) ? -ph : ph}, d});
+    }
+    std::sort(key.begin(), key.end());
+    std::vector<int> order(n);
+    for (int i = 0; i < n; i++) order[i] = key[i].second;
+    return order;
+}
+
 int check_params(const omni3d_params *p, std::string *why)
 {
     if (!p) { *why = "params is NULL"; return OMNI3D_ERR_ARG; }
@@ -249,8 +274,10 @@ int omni3d_create(const omni3d_params *params, omni3d_ctx **out)
     ctx->prm = *params;
     ctx->dirs.assign(params->dirs, params->dirs + 3 * (size_t)params->n_dirs);
     ctx->prm.dirs = ctx->dirs.data();
-    for (int d = 0; d < params->n_dirs; d++)
+    for (int d : sphere_order(ctx->dirs)) {
         ctx->table.push_back(make_dir(ctx->dirs[3 * d], ctx->dirs[3 * d + 1], ctx->dirs[3 * d + 2]));
+        ctx->table.back().orig = d;
+    }
 
     Grid &g = ctx->geo.grid;
     g.X = params->nx;
@@ -348,6 +375,7 @@ int omni3d_line_table(omni3d_ctx *ctx, int32_t *rows, long long n_max)
     cudaSetDevice(ctx->prm.device);
     CK(ctx, cudaMemcpyAsync(rows, ctx->geo.d_lines, sizeof(LineRec) * (size_t)n, cudaMemcpyDeviceToHost, ctx->st));
     CK(ctx, cudaStreamSynchronize(ctx->st));
+    for (long long i = 0; i < n; i++) rows[4 * i + 2] = ctx->table[rows[4 * i + 2]].orig;
     return OMNI3D_OK;
 }
 
@@ -506,6 +534,29 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
     double hred[2];
     long long n_anchor = 0, n_links = 0;
 
+    int solver = P.solver;
+    Anchor &A = ctx->anc;
+    long long ref_anchor = -1;
+    if (K > 0 && solver == OMNI3D_SOLVER_ANCHOR) {
+        std::string aerr;
+        cudaError_t e;
+        if (P.method == OMNI3D_METHOD_PLAIN && ctx->anc_cached) {
+            e = anchor_refresh_rhs(ctx->geo, F, bf16, &ctx->anc, st);
+            aerr = cudaGetErrorString(e);
+        } else {
+            ctx->anc_cached = false;
+            e = anchor_build(ctx->geo, F, P.method, bf16, P.gauge == OMNI3D_GAUGE_POINT ? ref : -1,
+                             ctx->geo.n_units / 4, &ctx->anc, st, &aerr);
+            ctx->anc_cached = e == cudaSuccess && P.method == OMNI3D_METHOD_PLAIN;
+        }
+        if (e == cudaErrorNotSupported) {
+            cudaGetLastError();
+            solver = OMNI3D_SOLVER_SWEEP;  // operator not profitable: one sweep per iteration
+        } else if (e != cudaSuccess) {
+            return fail(ctx, e == cudaErrorMemoryAllocation ? OMNI3D_ERR_NOMEM : OMNI3D_ERR_CUDA,
+                        "anchor operator: " + aerr);
+        }
+    }
     if (K == 0) {
         cudaEventRecord(ctx->ev[5], st);
         cudaEventRecord(ctx->ev[6], st);
@@ -513,7 +564,7 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
         CK(ctx, cudaMemsetAsync(dcnt, 0, sizeof(float) * (size_t)V, st));
         cudaEventRecord(ctx->ev[1], st);
         cudaEventRecord(ctx->ev[2], st);
-    } else if (P.solver == OMNI3D_SOLVER_SWEEP) {
+    } else if (solver == OMNI3D_SOLVER_SWEEP) {
         // the reference loop: NoItr x {sweep, devidecountInner}
         CK(ctx, ctx->pvol_b.ensure(sizeof(float) * (size_t)V));
         float *pc = ctx->pvol_a.as<float>(), *pn = ctx->pvol_b.as<float>();
@@ -521,9 +572,11 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
         // the convergence test runs over the anchor voxels, as in the anchor solver
         uint8_t *amask = nullptr;
         if (P.tol > 0.0) {
-            CK(ctx, ctx->flags.ensure((size_t)V));
+            CK(ctx, ctx->flags.ensure((size_t)V + 64));
             amask = ctx->flags.as<uint8_t>();
-            CK(ctx, anchor_mark(ctx->geo, F, P.method, bf16, P.gauge == OMNI3D_GAUGE_POINT ? ref : -1, amask, st));
+            unsigned long long *cnt1 = reinterpret_cast<unsigned long long *>(amask + ((V + 7) / 8) * 8);
+            CK(ctx, anchor_mark(ctx->geo, F, P.method, bf16, P.gauge == OMNI3D_GAUGE_POINT ? ref : -1, amask, cnt1,
+                                st));
         }
         cudaEventRecord(ctx->ev[1], st);
         for (int it = 1; it <= K; it++) {
@@ -547,23 +600,8 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
         CK(ctx, cudaMemcpyAsync(dout, pc, sizeof(float) * (size_t)V, cudaMemcpyDeviceToDevice, st));
     } else {
         // anchor form: iterate the anchors, then one full sweep
-        std::string aerr;
-        cudaError_t e;
-        if (P.method == OMNI3D_METHOD_PLAIN && ctx->anc_cached) {
-            e = anchor_refresh_rhs(ctx->geo, F, bf16, &ctx->anc, st);
-            aerr = cudaGetErrorString(e);
-        } else {
-            ctx->anc_cached = false;
-            e = anchor_build(ctx->geo, F, P.method, bf16, P.gauge == OMNI3D_GAUGE_POINT ? ref : -1, &ctx->anc, st,
-                             &aerr);
-            ctx->anc_cached = e == cudaSuccess && P.method == OMNI3D_METHOD_PLAIN;
-        }
-        if (e != cudaSuccess) return fail(ctx, e == cudaErrorMemoryAllocation ? OMNI3D_ERR_NOMEM : OMNI3D_ERR_CUDA,
-                                          "anchor operator: " + aerr);
-        Anchor &A = ctx->anc;
         n_anchor = A.n;
         n_links = A.nnz;
-        long long ref_anchor = -1;
         if (P.gauge == OMNI3D_GAUGE_POINT) {
             int32_t ra = -1;
             CK(ctx, cudaMemcpyAsync(&ra, A.id + ref, sizeof(ra), cudaMemcpyDeviceToHost, st));
@@ -623,6 +661,7 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
         stats->ms_total = ms_between(ctx->ev[0], ctx->ev[4]);
         stats->ms_sweep = ms_between(ctx->ev[5], ctx->ev[6]);
         stats->kernel_launches = (long long)(__atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED) - launches0);
+        stats->solver_used = solver;
     }
     if (ctx->geo.walk_errors) return fail(ctx, OMNI3D_ERR_NUMERIC, "line walk hit the wrong-point branch");
     return OMNI3D_OK;

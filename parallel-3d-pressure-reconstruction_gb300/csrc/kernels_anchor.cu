@@ -176,7 +176,9 @@ __global__ void __launch_bounds__(256) k_anchor_select(Grid g, const LineRec *__
     const float thr = g.thr;
     float4 gl = make_float4(0.f, 0.f, 0.f, 0.f);
     if (PASS == kFill) gl = load_grad<BF16>(f32, b16, L.v);
-    float ce = __ldg(curl + L.v);
+    // the FP32 field carries curl in .w: one gather per step in the filling pass
+    constexpr bool kW = PASS == kFill && !BF16;
+    float ce = kW ? gl.w : __ldg(curl + L.v);
     bool started = !(ce == 0.0f || ce > thr);
     bool paused = false;
     long long start = L.v;
@@ -190,7 +192,7 @@ __global__ void __launch_bounds__(256) k_anchor_select(Grid g, const LineRec *__
             L.v += a == 0 ? L.d0 : (a == 1 ? L.d1 : L.d2);
             float4 gv = make_float4(0.f, 0.f, 0.f, 0.f);
             if (PASS == kFill) gv = load_grad<BF16>(f32, b16, L.v);
-            float cn = __ldg(curl + L.v);
+            float cn = kW ? gv.w : __ldg(curl + L.v);
             if (!started) {
                 bool ok = (a == 0) ? (cn != 0.0f && cn < thr) : (cn != 0.0f);
                 if (ok) {
@@ -221,6 +223,35 @@ __global__ void __launch_bounds__(256) k_anchor_select(Grid g, const LineRec *__
             gl = gv;
         }
     }
+}
+
+// Selected method: a voxel can start a segment only if it is on the boundary (a line entry)
+// or if the voxel before it on some line is "bad" (curl == 0 or curl >= thr): a start
+// before the first good voxel follows a voxel that failed the start test, and a restart
+// follows a voxel that paused or kept the pause (K:2300-2506).  Flags that superset and
+// counts it into *count.
+__global__ void k_select_candidates(Grid g, const float *__restrict__ curl, uint8_t *flag,
+                                    unsigned long long *count)
+{
+    const long long X = g.X, Y = g.Y, Z = g.Z, XY = g.XY;
+    unsigned long long local = 0;
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < g.V;
+         v += (long long)gridDim.x * blockDim.x) {
+        long long i = v % X, j = (v / X) % Y, k = v / XY;
+        bool c = i == 0 || i == X - 1 || j == 0 || j == Y - 1 || k == 0 || k == Z - 1;
+        if (!c) {
+            const long long nb[6] = {v - 1, v + 1, v - X, v + X, v - XY, v + XY};
+#pragma unroll
+            for (int q = 0; q < 6; q++) {
+                float cu = __ldg(curl + nb[q]);
+                c |= (cu == 0.0f || cu >= g.thr);
+            }
+        }
+        flag[v] = c ? 1 : 0;
+        local += c ? 1 : 0;
+    }
+    for (int o = 16; o; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, local);
 }
 
 __global__ void k_flag_to_u32(long long V, const uint8_t *flag, uint32_t *out)
@@ -447,7 +478,7 @@ void anchor_free(Anchor *A)
 }
 
 cudaError_t anchor_build(const Geometry &geo, const Field &f, int method, bool bf16, long long ref_voxel,
-                         Anchor *A, cudaStream_t st, std::string *err)
+                         long long max_nnz, Anchor *A, cudaStream_t st, std::string *err)
 {
     const long long V = geo.grid.V;
     size_t *cap = A->cap;
@@ -458,10 +489,26 @@ cudaError_t anchor_build(const Geometry &geo, const Field &f, int method, bool b
     AN_TRY(grow(A->pos, cap[4], sizeof(uint32_t) * (size_t)(V + 1)));
     AN_TRY(grow(A->tmp, cap[5], sizeof(uint32_t) * scan_tmp_elems(V)));
     AN_TRY(grow(A->red, cap[6], sizeof(double) * change_scratch_doubles()));
-    AN_TRY(cudaMemsetAsync(A->flag, 0, (size_t)V, st));
     Sink S{};
     S.flag = A->flag;
-    AN_TRY(run_pass<kMark>(geo, f, method, bf16, S, st));
+    bool marked = false;
+    if (method == OMNI3D_METHOD_SELECT) {
+        // cheap superset of the segment starts; used when it stays small
+        AN_TRY(grow(A->cnt64, cap[8], sizeof(unsigned long long) * 1));
+        unsigned long long *dcount = A->cnt64;
+        AN_TRY(cudaMemsetAsync(dcount, 0, sizeof(unsigned long long), st));
+        k_select_candidates<<<grid_for(V), 256, 0, st>>>(geo.grid, f.curl, A->flag, dcount);
+        OM_COUNT_LAUNCH();
+        AN_TRY(cudaGetLastError());
+        unsigned long long nc = 0;
+        AN_TRY(cudaMemcpyAsync(&nc, dcount, sizeof(nc), cudaMemcpyDeviceToHost, st));
+        AN_TRY(cudaStreamSynchronize(st));
+        marked = (long long)nc <= V / 16;
+    }
+    if (!marked) {
+        AN_TRY(cudaMemsetAsync(A->flag, 0, (size_t)V, st));
+        AN_TRY(run_pass<kMark>(geo, f, method, bf16, S, st));
+    }
     if (ref_voxel >= 0 && ref_voxel < V) AN_TRY(cudaMemsetAsync(A->flag + ref_voxel, 1, 1, st));
 
     k_flag_to_u32<<<grid_for(V), 256, 0, st>>>(V, A->flag, A->u);
@@ -495,6 +542,10 @@ cudaError_t anchor_build(const Geometry &geo, const Field &f, int method, bool b
     AN_TRY(cudaMemcpyAsync(&nnz, A->rowptr + n, sizeof(nnz), cudaMemcpyDeviceToHost, st));
     AN_TRY(cudaStreamSynchronize(st));
     A->nnz = (long long)nnz;
+    if (max_nnz >= 0 && (long long)nnz > max_nnz) {
+        if (err) *err = "anchor operator larger than its limit";
+        return cudaErrorNotSupported;
+    }
 
     AN_TRY(grow(A->col, cap[11], sizeof(uint32_t) * (size_t)nnz));
     AN_TRY(grow(A->w, cap[12], sizeof(float) * (size_t)nnz));
@@ -537,14 +588,30 @@ cudaError_t change_sums(long long n, const float *pc, const float *pn, int gauge
 }
 
 cudaError_t anchor_mark(const Geometry &geo, const Field &f, int method, bool bf16, long long ref_voxel,
-                        uint8_t *flag, cudaStream_t st)
+                        uint8_t *flag, unsigned long long *count1, cudaStream_t st)
 {
-    cudaError_t e = cudaMemsetAsync(flag, 0, (size_t)geo.grid.V, st);
-    if (e != cudaSuccess) return e;
-    Sink S{};
-    S.flag = flag;
-    e = run_pass<kMark>(geo, f, method, bf16, S, st);
-    if (e != cudaSuccess) return e;
+    const long long V = geo.grid.V;
+    cudaError_t e;
+    bool marked = false;
+    if (method == OMNI3D_METHOD_SELECT) {
+        e = cudaMemsetAsync(count1, 0, sizeof(unsigned long long), st);
+        if (e != cudaSuccess) return e;
+        k_select_candidates<<<grid_for(V), 256, 0, st>>>(geo.grid, f.curl, flag, count1);
+        OM_COUNT_LAUNCH();
+        unsigned long long nc = 0;
+        e = cudaMemcpyAsync(&nc, count1, sizeof(nc), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return e;
+        marked = (long long)nc <= V / 16;
+    }
+    if (!marked) {
+        e = cudaMemsetAsync(flag, 0, (size_t)V, st);
+        if (e != cudaSuccess) return e;
+        Sink S{};
+        S.flag = flag;
+        e = run_pass<kMark>(geo, f, method, bf16, S, st);
+        if (e != cudaSuccess) return e;
+    }
     if (ref_voxel >= 0 && ref_voxel < geo.grid.V) e = cudaMemsetAsync(flag + ref_voxel, 1, 1, st);
     return e;
 }

@@ -20,6 +20,8 @@ struct DirEntry {
     float ct, st, cp, sp;  // cos/sin of theta and phi
     float k1, k2, k3;      // the direction as read from the direction file
     int cas;               // which branch of cross2point (K:663-1113) applies: 1..7, 0 none
+    int orig;              // index of the direction in the caller's list
+    int pad_;
 };
 
 // Grid constants passed by value to every kernel.
@@ -125,8 +127,11 @@ struct Anchor {
     // same geometry allocates nothing
     size_t cap[20] = {};
 };
+// Builds the operator; returns cudaErrorNotSupported (nothing filled) when it would hold
+// more than max_nnz entries (max_nnz < 0: no limit).
 cudaError_t anchor_build(const Geometry &geo, const Field &f, int method, bool bf16,
-                         long long ref_voxel, Anchor *A, cudaStream_t st, std::string *err);
+                         long long ref_voxel, long long max_nnz, Anchor *A, cudaStream_t st,
+                         std::string *err);
 void anchor_free(Anchor *A);
 // Plain method: recompute only b (the field-dependent part) of an operator built by
 // anchor_build for the same geometry; rows, columns and c depend on the geometry alone.
@@ -144,10 +149,12 @@ cudaError_t anchor_step(const Anchor &A, const float *p_init, bool seed, int gau
 size_t change_scratch_doubles();
 cudaError_t change_sums(long long n, const float *pc, const float *pn, int gauge, long long ref,
                         double *scratch, double *out2, cudaStream_t st, const uint8_t *mask);
-// Flag the anchor voxels (line entries, or segment starts of the selected method, plus
-// ref_voxel when >= 0) into a V-byte array.
+// Flag the anchor voxels (line entries, or the segment starts of the selected method or a
+// small superset of them, plus ref_voxel when >= 0) into a V-byte array.  count1 is one
+// device word of scratch.
 cudaError_t anchor_mark(const Geometry &geo, const Field &f, int method, bool bf16,
-                        long long ref_voxel, uint8_t *flag, cudaStream_t st);
+                        long long ref_voxel, uint8_t *flag, unsigned long long *count1,
+                        cudaStream_t st);
 // Scatter anchor values into a volume.
 cudaError_t anchor_scatter(const Anchor &A, const float *pa, float *vol, cudaStream_t st);
 // Gather anchor values from a volume.

@@ -42,7 +42,7 @@ class Stats(C.Structure):
     _fields_ = [("iterations", _i), ("rel_change", _d), ("n_lines", _ll), ("n_units", _ll), ("walk_errors", _ll),
                 ("n_anchors", _ll), ("n_links", _ll), ("ms_geometry", _d), ("ms_setup", _d), ("ms_iterate", _d),
                 ("ms_final", _d), ("ms_total", _d), ("ms_sweep", _d),
-                ("kernel_launches", _ll)]
+                ("kernel_launches", _ll), ("solver_used", _i)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
