@@ -154,6 +154,61 @@ def cpu_reference_sample(args, f, dirs, n_sample_dirs=None):
     return units / dt, dt, units, kind, min(nthreads, nd), nd
 
 
+def sor_baseline(args, sizes=(16, 24, 32), n_big=None, budget_s=60.0):
+    """The reference's CPU Poisson solver (sor3D.cpp: weighted Jacobi, omega 0.8, one
+    thread) on the same workload family: iterations to reach 1e-3 relative L2 of its own
+    converged solution at small sizes (found by doubling), the fitted growth exponent, the
+    measured seconds per iteration at the full size, and the extrapolated time-to-solution
+    at the full size (labelled as extrapolated)."""
+    import oracle
+    from omni3d import synthetic
+
+    path = oracle.build_ref()
+    if path is None:
+        return {"unavailable": "reference sources are not staged on this machine"}
+    R = oracle.RefLib(path)
+    t_start = time.perf_counter()
+    pts = []
+    for n in sizes:
+        f = synthetic.blobs(n=n, count=8, sigma_range=(8.0 * n / 256, 24.0 * n / 256), noise=0.05, seed=0,
+                            spacing=1e-3 * 256 / n)
+        dims = f["dims"]
+        conv = R.sor(dims, f["spacing"], f["ax"], f["ay"], f["az"], 200 * n * n, 1e-14)
+        k, err = 8, 1.0
+        while True:
+            p = R.sor(dims, f["spacing"], f["ax"], f["ay"], f["az"], k, 0.0)
+            err = synthetic.relative_l2(p, conv, gauge="mean")
+            if err <= 1e-3 or k > 100 * n * n:
+                break
+            k *= 2
+        lo, hi = k // 2, k
+        while hi - lo > max(1, hi // 32):
+            mid = (lo + hi) // 2
+            p = R.sor(dims, f["spacing"], f["ax"], f["ay"], f["az"], mid, 0.0)
+            if synthetic.relative_l2(p, conv, gauge="mean") <= 1e-3:
+                hi = mid
+            else:
+                lo = mid
+        t0 = time.perf_counter()
+        R.sor(dims, f["spacing"], f["ax"], f["ay"], f["az"], hi, 0.0)
+        pts.append({"n": n, "iterations_to_1e-3": hi, "seconds": time.perf_counter() - t0})
+        if time.perf_counter() - t_start > budget_s:
+            break
+    ns = np.array([q["n"] for q in pts], float)
+    its = np.array([q["iterations_to_1e-3"] for q in pts], float)
+    expo = float(np.polyfit(np.log(ns), np.log(its), 1)[0]) if len(pts) > 1 else 2.0
+    nb = n_big or args.n
+    f = workload(args)
+    t0 = time.perf_counter()
+    R.sor(f["dims"], f["spacing"], f["ax"], f["ay"], f["az"], 2, 0.0)
+    s_per_it = (time.perf_counter() - t0) / 2
+    its_big = its[-1] * (nb / ns[-1]) ** expo
+    return {"kind": "reference", "cores": 1, "solver": "sor3D (weighted Jacobi, omega 0.8, double)",
+            "small_sizes": pts, "iteration_growth_exponent": expo, "seconds_per_iteration_full_size": s_per_it,
+            "iterations_to_1e-3_full_size_extrapolated": its_big,
+            "time_to_solution_s_extrapolated": its_big * s_per_it}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -210,11 +265,15 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="only the warm-up and timed solves (for ncu): no calibration, e2e, variants or CPU arm")
     ap.add_argument("--no-variants", action="store_true", help="skip timing the sweep-solver and BF16 forms")
+    ap.add_argument("--sor", action="store_true", help="only the reference CPU SOR baseline (JSON line)")
     args = ap.parse_args()
     if args.iters <= 0:
         args.iters = DEFAULT_ITERS.get((args.n, args.level), 12)
     if args.impl == "reference":
         return run_reference(args)
+    if args.sor:
+        print(json.dumps({"metric": METRIC, "cpu_sor_baseline": sor_baseline(args)}))
+        return 0
 
     import torch
 

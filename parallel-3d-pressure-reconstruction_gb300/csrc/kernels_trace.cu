@@ -18,22 +18,40 @@ constexpr int kScanBlock = 1024;
 constexpr int kScanItems = 4;  // items per thread
 constexpr long long kScanTile = (long long)kScanBlock * kScanItems;
 
-__device__ __forceinline__ bool trace_candidate(const Grid &g, const DirEntry *dirs, long long ng2,
+// Candidate order: (group of `gsize` neighbouring directions, block of 32 lattice points,
+// direction within the group, point within the block).  A warp then holds 32 adjacent
+// lines of one direction and a block of warps holds the same lattice patch of several
+// nearly parallel directions, which walk through the same voxels at the same time.
+struct CandOrder {
+    long long ng2;    // lattice points per direction
+    long long nblk;   // 32-point lattice blocks per direction
+    int gsize;        // directions per group
+    int nv;
+};
+
+__device__ __forceinline__ bool trace_candidate(const Grid &g, const DirEntry *dirs, const CandOrder &co,
                                                 long long c, int in[3], int out[3], float o[3],
                                                 int *dir)
 {
-    int d = (int)(c / ng2);
-    long long pt = c - (long long)d * ng2;
+    const long long per_block = (long long)co.gsize * 32;
+    const long long per_group = co.nblk * per_block;
+    long long grp = c / per_group;
+    long long r = c - grp * per_group;
+    long long blk = r / per_block;
+    r -= blk * per_block;
+    int d = (int)(grp * co.gsize + r / 32);
+    long long pt = blk * 32 + (r & 31);
+    *dir = d;
+    if (d >= co.nv || pt >= co.ng2) return false;
     DirEntry D = dirs[d];
     om_line_offset(pt, g.ng, g.ls, D, o[0], o[1], o[2]);
     om_cross2point(g, o[0], o[1], o[2], D.k1, D.k2, D.k3, D.cas, in, out);
-    *dir = d;
     return om_line_valid(g, in, out);
 }
 
 // Pass 1: number of valid lines per block of candidates.
 __global__ void __launch_bounds__(kTraceBlock) k_trace_count(Grid g, const DirEntry *dirs,
-                                                             long long ncand, long long ng2,
+                                                             long long ncand, CandOrder co,
                                                              uint32_t *blk_cnt)
 {
     __shared__ uint32_t warp_cnt[kTraceBlock / 32];
@@ -42,7 +60,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_count(Grid g, const DirEn
     if (c < ncand) {
         int in[3], out[3], d;
         float o[3];
-        valid = trace_candidate(g, dirs, ng2, c, in, out, o, &d);
+        valid = trace_candidate(g, dirs, co, c, in, out, o, &d);
     }
     unsigned b = __ballot_sync(0xffffffffu, valid);
     if ((threadIdx.x & 31) == 0) warp_cnt[threadIdx.x >> 5] = __popc(b);
@@ -56,7 +74,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_count(Grid g, const DirEn
 
 // Pass 2: write the valid lines of each block at its offset, in candidate order.
 __global__ void __launch_bounds__(kTraceBlock) k_trace_emit(Grid g, const DirEntry *dirs,
-                                                            long long ncand, long long ng2,
+                                                            long long ncand, CandOrder co,
                                                             const uint32_t *blk_off,
                                                             LineRec *lines, float4 *off)
 {
@@ -65,7 +83,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_emit(Grid g, const DirEnt
     bool valid = false;
     int in[3], out[3], d = 0;
     float o[3];
-    if (c < ncand) valid = trace_candidate(g, dirs, ng2, c, in, out, o, &d);
+    if (c < ncand) valid = trace_candidate(g, dirs, co, c, in, out, o, &d);
     unsigned b = __ballot_sync(0xffffffffu, valid);
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) warp_cnt[warp] = __popc(b);
@@ -268,8 +286,13 @@ void free_geometry(Geometry *g)
 cudaError_t build_geometry(Geometry *g, cudaStream_t st, std::string *err)
 {
     const Grid &G = g->grid;
-    long long ng2 = (long long)G.ng * G.ng;
-    long long ncand = ng2 * g->nv;
+    CandOrder co;
+    co.ng2 = (long long)G.ng * G.ng;
+    co.nblk = (co.ng2 + 31) / 32;
+    co.gsize = std::max(1, std::min(g->dir_group, g->nv));
+    co.nv = g->nv;
+    long long ngroups = (g->nv + co.gsize - 1) / co.gsize;
+    long long ncand = ngroups * co.nblk * co.gsize * 32;
     long long nblk = (ncand + kTraceBlock - 1) / kTraceBlock;
     if (nblk > 0x7fffffffLL) {
         if (err) *err = "too many lattice candidates";
@@ -279,7 +302,7 @@ cudaError_t build_geometry(Geometry *g, cudaStream_t st, std::string *err)
     OM_TRY(cudaMalloc(&blk, sizeof(uint32_t) * (size_t)(2 * nblk + 1)));
     OM_TRY(cudaMalloc(&tmp, sizeof(uint32_t) * scan_tmp_elems(nblk)));
     uint32_t *blk_off = blk + nblk;
-    k_trace_count<<<(unsigned)nblk, kTraceBlock, 0, st>>>(G, g->d_dirs, ncand, ng2, blk);
+    k_trace_count<<<(unsigned)nblk, kTraceBlock, 0, st>>>(G, g->d_dirs, ncand, co, blk);
     OM_COUNT_LAUNCH();
     OM_TRY(cudaGetLastError());
     OM_TRY(exclusive_scan_u32(blk, blk_off, nblk, tmp, st));
@@ -297,7 +320,7 @@ cudaError_t build_geometry(Geometry *g, cudaStream_t st, std::string *err)
     }
     OM_TRY(cudaMalloc(&g->d_lines, sizeof(LineRec) * (size_t)total));
     OM_TRY(cudaMalloc(&g->d_off, sizeof(float4) * (size_t)total));
-    k_trace_emit<<<(unsigned)nblk, kTraceBlock, 0, st>>>(G, g->d_dirs, ncand, ng2, blk_off, g->d_lines,
+    k_trace_emit<<<(unsigned)nblk, kTraceBlock, 0, st>>>(G, g->d_dirs, ncand, co, blk_off, g->d_lines,
                                                          g->d_off);
     OM_COUNT_LAUNCH();
     OM_TRY(cudaGetLastError());
