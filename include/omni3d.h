@@ -158,6 +158,24 @@ int omni3d_line_table(omni3d_ctx *ctx, int32_t *rows, long long n_max);
 /* Copy the staircase of line `line` (one axis code 0/1/2 per step) to host memory. */
 int omni3d_line_steps(omni3d_ctx *ctx, long long line, int8_t *axes, int cap);
 
+/* ---------------------------------------------------------------- batches of snapshots */
+
+/* A batch solves several snapshots, each with its own context (grid sizes may differ), in
+ * one CUDA-graph launch: every member's solve runs on its own stream, forked from and
+ * joined to the batch stream, captured once and relaunched while the buffers stay the same.
+ * This replaces the reference's sequential per-file loop (K:8701-8963).  Members need the
+ * plain method, the anchor solver and tol = 0 (a fixed iteration count); the first
+ * omni3d_batch_solve prepares each member with one regular solve. */
+typedef struct omni3d_batch omni3d_batch;
+int omni3d_batch_create(omni3d_ctx *const *ctxs, int n, omni3d_batch **out);
+int omni3d_batch_destroy(omni3d_batch *batch);
+const char *omni3d_batch_last_error(const omni3d_batch *batch);
+/* Per-member arrays of n pointers; p_init and count_out (and their entries) may be NULL.
+ * stats (optional) aggregates the members; ms_total is the device time of the graph. */
+int omni3d_batch_solve(omni3d_batch *batch, const float *const *ax, const float *const *ay,
+                       const float *const *az, const float *const *p_init, float *const *p_out,
+                       float *const *count_out, int device_ptrs, omni3d_stats *stats);
+
 /* ---------------------------------------------------------------- host-side helpers */
 
 /* Direction set of an icosahedron subdivided `level` times (level 2: 42, 3: 162, 4: 642,

@@ -656,3 +656,129 @@ int orc_num_threads(void)
     return 1;
 #endif
 }
+
+/* ------------------------------------------------------------------------------------ */
+/* FP64 adjoint of the plain iteration                                                    */
+/* ------------------------------------------------------------------------------------ */
+
+/* Visit every valid line of the plain method (same geometry as the sweep): the callback
+ * receives the line's voxels v_0 (entry) .. v_n and the per-step axis and trapezoid
+ * coefficient h_t = -rho * sign * dl / 2. */
+typedef void (*orc_line_fn)(void *ud, const long *vox, const signed char *ax, const double *h, int n);
+
+static void for_each_line(const orc_problem *P, orc_line_fn fn, void *ud)
+{
+    int ng = orc_nogrid(P->X, P->Y, P->Z, P->ls, P->geom_cpu_twin);
+    long cap = max_path(P->X, P->Y, P->Z);
+    signed char *ax = (signed char *)malloc((size_t)cap);
+    long *vox = (long *)malloc(sizeof(long) * (size_t)(cap + 1));
+    double *h = (double *)malloc(sizeof(double) * (size_t)cap);
+    const long stride[3] = {1, P->X, P->X * P->Y};
+    const float dl[3] = {P->dx, P->dy, P->dz};
+    for (int d = 0; d < P->nv; d++) {
+        float c[4];
+        orc_dir_coeffs(P->k1[d], P->k2[d], P->k3[d], P->geom_cpu_twin, c);
+        for (int pt = 0; pt < ng * ng; pt++) {
+            float xyz[3];
+            int in[3], out[3], sg[3];
+            orc_line_offset(pt, ng, P->ls, c, xyz);
+            orc_cross2point(P->X, P->Y, P->Z, xyz[0], xyz[1], xyz[2], P->k1[d], P->k2[d], P->k3[d], in, out);
+            if (!orc_line_valid(P->X, P->Y, P->Z, in, out)) continue;
+            int n = orc_walk(P->X, P->Y, P->Z, in, out, xyz[0], xyz[1], xyz[2], P->k1[d], P->k2[d], P->k3[d], ax,
+                             (int)cap);
+            if (n < 0) n = -n - 1;
+            axis_signs(in, out, sg);
+            vox[0] = in[0] + in[1] * P->X + in[2] * P->X * P->Y;
+            for (int s = 0; s < n; s++) {
+                int a = ax[s];
+                vox[s + 1] = vox[s] + sg[a] * stride[a];
+                h[s] = -(double)P->rho * (double)sg[a] * (double)dl[a] * 0.5;
+            }
+            fn(ud, vox, ax, h, n);
+        }
+    }
+    free(ax);
+    free(vox);
+    free(h);
+}
+
+typedef struct {
+    const double *mu;   /* per voxel */
+    double *lam;        /* per voxel: gathered to line entries */
+    double *cnt;
+    double *ga[3];
+} adj_ud;
+
+static void cb_count(void *ud, const long *vox, const signed char *ax, const double *h, int n)
+{
+    adj_ud *U = (adj_ud *)ud;
+    (void)ax; (void)h;
+    for (int s = 0; s <= n; s++) U->cnt[vox[s]] += 1.0;
+}
+
+static void cb_gather(void *ud, const long *vox, const signed char *ax, const double *h, int n)
+{
+    adj_ud *U = (adj_ud *)ud;
+    (void)ax; (void)h;
+    double t = 0.0;
+    for (int s = 0; s <= n; s++) t += U->mu[vox[s]];
+    U->lam[vox[0]] += t;
+}
+
+static void cb_grad(void *ud, const long *vox, const signed char *ax, const double *h, int n)
+{
+    adj_ud *U = (adj_ud *)ud;
+    double R = 0.0;
+    for (int s = 1; s <= n; s++) R += U->mu[vox[s]];
+    for (int t = 1; t <= n; t++) {
+        int a = ax[t - 1];
+        U->ga[a][vox[t]] += h[t - 1] * R;
+        U->ga[a][vox[t - 1]] += h[t - 1] * R;
+        R -= U->mu[vox[t]];
+    }
+}
+
+/* Gradient of <g, p_K> with respect to (au, av, aw) for the plain iteration of orc_solve
+ * (p = pn = p_init, niter x {sweep, divide where count > 0}), in FP64: the transpose of
+ * p_k(v) = (sum over lines through v of p_{k-1}(entry) + I(v)) / c(v), kept p where c = 0.
+ * The seeding of the first sweep with p_init does not depend on the gradient field. */
+void orc_adjoint_f64(const orc_problem *P, int niter, const double *g, double *gau, double *gav, double *gaw)
+{
+    long V = P->X * P->Y * P->Z;
+    double *cnt = (double *)calloc((size_t)V, sizeof(double));
+    double *lam = (double *)malloc(sizeof(double) * (size_t)V);
+    double *nxt = (double *)malloc(sizeof(double) * (size_t)V);
+    double *mu = (double *)malloc(sizeof(double) * (size_t)V);
+    double *macc = (double *)calloc((size_t)V, sizeof(double));
+    adj_ud U;
+    memset(&U, 0, sizeof(U));
+    U.cnt = cnt;
+    for_each_line(P, cb_count, &U);
+    memcpy(lam, g, sizeof(double) * (size_t)V);
+    for (int k = niter; k >= 1; k--) {
+        for (long v = 0; v < V; v++) {
+            mu[v] = cnt[v] > 0 ? lam[v] / cnt[v] : 0.0;
+            macc[v] += mu[v];
+            nxt[v] = cnt[v] > 0 ? 0.0 : lam[v];
+        }
+        if (k > 1) {
+            U.mu = mu;
+            U.lam = nxt;
+            for_each_line(P, cb_gather, &U);
+            memcpy(lam, nxt, sizeof(double) * (size_t)V);
+        }
+    }
+    memset(gau, 0, sizeof(double) * (size_t)V);
+    memset(gav, 0, sizeof(double) * (size_t)V);
+    memset(gaw, 0, sizeof(double) * (size_t)V);
+    U.mu = macc;
+    U.ga[0] = gau;
+    U.ga[1] = gav;
+    U.ga[2] = gaw;
+    for_each_line(P, cb_grad, &U);
+    free(cnt);
+    free(lam);
+    free(nxt);
+    free(mu);
+    free(macc);
+}

@@ -107,6 +107,7 @@ class Oracle:
             fn.argtypes = [C.POINTER(OrcProblem), _fp, _fp, _fp, _fp, _fp, _i, ptr, ptr, _i]
             fn = getattr(L, "orc_divide_" + s)
             fn.argtypes = [_l, ptr, ptr, ptr, _i]
+        L.orc_adjoint_f64.argtypes = [C.POINTER(OrcProblem), _i, _dp, _dp, _dp, _dp]
         L.orc_calindex.argtypes = [_l, _l, _l, _lp]
         L.orc_curl.argtypes = [_l, _l, _l, _f, _f, _f, _fp, _fp, _fp, _fp, _fp]
         L.orc_num_threads.restype = _i
@@ -199,6 +200,15 @@ class Oracle:
         if err:
             raise RuntimeError("oracle: %d lines hit the wrong-point branch" % err)
         return pn, cnt
+
+    def adjoint(self, dims, spacing, k, niter, g, *, rho=1.0, ls=1.0):
+        """FP64 gradient of <g, p_niter> with respect to (au, av, aw), plain method."""
+        P, keep = self._problem(dims, spacing, rho, ls, 0.0, k, 0, False)
+        V = dims[0] * dims[1] * dims[2]
+        g = np.ascontiguousarray(np.asarray(g, np.float64).reshape(-1))
+        out = [np.zeros(V, np.float64) for _ in range(3)]
+        self.lib.orc_adjoint_f64(C.byref(P), int(niter), _ptr(g, C.c_double), *[_ptr(o, C.c_double) for o in out])
+        return out
 
     def calindex(self, dims) -> np.ndarray:
         X, Y, Z = dims

@@ -229,7 +229,78 @@ int prepare_field(omni3d_ctx *ctx, const float *ax, const float *ay, const float
     return OMNI3D_OK;
 }
 
+// True when ctx can run the fully asynchronous solve: plain method, anchor solver with its
+// operator already built for this geometry, a fixed iteration count, buffers allocated.
+bool prepared_for_graph(const omni3d_ctx *ctx)
+{
+    const omni3d_params &P = ctx->prm;
+    return P.method == OMNI3D_METHOD_PLAIN && P.solver == OMNI3D_SOLVER_ANCHOR && P.tol == 0.0 && ctx->anc_cached &&
+           ctx->f32.p && ctx->in_pinit.p && ctx->pncnt.p && ctx->pout.p && ctx->cnt.p && ctx->pvol_a.p &&
+           ctx->scratch.p && (P.grad_storage != OMNI3D_GRAD_BF16 || ctx->b16.p);
+}
+
+// The solve of omni3d_solve for a prepared context, issued on `st` with no host
+// synchronisation and no allocation, so that it can be captured into a CUDA graph.
+// Inputs are device pointers; p_init may be null (zero).
+cudaError_t enqueue_prepared(omni3d_ctx *ctx, const float *dax, const float *day, const float *daz,
+                             const float *dpinit, float *p_out, float *count_out, cudaStream_t st)
+{
+    const omni3d_params &P = ctx->prm;
+    const Grid &g = ctx->geo.grid;
+    const long long V = g.V;
+    const bool bf16 = P.grad_storage == OMNI3D_GRAD_BF16;
+    const long long ref = (long long)P.ref_i + (long long)P.ref_j * g.X + (long long)P.ref_k * g.XY;
+    Field F;
+    F.f32 = ctx->f32.as<float4>();
+    F.bf16 = bf16 ? ctx->b16.as<uint2>() : nullptr;
+    cudaError_t e = pack_field(g, dax, day, daz, nullptr, &F, bf16, st);
+    if (e != cudaSuccess) return e;
+    if (!dpinit) {
+        if ((e = cudaMemsetAsync(ctx->in_pinit.p, 0, sizeof(float) * (size_t)V, st)) != cudaSuccess) return e;
+        dpinit = ctx->in_pinit.as<float>();
+    }
+    Anchor &A = ctx->anc;
+    if ((e = anchor_refresh_rhs(ctx->geo, F, bf16, &A, st)) != cudaSuccess) return e;
+    if ((e = anchor_gather(A, dpinit, A.pa, st)) != cudaSuccess) return e;
+    const int K = P.max_iter;
+    const bool seed = P.seed_first_iteration != 0;
+    float *pc = A.pa, *pn = A.pb;
+    for (int it = 1; it <= K - 1; it++) {
+        if ((e = anchor_step(A, dpinit, seed && it == 1, P.gauge, -1, pc, pn, nullptr, st)) != cudaSuccess) return e;
+        std::swap(pc, pn);
+    }
+    float2 *acc = ctx->pncnt.as<float2>();
+    float *vol = ctx->pvol_a.as<float>(), *dout = ctx->pout.as<float>(), *dcnt = ctx->cnt.as<float>();
+    if (K == 0) {
+        if ((e = cudaMemcpyAsync(dout, dpinit, sizeof(float) * (size_t)V, cudaMemcpyDeviceToDevice, st))) return e;
+        if ((e = cudaMemsetAsync(dcnt, 0, sizeof(float) * (size_t)V, st))) return e;
+    } else {
+        if ((e = cudaMemcpyAsync(vol, dpinit, sizeof(float) * (size_t)V, cudaMemcpyDeviceToDevice, st))) return e;
+        if ((e = anchor_scatter(A, pc, vol, st))) return e;
+        if ((e = init_accum(V, dpinit, seed && K == 1, acc, st))) return e;
+        if ((e = sweep_full(ctx->geo, F, P.method, bf16, vol, acc, st))) return e;
+        if ((e = normalize(V, acc, dpinit, dout, dcnt, st))) return e;
+    }
+    if ((e = apply_gauge(V, P.gauge, ref, dcnt, dout, ctx->scratch.as<double>() + 4, st))) return e;
+    if (p_out && (e = cudaMemcpyAsync(p_out, dout, sizeof(float) * (size_t)V, cudaMemcpyDeviceToDevice, st))) return e;
+    if (count_out && (e = cudaMemcpyAsync(count_out, dcnt, sizeof(float) * (size_t)V, cudaMemcpyDeviceToDevice, st)))
+        return e;
+    return cudaSuccess;
+}
+
 }  // namespace
+
+struct omni3d_batch {
+    std::vector<omni3d_ctx *> ctx;
+    int device = 0;
+    cudaStream_t st = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<const void *> key;  // pointers the captured graph reads and writes
+    cudaEvent_t fork = nullptr, t0 = nullptr, t1 = nullptr;
+    std::vector<cudaEvent_t> join;
+    long long launches_per_graph = 0;
+    std::string err;
+};
 
 extern "C" {
 
@@ -664,6 +735,184 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
         stats->solver_used = solver;
     }
     if (ctx->geo.walk_errors) return fail(ctx, OMNI3D_ERR_NUMERIC, "line walk hit the wrong-point branch");
+    return OMNI3D_OK;
+}
+
+// ------------------------------------------------------------------------- batches
+
+int omni3d_batch_create(omni3d_ctx *const *ctxs, int n, omni3d_batch **out)
+{
+    if (!ctxs || n <= 0 || !out) return fail(nullptr, OMNI3D_ERR_ARG, "bad arguments");
+    *out = nullptr;
+    int dev = ctxs[0] ? ctxs[0]->prm.device : 0;
+    for (int i = 0; i < n; i++) {
+        if (!ctxs[i]) return fail(nullptr, OMNI3D_ERR_ARG, "NULL context in the batch");
+        if (ctxs[i]->prm.device != dev) return fail(nullptr, OMNI3D_ERR_ARG, "contexts on different devices");
+        for (int j = 0; j < i; j++)
+            if (ctxs[j] == ctxs[i]) return fail(nullptr, OMNI3D_ERR_ARG, "a context appears twice in the batch");
+    }
+    cudaSetDevice(dev);
+    omni3d_batch *b = new omni3d_batch();
+    b->ctx.assign(ctxs, ctxs + n);
+    b->device = dev;
+    cudaError_t e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->t0);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->t1);
+    b->join.assign((size_t)n, nullptr);
+    for (int i = 0; i < n && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&b->join[i], cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        omni3d_batch_destroy(b);
+        return fail(nullptr, OMNI3D_ERR_CUDA, std::string("batch setup: ") + cudaGetErrorString(e));
+    }
+    *out = b;
+    return OMNI3D_OK;
+}
+
+int omni3d_batch_destroy(omni3d_batch *b)
+{
+    if (!b) return OMNI3D_OK;
+    cudaSetDevice(b->device);
+    if (b->st) cudaStreamSynchronize(b->st);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    for (cudaEvent_t ev : b->join)
+        if (ev) cudaEventDestroy(ev);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->t0) cudaEventDestroy(b->t0);
+    if (b->t1) cudaEventDestroy(b->t1);
+    if (b->st) cudaStreamDestroy(b->st);
+    delete b;
+    return OMNI3D_OK;
+}
+
+const char *omni3d_batch_last_error(const omni3d_batch *b) { return b ? b->err.c_str() : g_error.c_str(); }
+
+int omni3d_batch_solve(omni3d_batch *b, const float *const *ax, const float *const *ay, const float *const *az,
+                       const float *const *p_init, float *const *p_out, float *const *count_out, int device_ptrs,
+                       omni3d_stats *stats)
+{
+    auto bfail = [&](int code, const std::string &m) {
+        if (b) b->err = m;
+        g_error = m;
+        return code;
+    };
+    if (!b || !ax || !ay || !az || !p_out) return bfail(OMNI3D_ERR_ARG, "NULL argument");
+    cudaSetDevice(b->device);
+    const int n = (int)b->ctx.size();
+    const bool dev = device_ptrs != 0;
+    // device-side inputs and outputs of every member
+    std::vector<const float *> dax(n), day(n), daz(n), dp0(n);
+    std::vector<float *> dout(n), dcnt(n);
+    for (int i = 0; i < n; i++) {
+        omni3d_ctx *c = b->ctx[i];
+        if (!ax[i] || !ay[i] || !az[i] || !p_out[i]) return bfail(OMNI3D_ERR_ARG, "NULL member argument");
+        // first use: a regular solve builds the context's cached operator and buffers
+        if (!prepared_for_graph(c)) {
+            if (c->prm.method != OMNI3D_METHOD_PLAIN || c->prm.solver != OMNI3D_SOLVER_ANCHOR || c->prm.tol != 0.0)
+                return bfail(OMNI3D_ERR_STATE, "batch members need the plain method, the anchor solver and tol = 0");
+            int rc = omni3d_solve(c, ax[i], ay[i], az[i], nullptr, nullptr, p_init ? p_init[i] : nullptr, p_out[i],
+                                  count_out ? count_out[i] : nullptr, device_ptrs, nullptr);
+            if (rc) return bfail(rc, std::string("preparing batch member: ") + c->err);
+            if (!prepared_for_graph(c)) return bfail(OMNI3D_ERR_STATE, "batch member could not be prepared");
+        }
+        const long long V = c->geo.grid.V;
+        if (dev) {
+            dax[i] = ax[i]; day[i] = ay[i]; daz[i] = az[i];
+            dp0[i] = p_init ? p_init[i] : nullptr;
+            dout[i] = p_out[i];
+            dcnt[i] = count_out ? count_out[i] : nullptr;
+        } else {
+            // host buffers: copied outside the graph into the member's staging buffers
+            const float *src[4] = {ax[i], ay[i], az[i], p_init ? p_init[i] : nullptr};
+            DeviceBuf *stg[4] = {&c->in_ax, &c->in_ay, &c->in_az, &c->in_aux};
+            const float *dst[4] = {nullptr, nullptr, nullptr, nullptr};
+            for (int q = 0; q < 4; q++) {
+                if (!src[q]) continue;
+                if (stg[q]->ensure(sizeof(float) * (size_t)V) != cudaSuccess) return bfail(OMNI3D_ERR_NOMEM, "staging");
+                dst[q] = stg[q]->as<float>();
+            }
+            dax[i] = dst[0]; day[i] = dst[1]; daz[i] = dst[2]; dp0[i] = dst[3];
+            dout[i] = nullptr;  // results stay in the member's own output buffers
+            dcnt[i] = nullptr;
+        }
+    }
+    std::vector<const void *> key;
+    for (int i = 0; i < n; i++) {
+        key.insert(key.end(), {dax[i], day[i], daz[i], dp0[i], dout[i], dcnt[i]});
+    }
+    cudaError_t e;
+    if (!dev) {
+        for (int i = 0; i < n; i++) {
+            omni3d_ctx *c = b->ctx[i];
+            const size_t bytes = sizeof(float) * (size_t)c->geo.grid.V;
+            const float *src[4] = {ax[i], ay[i], az[i], p_init ? p_init[i] : nullptr};
+            const float *dst[4] = {dax[i], day[i], daz[i], dp0[i]};
+            for (int q = 0; q < 4; q++)
+                if (src[q] && (e = cudaMemcpyAsync((void *)dst[q], src[q], bytes, cudaMemcpyHostToDevice, b->st)))
+                    return bfail(OMNI3D_ERR_CUDA, cudaGetErrorString(e));
+        }
+    }
+    if (!b->exec || key != b->key) {
+        if (b->exec) {
+            cudaGraphExecDestroy(b->exec);
+            b->exec = nullptr;
+        }
+        // capture: fork every member onto its own stream, join back
+        unsigned long long l0 = __atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED);
+        if ((e = cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal)))
+            return bfail(OMNI3D_ERR_CUDA, std::string("begin capture: ") + cudaGetErrorString(e));
+        cudaError_t ce = cudaEventRecord(b->fork, b->st);
+        for (int i = 0; i < n && ce == cudaSuccess; i++) {
+            omni3d_ctx *c = b->ctx[i];
+            ce = cudaStreamWaitEvent(c->st, b->fork, 0);
+            if (ce == cudaSuccess) ce = enqueue_prepared(c, dax[i], day[i], daz[i], dp0[i], dout[i], dcnt[i], c->st);
+            if (ce == cudaSuccess) ce = cudaEventRecord(b->join[i], c->st);
+            if (ce == cudaSuccess) ce = cudaStreamWaitEvent(b->st, b->join[i], 0);
+        }
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamEndCapture(b->st, &graph);
+        if (ce != cudaSuccess || e != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            cudaGetLastError();
+            return bfail(OMNI3D_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(ce != cudaSuccess ? ce : e));
+        }
+        e = cudaGraphInstantiate(&b->exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e) return bfail(OMNI3D_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(e));
+        b->launches_per_graph = (long long)(__atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED) - l0);
+        b->key = key;
+    }
+    cudaEventRecord(b->t0, b->st);
+    if ((e = cudaGraphLaunch(b->exec, b->st))) return bfail(OMNI3D_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
+    cudaEventRecord(b->t1, b->st);
+    if (!dev) {
+        for (int i = 0; i < n; i++) {
+            omni3d_ctx *c = b->ctx[i];
+            const size_t bytes = sizeof(float) * (size_t)c->geo.grid.V;
+            if ((e = cudaMemcpyAsync(p_out[i], c->pout.p, bytes, cudaMemcpyDeviceToHost, b->st)))
+                return bfail(OMNI3D_ERR_CUDA, cudaGetErrorString(e));
+            if (count_out && count_out[i] &&
+                (e = cudaMemcpyAsync(count_out[i], c->cnt.p, bytes, cudaMemcpyDeviceToHost, b->st)))
+                return bfail(OMNI3D_ERR_CUDA, cudaGetErrorString(e));
+        }
+    }
+    if ((e = cudaStreamSynchronize(b->st))) return bfail(OMNI3D_ERR_CUDA, cudaGetErrorString(e));
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, b->t0, b->t1);
+        stats->ms_total = ms;
+        stats->kernel_launches = b->launches_per_graph;
+        stats->solver_used = OMNI3D_SOLVER_ANCHOR;
+        for (omni3d_ctx *c : b->ctx) {
+            stats->n_lines += c->geo.n_lines;
+            stats->n_units += c->geo.n_units;
+            stats->walk_errors += c->geo.walk_errors;
+            stats->n_anchors += c->anc.n;
+            stats->n_links += c->anc.nnz;
+            stats->iterations = c->prm.max_iter;
+        }
+    }
     return OMNI3D_OK;
 }
 

@@ -55,13 +55,12 @@ __device__ __forceinline__ bool is_anchor(const uint32_t *bits, long long v)
     return (__ldg(bits + (v >> 5)) >> (v & 31)) & 1u;
 }
 
-enum Pass { kMark = 0, kCount = 1, kFill = 2, kRhs = 3 };
+enum Pass { kMark = 0, kFill = 2, kRhs = 3 };
 
 struct Sink {
     const uint32_t *bits;
     const int32_t *id;
     uint8_t *flag;
-    uint32_t *rowcnt;
     const unsigned long long *rowptr;
     uint32_t *cursor;
     uint32_t *col;
@@ -82,15 +81,11 @@ __device__ __forceinline__ void emit(const Sink &S, long long v, long long start
         atomicAdd(S.b + row, I);
         return;
     }
-    if (PASS == kCount) {
-        atomicAdd(S.rowcnt + row, 1u);
-    } else {
-        unsigned long long slot = S.rowptr[row] + atomicAdd(S.cursor + row, 1u);
-        S.col[slot] = (uint32_t)__ldg(S.id + start);
-        S.w[slot] = wt;
-        atomicAdd(S.b + row, wt * I);
-        atomicAdd(S.c + row, wt);
-    }
+    unsigned long long slot = S.rowptr[row] + atomicAdd(S.cursor + row, 1u);
+    S.col[slot] = (uint32_t)__ldg(S.id + start);
+    S.w[slot] = wt;
+    atomicAdd(S.b + row, wt * I);
+    atomicAdd(S.c + row, wt);
 }
 
 struct Walk {
@@ -121,7 +116,7 @@ struct Walk {
 
 // Plain method: anchors are the entries; every voxel of a line takes (p[entry] + I, 1).
 template <int PASS, bool BF16>
-__global__ void __launch_bounds__(256) k_anchor_plain(Grid g, const LineRec *__restrict__ lines,
+__global__ void __launch_bounds__(256, 6) k_anchor_plain(Grid g, const LineRec *__restrict__ lines,
                                                       const uint32_t *__restrict__ gbase,
                                                       const uint32_t *__restrict__ desc, long long n_lines,
                                                       const float4 *__restrict__ f32,
@@ -161,7 +156,7 @@ __global__ void __launch_bounds__(256) k_anchor_plain(Grid g, const LineRec *__r
 // Selected method: the state machine of k_sweep_select (K:2280-2537); anchors are the
 // segment starts.
 template <int PASS, bool BF16>
-__global__ void __launch_bounds__(256) k_anchor_select(Grid g, const LineRec *__restrict__ lines,
+__global__ void __launch_bounds__(256, 6) k_anchor_select(Grid g, const LineRec *__restrict__ lines,
                                                        const uint32_t *__restrict__ gbase,
                                                        const uint32_t *__restrict__ desc, long long n_lines,
                                                        const float4 *__restrict__ f32,
@@ -206,9 +201,9 @@ __global__ void __launch_bounds__(256) k_anchor_select(Grid g, const LineRec *__
                 if (!paused && good) {
                     if (PASS == kFill)
                         kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
-                    csum += __fdiv_rn(cn, 10000.0f);
+                    csum += cn * 1.0e-4f;  // the weights as in k_sweep_select
                     nseg += 1.0f;
-                    emit<PASS>(S, L.v, start, __fdiv_rn(1.0f, csum) * nseg, I);
+                    emit<PASS>(S, L.v, start, __frcp_rn(csum) * nseg, I);
                 }
                 bool enter_bad = (a == 0) ? ((!paused && cn >= thr) || cn == 0.0f) : (!paused && cn >= thr);
                 if (enter_bad) paused = true;
@@ -277,6 +272,13 @@ __global__ void k_assign_ids(long long V, const uint8_t *flag, const uint32_t *p
     }
 }
 
+__global__ void k_row_capacity(long long n, const uint32_t *vox, const uint32_t *lines_through,
+                               unsigned long long *out)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = lines_through[vox[i]];
+}
+
 __global__ void k_u32_to_u64(long long n, const uint32_t *in, unsigned long long *out)
 {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
@@ -285,6 +287,7 @@ __global__ void k_u32_to_u64(long long n, const uint32_t *in, unsigned long long
 
 // One anchor iteration, a warp per row.
 __global__ void __launch_bounds__(256) k_anchor_spmv(long long n, const unsigned long long *__restrict__ rowptr,
+                                                     const uint32_t *__restrict__ rowlen,
                                                      const uint32_t *__restrict__ col, const float *__restrict__ w,
                                                      const float *__restrict__ b, const float *__restrict__ c,
                                                      const uint32_t *__restrict__ vox, const float *__restrict__ p_init,
@@ -293,7 +296,7 @@ __global__ void __launch_bounds__(256) k_anchor_spmv(long long n, const unsigned
     long long row = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     if (row >= n) return;  // whole warps
-    unsigned long long j0 = rowptr[row], j1 = rowptr[row + 1];
+    unsigned long long j0 = rowptr[row], j1 = j0 + rowlen[row];
     float s = 0.0f;
     for (unsigned long long j = j0 + lane; j < j1; j += 32) s += __ldg(w + j) * __ldg(pc + __ldg(col + j));
     for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
@@ -307,6 +310,7 @@ __global__ void __launch_bounds__(256) k_anchor_spmv(long long n, const unsigned
 
 // Plain method: every weight is 1, so a row is a plain sum of gathered anchor values.
 __global__ void __launch_bounds__(256) k_anchor_spmv_unit(long long n, const unsigned long long *__restrict__ rowptr,
+                                                          const uint32_t *__restrict__ rowlen,
                                                           const uint32_t *__restrict__ col, const float *__restrict__ b,
                                                           const float *__restrict__ c, const uint32_t *__restrict__ vox,
                                                           const float *__restrict__ p_init, int seed,
@@ -315,7 +319,7 @@ __global__ void __launch_bounds__(256) k_anchor_spmv_unit(long long n, const uns
     long long row = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     if (row >= n) return;  // whole warps
-    unsigned long long j0 = rowptr[row], j1 = rowptr[row + 1];
+    unsigned long long j0 = rowptr[row], j1 = j0 + rowlen[row];
     float s = 0.0f;
     for (unsigned long long j = j0 + lane; j < j1; j += 32) s += __ldg(pc + __ldg(col + j));
     for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
@@ -473,11 +477,11 @@ void anchor_free(Anchor *A)
 {
     cudaFree(A->flag); cudaFree(A->bits); cudaFree(A->id); cudaFree(A->vox); cudaFree(A->rowptr);
     cudaFree(A->col); cudaFree(A->w); cudaFree(A->b); cudaFree(A->c); cudaFree(A->pa); cudaFree(A->pb);
-    cudaFree(A->red); cudaFree(A->u); cudaFree(A->pos); cudaFree(A->tmp); cudaFree(A->cnt64); cudaFree(A->tmp64);
+    cudaFree(A->red); cudaFree(A->rowlen); cudaFree(A->u); cudaFree(A->pos); cudaFree(A->tmp); cudaFree(A->cnt64); cudaFree(A->tmp64);
     *A = Anchor();
 }
 
-cudaError_t anchor_build(const Geometry &geo, const Field &f, int method, bool bf16, long long ref_voxel,
+cudaError_t anchor_build(Geometry &geo, const Field &f, int method, bool bf16, long long ref_voxel,
                          long long max_nnz, Anchor *A, cudaStream_t st, std::string *err)
 {
     const long long V = geo.grid.V;
@@ -524,17 +528,13 @@ cudaError_t anchor_build(const Geometry &geo, const Field &f, int method, bool b
     OM_COUNT_LAUNCH();
     AN_TRY(cudaGetLastError());
 
-    // rows
-    uint32_t *rowcnt = A->u;  // reuse: n <= V
-    AN_TRY(cudaMemsetAsync(rowcnt, 0, sizeof(uint32_t) * (size_t)std::max<long long>(n, 1), st));
-    S.bits = A->bits;
-    S.id = A->id;
-    S.rowcnt = rowcnt;
-    AN_TRY(run_pass<kCount>(geo, f, method, bf16, S, st));
+    // rows: a voxel receives at most one contribution per line through it, so the
+    // geometry-only line counts size the rows and no counting pass is needed
+    AN_TRY(ensure_lines_through(&geo, st));
     AN_TRY(grow(A->cnt64, cap[8], sizeof(unsigned long long) * (size_t)n));
     AN_TRY(grow(A->tmp64, cap[9], sizeof(unsigned long long) * scan_tmp_elems(n)));
     AN_TRY(grow(A->rowptr, cap[10], sizeof(unsigned long long) * (size_t)(n + 1)));
-    k_u32_to_u64<<<grid_for(n), 256, 0, st>>>(n, rowcnt, A->cnt64);
+    k_row_capacity<<<grid_for(n), 256, 0, st>>>(n, A->vox, geo.d_lines_through, A->cnt64);
     OM_COUNT_LAUNCH();
     AN_TRY(cudaGetLastError());
     AN_TRY(exclusive_scan_u64(A->cnt64, A->rowptr, n, A->tmp64, st));
@@ -553,7 +553,8 @@ cudaError_t anchor_build(const Geometry &geo, const Field &f, int method, bool b
     AN_TRY(grow(A->c, cap[14], sizeof(float) * (size_t)n));
     AN_TRY(grow(A->pa, cap[15], sizeof(float) * (size_t)n));
     AN_TRY(grow(A->pb, cap[16], sizeof(float) * (size_t)n));
-    uint32_t *cursor = rowcnt;
+    AN_TRY(grow(A->rowlen, cap[17], sizeof(uint32_t) * (size_t)n));
+    uint32_t *cursor = A->rowlen;
     AN_TRY(cudaMemsetAsync(cursor, 0, sizeof(uint32_t) * (size_t)std::max<long long>(n, 1), st));
     AN_TRY(cudaMemsetAsync(A->b, 0, sizeof(float) * (size_t)std::max<long long>(n, 1), st));
     AN_TRY(cudaMemsetAsync(A->c, 0, sizeof(float) * (size_t)std::max<long long>(n, 1), st));
@@ -622,10 +623,10 @@ cudaError_t anchor_step(const Anchor &A, const float *p_init, bool seed, int gau
     if (A.n == 0) return cudaSuccess;
     long long threads = A.n * 32;
     if (A.unit_weights)
-        k_anchor_spmv_unit<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(A.n, A.rowptr, A.col, A.b, A.c, A.vox,
+        k_anchor_spmv_unit<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(A.n, A.rowptr, A.rowlen, A.col, A.b, A.c, A.vox,
                                                                                p_init, seed ? 1 : 0, p_cur, p_next);
     else
-        k_anchor_spmv<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(A.n, A.rowptr, A.col, A.w, A.b, A.c,
+        k_anchor_spmv<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(A.n, A.rowptr, A.rowlen, A.col, A.w, A.b, A.c,
                                                                           A.vox, p_init, seed ? 1 : 0, p_cur, p_next);
     OM_COUNT_LAUNCH();
     if (red2) return change_sums(A.n, p_cur, p_next, gauge, ref_anchor, A.red, red2, st, nullptr);

@@ -74,7 +74,7 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x)
 
 // Plain method: every voxel of the line, the entry included, receives p[entry] + I(v).
 template <bool BF16>
-__global__ void __launch_bounds__(256) k_sweep_plain(Grid g, const LineRec *__restrict__ lines,
+__global__ void __launch_bounds__(256, 6) k_sweep_plain(Grid g, const LineRec *__restrict__ lines,
                                                      const uint32_t *__restrict__ gbase,
                                                      const uint32_t *__restrict__ desc, long long n_lines,
                                                      const float4 *__restrict__ f32,
@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(256) k_sweep_plain(Grid g, const LineRec *__re
 // increment); a good voxel after a pause restarts the segment at that voxel; the z
 // branch keeps the running curl/count sums on restart.
 template <bool BF16>
-__global__ void __launch_bounds__(256) k_sweep_select(Grid g, const LineRec *__restrict__ lines,
+__global__ void __launch_bounds__(256, 6) k_sweep_select(Grid g, const LineRec *__restrict__ lines,
                                                       const uint32_t *__restrict__ gbase,
                                                       const uint32_t *__restrict__ desc, long long n_lines,
                                                       const float4 *__restrict__ f32,
@@ -152,11 +152,12 @@ __global__ void __launch_bounds__(256) k_sweep_select(Grid g, const LineRec *__r
                 if (!paused && good) {
                     float term = sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z));
                     kahan_add(I, comp, term);
-                    csum += __fdiv_rn(cn, 10000.0f);
+                    // weight n / sum(curl / 1e4) of the reference (K:2390-2392); one
+                    // correctly rounded reciprocal instead of its two divisions
+                    csum += cn * 1.0e-4f;
                     nseg += 1.0f;
-                    float wp = __fdiv_rn(p0 + I, csum) * nseg;
-                    float wc = __fdiv_rn(1.0f, csum) * nseg;
-                    atomicAdd(pncnt + L.v, make_float2(wp, wc));
+                    float wc = __frcp_rn(csum) * nseg;
+                    atomicAdd(pncnt + L.v, make_float2((p0 + I) * wc, wc));
                 }
                 bool enter_bad = (a == 0) ? ((!paused && cn >= thr) || cn == 0.0f) : (!paused && cn >= thr);
                 if (enter_bad) paused = true;

@@ -147,6 +147,35 @@ __global__ void __launch_bounds__(256) k_walk(Grid g, const DirEntry *dirs, Line
     if ((threadIdx.x & 31) == (__ffs(mask) - 1)) atomicAdd(&counters[1], (unsigned long long)u);
 }
 
+// Number of lines through every voxel (entry included): a geometry-only bound on the
+// contributions any voxel can receive in one sweep.
+__global__ void __launch_bounds__(256) k_lines_through(Grid g, const LineRec *__restrict__ lines,
+                                                       const uint32_t *__restrict__ gbase,
+                                                       const uint32_t *__restrict__ desc, long long n_lines,
+                                                       uint32_t *cnt)
+{
+    long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= n_lines) return;
+    LineRec r = lines[li];
+    int ie = (int)(r.e % (uint32_t)g.X), je = (int)((r.e / (uint32_t)g.X) % (uint32_t)g.Y),
+        ke = (int)(r.e / (uint32_t)g.XY);
+    int ix = (int)(r.x % (uint32_t)g.X), jx = (int)((r.x / (uint32_t)g.X) % (uint32_t)g.Y),
+        kx = (int)(r.x / (uint32_t)g.XY);
+    const int d0 = ix > ie ? 1 : -1, d1 = (jx > je ? 1 : -1) * g.X, d2 = (kx > ke ? 1 : -1) * (int)g.XY;
+    long long v = r.e;
+    atomicAdd(cnt + v, 1u);
+    const uint32_t *dp = desc + 32ull * gbase[li >> 5] + (li & 31);
+    for (int s0 = 0; s0 < r.m; s0 += 16) {
+        uint32_t w = __ldg(dp + 32 * (s0 >> 4));
+        int n = min(16, r.m - s0);
+        for (int t = 0; t < n; t++, w >>= 2) {
+            int a = (int)(w & 3u);
+            v += a == 0 ? d0 : (a == 1 ? d1 : d2);
+            atomicAdd(cnt + v, 1u);
+        }
+    }
+}
+
 // ---------------------------------------------------------------- scan
 template <typename T>
 __device__ __forceinline__ T block_exclusive_scan(T v, T *sh, T *total)
@@ -270,8 +299,23 @@ cudaError_t exclusive_scan_u64(const unsigned long long *in, unsigned long long 
         }                                                                 \
     } while (0)
 
+cudaError_t ensure_lines_through(Geometry *g, cudaStream_t st)
+{
+    if (g->d_lines_through) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&g->d_lines_through, sizeof(uint32_t) * (size_t)std::max(g->grid.V, 1LL));
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(g->d_lines_through, 0, sizeof(uint32_t) * (size_t)g->grid.V, st);
+    if (e != cudaSuccess || g->n_lines == 0) return e;
+    k_lines_through<<<(unsigned)((g->n_lines + 255) / 256), 256, 0, st>>>(g->grid, g->d_lines, g->d_gbase, g->d_desc,
+                                                                          g->n_lines, g->d_lines_through);
+    OM_COUNT_LAUNCH();
+    return cudaGetLastError();
+}
+
 void free_geometry(Geometry *g)
 {
+    cudaFree(g->d_lines_through);
+    g->d_lines_through = nullptr;
     cudaFree(g->d_off);
     cudaFree(g->d_lines);
     cudaFree(g->d_gbase);

@@ -57,6 +57,7 @@ struct Geometry {
     LineRec *d_lines = nullptr;
     uint32_t *d_gbase = nullptr;    // n_groups + 1 prefix sums of words per lane
     uint32_t *d_desc = nullptr;
+    uint32_t *d_lines_through = nullptr;  // per voxel: lines through it (built on first use)
     long long n_lines = 0, n_groups = 0, n_words = 0;
     long long n_units = 0;          // sum over lines of (steps + 1)
     long long walk_errors = 0;
@@ -69,6 +70,8 @@ struct Geometry {
 // g->d_off, g->d_lines, g->d_gbase, g->d_desc; walks every line.  Synchronises `st`.
 cudaError_t build_geometry(Geometry *g, cudaStream_t st, std::string *err);
 void free_geometry(Geometry *g);
+// Count the lines through every voxel into g->d_lines_through (once per geometry).
+cudaError_t ensure_lines_through(Geometry *g, cudaStream_t st);
 
 // Exclusive scans (out has n + 1 entries; out[n] = total).  tmp must hold
 // scan_tmp_elems(n) elements.
@@ -113,7 +116,8 @@ struct Anchor {
     uint32_t *bits = nullptr;       // V bits
     int32_t *id = nullptr;          // V: anchor id or -1
     uint32_t *vox = nullptr;        // n: voxel of anchor
-    unsigned long long *rowptr = nullptr;  // n + 1
+    unsigned long long *rowptr = nullptr;  // n + 1: row capacities (lines through the voxel)
+    uint32_t *rowlen = nullptr;     // n: entries in each row
     uint32_t *col = nullptr;        // nnz
     float *w = nullptr;             // nnz
     float *b = nullptr;             // n: sum of w * I
@@ -130,7 +134,7 @@ struct Anchor {
 };
 // Builds the operator; returns cudaErrorNotSupported (nothing filled) when it would hold
 // more than max_nnz entries (max_nnz < 0: no limit).
-cudaError_t anchor_build(const Geometry &geo, const Field &f, int method, bool bf16,
+cudaError_t anchor_build(Geometry &geo, const Field &f, int method, bool bf16,
                          long long ref_voxel, long long max_nnz, Anchor *A, cudaStream_t st,
                          std::string *err);
 void anchor_free(Anchor *A);

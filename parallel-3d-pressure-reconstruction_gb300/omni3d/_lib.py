@@ -70,6 +70,10 @@ SIGNATURES = {
     "omni3d_geometry_info": (_i, [_vp, C.POINTER(_ll), C.POINTER(_ll), C.POINTER(_ll)]),
     "omni3d_line_table": (_i, [_vp, _vp, _ll]),
     "omni3d_line_steps": (_i, [_vp, _ll, _vp, _i]),
+    "omni3d_batch_create": (_i, [_vp, _i, C.POINTER(_vp)]),
+    "omni3d_batch_destroy": (_i, [_vp]),
+    "omni3d_batch_last_error": (C.c_char_p, [_vp]),
+    "omni3d_batch_solve": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, C.POINTER(Stats)]),
     "omni3d_icosphere": (_i, [_i, _vp, _i]),
     "omni3d_read_directions": (_i, [C.c_char_p, _i, _vp]),
     "omni3d_read_params": (_i, [C.c_char_p, C.POINTER(FileParams)]),

@@ -261,3 +261,88 @@ def write_curl(path, dims, x, y, z, curl):
     x, y, z, curl = f(x), f(y), f(z), f(curl)
     check(lib().omni3d_write_curl(str(path).encode(), nx, ny, nz, x.ctypes.data, y.ctypes.data, z.ctypes.data,
                                   curl.ctypes.data))
+
+
+class Batch:
+    """Several snapshots, one context each (grid sizes may differ), solved together in one
+    CUDA-graph launch (omni3d_batch_*).  Members need the plain method, the anchor solver
+    and tol = 0."""
+
+    def __init__(self, solvers):
+        self.solvers = list(solvers)
+        arr = (C.c_void_p * len(self.solvers))(*[s.handle for s in self.solvers])
+        h = C.c_void_p()
+        check(lib().omni3d_batch_create(arr, len(self.solvers), C.byref(h)))
+        self._h = h
+        self._keep = arr
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().omni3d_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def solve(self, fields, p_init=None, out=None):
+        """fields: list of (ax, ay, az) per member (all CUDA tensors, or all host arrays).
+        out: optional list of (p, count) output buffers (reused between calls so that the
+        captured graph is relaunched).  Returns ([p], [count], stats)."""
+        n = len(self.solvers)
+        if len(fields) != n:
+            raise ValueError("one field per member")
+        dev = _is_cuda_tensor(fields[0][0])
+        keep = []
+
+        def ptr(a, V):
+            if a is None:
+                return None
+            if dev:
+                if not (_is_cuda_tensor(a) and a.is_contiguous() and a.numel() == V):
+                    raise ValueError("batch inputs must all be contiguous CUDA tensors")
+                keep.append(a)
+                return a.data_ptr()
+            h = _as_host(a, V)
+            keep.append(h)
+            return h.ctypes.data
+
+        outs = []
+        for i, s in enumerate(self.solvers):
+            if out is not None:
+                outs.append(out[i])
+            elif dev:
+                import torch
+
+                p = torch.empty(s.V, dtype=torch.float32, device=fields[i][0].device)
+                outs.append((p, torch.empty_like(p)))
+            else:
+                outs.append((np.empty(s.V, np.float32), np.empty(s.V, np.float32)))
+        arrs = []
+        for k in range(3):
+            arrs.append((C.c_void_p * n)(*[ptr(fields[i][k], s.V) for i, s in enumerate(self.solvers)]))
+        p0 = None
+        if p_init is not None:
+            p0 = (C.c_void_p * n)(*[ptr(p_init[i], s.V) for i, s in enumerate(self.solvers)])
+        po = (C.c_void_p * n)(*[ptr(outs[i][0], s.V) for i, s in enumerate(self.solvers)])
+        co = (C.c_void_p * n)(*[ptr(outs[i][1], s.V) for i, s in enumerate(self.solvers)])
+        if dev:
+            import torch
+
+            torch.cuda.current_stream().synchronize()
+        st = L.Stats()
+        rc = lib().omni3d_batch_solve(self._h, arrs[0], arrs[1], arrs[2], p0, po, co, int(dev), C.byref(st))
+        if rc < 0:
+            msg = (lib().omni3d_batch_last_error(self._h) or b"").decode(errors="replace")
+            raise L.Omni3DError(rc, msg)
+        ps = [o[0].reshape(s.dims[::-1]) for o, s in zip(outs, self.solvers)]
+        cs = [o[1].reshape(s.dims[::-1]) for o, s in zip(outs, self.solvers)]
+        return ps, cs, st.as_dict()
