@@ -141,6 +141,14 @@ int omni3d_sweep(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
 int omni3d_gauge(omni3d_ctx *ctx, float *p, const float *count, long long n, int gauge,
                  long long ref, int device_ptrs);
 
+/* Adjoint of the last omni3d_solve on ctx (plain method): writes the gradient of
+ * <grad_p, p_out> with respect to ax, ay, az, i.e. the transpose of the solve's affine map
+ * (scatter back along the lines and through the iterations, no stored iterates), including
+ * the transpose of the output gauge.  No counterpart in the reference; it serves pressure
+ * sensitivities and torch.autograd (the omni3d Python package). */
+int omni3d_adjoint(omni3d_ctx *ctx, const float *grad_p, float *grad_ax, float *grad_ay,
+                   float *grad_az, int device_ptrs);
+
 /* |curl a| x mask: calCurlofMaterialAccCPU, K:8352-8378 (GPU twin K:6863-6888). */
 int omni3d_curl(omni3d_ctx *ctx, const float *ax, const float *ay, const float *az,
                 const float *mask, float *curl_out, int device_ptrs);

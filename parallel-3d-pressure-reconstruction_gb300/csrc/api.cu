@@ -65,6 +65,10 @@ struct omni3d_ctx {
     DeviceBuf pvol_a, pvol_b, pout, cnt, pncnt, scratch, flags;
     Anchor anc;
     bool anc_cached = false;  // plain method: operator structure built for this geometry
+    AdjointBuffers adj;
+    DeviceBuf adj_g, adj_out;  // staging of the adjoint's host arguments
+    int last_iterations = -1;  // iterations of the last solve (-1: no solve yet)
+    int last_method = -1;
     cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 };
 
@@ -408,6 +412,9 @@ int omni3d_destroy(omni3d_ctx *ctx)
     free_geometry(&ctx->geo);
     cudaFree(ctx->geo.d_dirs);
     anchor_free(&ctx->anc);
+    adjoint_free(&ctx->adj);
+    ctx->adj_g.release();
+    ctx->adj_out.release();
     for (DeviceBuf *b : {&ctx->in_ax, &ctx->in_ay, &ctx->in_az, &ctx->in_aux, &ctx->in_pinit, &ctx->f32, &ctx->b16,
                          &ctx->curl, &ctx->pvol_a, &ctx->pvol_b, &ctx->pout, &ctx->cnt, &ctx->pncnt, &ctx->scratch,
                          &ctx->flags})
@@ -619,6 +626,7 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
             e = anchor_build(ctx->geo, F, P.method, bf16, P.gauge == OMNI3D_GAUGE_POINT ? ref : -1,
                              ctx->geo.n_units / 4, &ctx->anc, st, &aerr);
             ctx->anc_cached = e == cudaSuccess && P.method == OMNI3D_METHOD_PLAIN;
+            adjoint_free(&ctx->adj);
         }
         if (e == cudaErrorNotSupported) {
             cudaGetLastError();
@@ -717,6 +725,8 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
     cudaEventRecord(ctx->ev[4], st);
     CK(ctx, cudaStreamSynchronize(st));
     CK(ctx, cudaGetLastError());
+    ctx->last_iterations = done;
+    ctx->last_method = P.method;
     if (stats) {
         stats->iterations = done;
         stats->rel_change = rel;
@@ -735,6 +745,61 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
         stats->solver_used = solver;
     }
     if (ctx->geo.walk_errors) return fail(ctx, OMNI3D_ERR_NUMERIC, "line walk hit the wrong-point branch");
+    return OMNI3D_OK;
+}
+
+int omni3d_adjoint(omni3d_ctx *ctx, const float *grad_p, float *grad_ax, float *grad_ay, float *grad_az,
+                   int device_ptrs)
+{
+    if (!ctx || !grad_p || !grad_ax || !grad_ay || !grad_az) return fail(ctx, OMNI3D_ERR_ARG, "NULL argument");
+    if (ctx->last_iterations < 0) return fail(ctx, OMNI3D_ERR_STATE, "no solve to differentiate on this context");
+    if (ctx->last_method != OMNI3D_METHOD_PLAIN)
+        return fail(ctx, OMNI3D_ERR_STATE, "the adjoint covers the plain method (the selected method's weights "
+                                           "depend on the field non-linearly)");
+    cudaSetDevice(ctx->prm.device);
+    const omni3d_params &P = ctx->prm;
+    const Grid &g = ctx->geo.grid;
+    const long long V = g.V;
+    const bool dev = device_ptrs != 0;
+    cudaStream_t st = ctx->st;
+    const long long ref = (long long)P.ref_i + (long long)P.ref_j * g.X + (long long)P.ref_k * g.XY;
+    if (!ctx->anc_cached) {  // the last solve ran the sweep form: build the operator now
+        Field F;
+        F.f32 = ctx->f32.as<float4>();
+        F.bf16 = P.grad_storage == OMNI3D_GRAD_BF16 ? ctx->b16.as<uint2>() : nullptr;
+        std::string aerr;
+        cudaError_t e = anchor_build(ctx->geo, F, OMNI3D_METHOD_PLAIN, F.bf16 != nullptr,
+                                     P.gauge == OMNI3D_GAUGE_POINT ? ref : -1, -1, &ctx->anc, st, &aerr);
+        if (e != cudaSuccess) return fail(ctx, OMNI3D_ERR_CUDA, "anchor operator: " + aerr);
+        ctx->anc_cached = true;
+        adjoint_free(&ctx->adj);
+    }
+    const float *dg = grad_p;
+    CK(ctx, ctx->adj_g.ensure(sizeof(float) * (size_t)V));
+    if (!dev) {
+        CK(ctx, ctx->adj_out.ensure(sizeof(float) * 3 * (size_t)V));
+        CK(ctx, cudaMemcpyAsync(ctx->adj_out.p, grad_p, sizeof(float) * (size_t)V, cudaMemcpyHostToDevice, st));
+        dg = ctx->adj_out.as<float>();
+    }
+    CK(ctx, ctx->scratch.ensure(sizeof(double) * std::max(change_scratch_doubles(),
+                                                          std::max(gauge_scratch_doubles(),
+                                                                   gauge_transpose_scratch_doubles())) + 64));
+    float *gg = ctx->adj_g.as<float>();
+    CK(ctx, gauge_transpose(V, P.gauge, ref, dg, ctx->cnt.as<float>(), gg, ctx->scratch.as<double>() + 4, st));
+    float *gx = grad_ax, *gy = grad_ay, *gz = grad_az;
+    if (!dev) {
+        gx = ctx->adj_out.as<float>();
+        gy = gx + V;
+        gz = gy + V;
+    }
+    CK(ctx, adjoint_plain(ctx->geo, ctx->anc, &ctx->adj, ctx->last_iterations, gg, ctx->cnt.as<float>(), gx, gy, gz,
+                          st));
+    if (!dev) {
+        CK(ctx, cudaMemcpyAsync(grad_ax, gx, sizeof(float) * (size_t)V, cudaMemcpyDeviceToHost, st));
+        CK(ctx, cudaMemcpyAsync(grad_ay, gy, sizeof(float) * (size_t)V, cudaMemcpyDeviceToHost, st));
+        CK(ctx, cudaMemcpyAsync(grad_az, gz, sizeof(float) * (size_t)V, cudaMemcpyDeviceToHost, st));
+    }
+    CK(ctx, cudaStreamSynchronize(st));
     return OMNI3D_OK;
 }
 

@@ -424,6 +424,15 @@ template <int PASS>
 cudaError_t run_pass(const Geometry &geo, const Field &f, int method, bool bf16, const Sink &S, cudaStream_t st)
 {
     if (geo.n_lines == 0) return cudaSuccess;
+    // every pointer the pass dereferences must be set: refuse to launch otherwise
+    const bool need_field = PASS == kFill || PASS == kRhs;
+    bool ok = geo.d_lines && geo.d_gbase && geo.d_desc;
+    if (PASS == kMark) ok = ok && S.flag;
+    else ok = ok && S.bits && S.id && S.b;
+    if (PASS == kFill) ok = ok && S.rowptr && S.cursor && S.col && S.w && S.c;
+    if (need_field) ok = ok && (bf16 ? f.bf16 != nullptr : f.f32 != nullptr);
+    if (method == OMNI3D_METHOD_SELECT) ok = ok && f.curl && (bf16 || f.f32);
+    if (!ok) return cudaErrorInvalidValue;
     unsigned blocks = (unsigned)((geo.n_lines + 255) / 256);
     const Grid &g = geo.grid;
     if (method == OMNI3D_METHOD_SELECT) {
@@ -558,6 +567,8 @@ cudaError_t anchor_build(Geometry &geo, const Field &f, int method, bool bf16, l
     AN_TRY(cudaMemsetAsync(cursor, 0, sizeof(uint32_t) * (size_t)std::max<long long>(n, 1), st));
     AN_TRY(cudaMemsetAsync(A->b, 0, sizeof(float) * (size_t)std::max<long long>(n, 1), st));
     AN_TRY(cudaMemsetAsync(A->c, 0, sizeof(float) * (size_t)std::max<long long>(n, 1), st));
+    S.bits = A->bits;
+    S.id = A->id;
     S.rowptr = A->rowptr;
     S.cursor = cursor;
     S.col = A->col;

@@ -304,6 +304,10 @@ cudaError_t sweep_full(const Geometry &geo, const Field &f, int method, bool bf1
                        float2 *pncnt, cudaStream_t st)
 {
     if (geo.n_lines == 0) return cudaSuccess;
+    // every pointer the kernels dereference must be set: refuse to launch otherwise
+    if (!geo.d_lines || !geo.d_gbase || !geo.d_desc || !p || !pncnt || (bf16 ? !f.bf16 : !f.f32) ||
+        (method == OMNI3D_METHOD_SELECT && !f.curl))
+        return cudaErrorInvalidValue;
     unsigned blocks = (unsigned)((geo.n_lines + 255) / 256);
     if (method == OMNI3D_METHOD_SELECT) {
         if (bf16)

@@ -165,6 +165,24 @@ cudaError_t anchor_scatter(const Anchor &A, const float *pa, float *vol, cudaStr
 // Gather anchor values from a volume.
 cudaError_t anchor_gather(const Anchor &A, const float *vol, float *pa, cudaStream_t st);
 
+// Adjoint of the plain-method solve (kernels_adjoint.cu).
+struct AdjointBuffers {
+    unsigned long long *tptr = nullptr;  // transposed operator (built once per operator)
+    uint32_t *trow = nullptr;
+    unsigned long long *tmp = nullptr;
+    float *mu = nullptr, *lam = nullptr, *nxt = nullptr, *acc = nullptr;
+};
+void adjoint_free(AdjointBuffers *B);
+// gx, gy, gz = d<g, p_K>/d(ax, ay, az) for the plain method after K iterations, given the
+// operator A of that solve and its per-voxel count cnt.
+cudaError_t adjoint_plain(const Geometry &geo, const Anchor &A, AdjointBuffers *B, int K,
+                          const float *g, const float *cnt, float *gx, float *gy, float *gz,
+                          cudaStream_t st);
+// out = G^T g for the output gauge G (part: gauge_transpose_scratch_doubles()).
+cudaError_t gauge_transpose(long long V, int gauge, long long ref, const float *g,
+                            const float *cnt, float *out, double *part, cudaStream_t st);
+size_t gauge_transpose_scratch_doubles();
+
 // Gauge: subtract p[ref] (mode POINT) or the mean over count > 0 (MEAN), FP64 reduction.
 cudaError_t apply_gauge(long long V, int gauge, long long ref, const float *cnt, float *p,
                         double *scratch, cudaStream_t st);

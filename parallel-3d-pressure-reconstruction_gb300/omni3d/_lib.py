@@ -67,6 +67,7 @@ SIGNATURES = {
     "omni3d_sweep": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i]),
     "omni3d_curl": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _i]),
     "omni3d_gauge": (_i, [_vp, _vp, _vp, _ll, _i, _ll, _i]),
+    "omni3d_adjoint": (_i, [_vp, _vp, _vp, _vp, _vp, _i]),
     "omni3d_geometry_info": (_i, [_vp, C.POINTER(_ll), C.POINTER(_ll), C.POINTER(_ll)]),
     "omni3d_line_table": (_i, [_vp, _vp, _ll]),
     "omni3d_line_steps": (_i, [_vp, _ll, _vp, _i]),

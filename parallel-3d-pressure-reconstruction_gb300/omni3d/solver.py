@@ -71,6 +71,7 @@ class Omni3D:
         P.device = int(device)
         self.params = P
         self.method = method
+        self.solve_count = 0
         h = C.c_void_p()
         check(lib().omni3d_create(C.byref(P), C.byref(h)))
         self._h = h
@@ -154,6 +155,7 @@ class Omni3D:
             pp, cp = p.ctypes.data, cnt.ctypes.data
         check(lib().omni3d_solve(self._h, ptrs[0], ptrs[1], ptrs[2], ptrs[3], ptrs[4], ptrs[5], pp, cp, int(dev),
                                  C.byref(st)), self._h)
+        self.solve_count += 1
         shape = self.dims[::-1]
         return SolveResult(p.reshape(shape), cnt.reshape(shape), st.as_dict())
 
@@ -173,6 +175,22 @@ class Omni3D:
         check(lib().omni3d_sweep(self._h, ptrs[0], ptrs[1], ptrs[2], ptrs[3], ptrs[4], a, b, int(dev)), self._h)
         shape = self.dims[::-1]
         return pn.reshape(shape), cnt.reshape(shape)
+
+    def adjoint(self, grad_p):
+        """Gradient of <grad_p, p> with respect to (ax, ay, az) for the last solve on this
+        context (plain method): the transpose of the solve's affine map."""
+        if _is_cuda_tensor(grad_p):
+            import torch
+
+            g = grad_p.reshape(-1).to(torch.float32).contiguous()
+            out = [torch.empty(self.V, dtype=torch.float32, device=g.device) for _ in range(3)]
+            torch.cuda.current_stream().synchronize()
+            check(lib().omni3d_adjoint(self._h, g.data_ptr(), *[o.data_ptr() for o in out], 1), self._h)
+        else:
+            g = _as_host(grad_p, self.V)
+            out = [np.empty(self.V, np.float32) for _ in range(3)]
+            check(lib().omni3d_adjoint(self._h, g.ctypes.data, *[o.ctypes.data for o in out], 0), self._h)
+        return [o.reshape(self.dims[::-1]) for o in out]
 
     def gauge(self, p, count=None, mode="mean", ref=0):
         """Remove the constant mode of p (returns a gauged copy): p - p[ref] or p - mean(p)
