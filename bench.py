@@ -112,6 +112,19 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(value, device=None):
+    """Max of a per-rank float over all ranks (the job's time is its slowest rank); the
+    identity without an initialised process group."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def measured_peak_hbm():
     try:
         with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as fh:
@@ -361,11 +374,7 @@ def main():
             for t, s_ in zip(d_in, src):  # rewrite inputs outside the timed region
                 t.copy_(s_)
     torch.cuda.synchronize()
-    t_dev = float(np.mean(times))
-    if world > 1:
-        tt = torch.tensor([t_dev], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_dev = float(tt.item())
+    t_dev = max_over_ranks(float(np.mean(times)), dev)
 
     # end to end through the C ABI with pinned host buffers
     t_e2e = None
@@ -406,7 +415,8 @@ def main():
     achieved = alg / t_sweep / 1e9
 
     line = {
-        "metric": METRIC, "value": t_dev, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "metric": METRIC, "value": t_dev, "unit": "s", "n_gpus": world,
+        "units_all_ranks": geo["n_units"] * world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_dev * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded analytic blobs, a = -grad p / rho + 5% noise)",
         "config": config_dict(args),

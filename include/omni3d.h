@@ -76,6 +76,9 @@ typedef struct {
     int seed_first_iteration;  /* 1 (reference, K:8811): the first sweep accumulates on top of
                                   p_init; 0: on top of zero */
     int device;                /* CUDA device ordinal */
+    long long anchor_max_links;/* anchor operator entries allowed before the solve falls back
+                                  to the sweep form (0: what 80 % of the free device memory
+                                  holds) */
 } omni3d_params;
 
 typedef struct {
@@ -94,8 +97,7 @@ typedef struct {
     double ms_sweep;           /* device time of the final full sweep kernel alone */
     long long kernel_launches; /* CUDA kernels this library launched during the call */
     int solver_used;           /* OMNI3D_SOLVER_*: the anchor solver falls back to the sweep
-                                  solver when its operator would cost more than a quarter of a
-                                  sweep per iteration (many scattered segment starts) */
+                                  solver when its operator would exceed anchor_max_links */
 } omni3d_stats;
 
 /* Fill *p with the reference's defaults (K:8512-8535) and this implementation's. */

@@ -174,6 +174,7 @@ int check_params(const omni3d_params *p, std::string *why)
         return OMNI3D_ERR_ARG;
     }
     if (!(p->tol >= 0.0)) { *why = "tol must be >= 0"; return OMNI3D_ERR_ARG; }
+    if (p->anchor_max_links < 0) { *why = "anchor_max_links must be >= 0"; return OMNI3D_ERR_ARG; }
     double ng = std::max(std::max(p->nx, p->ny), p->nz) * 1.732 / (double)p->line_spacing;
     if (ng * ng * (double)p->n_dirs / 256.0 > 2.0e9) { *why = "too many lines (lattice x directions)"; return OMNI3D_ERR_RANGE; }
     return OMNI3D_OK;
@@ -623,8 +624,14 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
             aerr = cudaGetErrorString(e);
         } else {
             ctx->anc_cached = false;
-            e = anchor_build(ctx->geo, F, P.method, bf16, P.gauge == OMNI3D_GAUGE_POINT ? ref : -1,
-                             ctx->geo.n_units / 4, &ctx->anc, st, &aerr);
+            long long max_links = P.anchor_max_links;
+            if (max_links <= 0) {  // what 80 % of the free memory holds (column + weight)
+                size_t fr = 0, tot = 0;
+                cudaMemGetInfo(&fr, &tot);
+                max_links = (long long)(0.8 * (double)fr / 8.0);
+            }
+            e = anchor_build(ctx->geo, F, P.method, bf16, P.gauge == OMNI3D_GAUGE_POINT ? ref : -1, max_links,
+                             &ctx->anc, st, &aerr);
             ctx->anc_cached = e == cudaSuccess && P.method == OMNI3D_METHOD_PLAIN;
             adjoint_free(&ctx->adj);
         }

@@ -35,7 +35,8 @@ class Params(C.Structure):
     _fields_ = [("nx", _i), ("ny", _i), ("nz", _i), ("dx", _f), ("dy", _f), ("dz", _f), ("density", _f),
                 ("line_spacing", _f), ("n_dirs", _i), ("dirs", _fp), ("max_iter", _i), ("threshold", _f),
                 ("method", _i), ("solver", _i), ("grad_storage", _i), ("tol", _d), ("gauge", _i),
-                ("ref_i", _i), ("ref_j", _i), ("ref_k", _i), ("seed_first_iteration", _i), ("device", _i)]
+                ("ref_i", _i), ("ref_j", _i), ("ref_k", _i), ("seed_first_iteration", _i), ("device", _i),
+                ("anchor_max_links", _ll)]
 
 
 class Stats(C.Structure):

@@ -45,7 +45,7 @@ class Omni3D:
 
     def __init__(self, dims, spacing, dirs, *, density=1.0, line_spacing=1.0, max_iter=4, threshold=0.0,
                  method="plain", solver="anchor", grad="f32", tol=0.0, gauge="none", ref=(0, 0, 0),
-                 seed_first_iteration=True, device=0):
+                 seed_first_iteration=True, device=0, anchor_max_links=0):
         nx, ny, nz = (int(d) for d in dims)
         self.dims = (nx, ny, nz)
         self.V = nx * ny * nz
@@ -69,6 +69,7 @@ class Omni3D:
         P.ref_i, P.ref_j, P.ref_k = (int(r) for r in ref)
         P.seed_first_iteration = int(bool(seed_first_iteration))
         P.device = int(device)
+        P.anchor_max_links = int(anchor_max_links)
         self.params = P
         self.method = method
         self.solve_count = 0

@@ -239,21 +239,23 @@ def test_counts_deterministic(omni):
     assert synthetic.relative_l2(a.p, b.p, gauge="none") < 1e-6
 
 
-def test_select_scattered_bad_voxels_falls_back_to_sweep(omni, orc):
-    """With half of the voxels above the threshold, segment starts are everywhere and the
-    anchor operator would cost more than a sweep: the solve runs the sweep form instead and
-    still matches the oracle."""
+def test_select_scattered_bad_voxels_and_fallback(omni, orc):
+    """With half of the voxels above the threshold, segment starts are everywhere: the
+    anchor operator is large but still exact; with a small anchor_max_links the solve runs
+    the sweep form instead.  Both match the oracle."""
     dims = (16, 14, 12)
     f = _field(dims, seed=13, noise=0.3)
     dirs = omni.icosphere(2)
     curl = orc.curl(dims, f["spacing"], f["ax"], f["ay"], f["az"], f["mask"])
     thr = float(np.percentile(curl[curl > 0], 50))
-    with omni.Omni3D(dims, f["spacing"], dirs, max_iter=3, method="select", threshold=thr) as s:
-        r = s.solve(f["ax"], f["ay"], f["az"], curl=curl)
-    assert r.stats["solver_used"] == 1
     ep, ecnt = orc.solve(dims, f["spacing"], dirs, f["ax"], f["ay"], f["az"], np.zeros(curl.size, np.float32), 3,
                          mode=1, thr=thr, curl=curl, precision="f64")
-    assert synthetic.relative_l2(r.p, ep, gauge="none") < TOL_P_SELECT
+    for limit, used in ((0, 0), (1000, 1)):
+        with omni.Omni3D(dims, f["spacing"], dirs, max_iter=3, method="select", threshold=thr,
+                         anchor_max_links=limit) as s:
+            r = s.solve(f["ax"], f["ay"], f["az"], curl=curl)
+        assert r.stats["solver_used"] == used
+        assert synthetic.relative_l2(r.p, ep, gauge="none") < TOL_P_SELECT
 
 
 def test_batch_graph_matches_single_solves(omni, orc):
