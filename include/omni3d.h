@@ -168,6 +168,26 @@ int omni3d_line_table(omni3d_ctx *ctx, int32_t *rows, long long n_max);
 /* Copy the staircase of line `line` (one axis code 0/1/2 per step) to host memory. */
 int omni3d_line_steps(omni3d_ctx *ctx, long long line, int8_t *axes, int cap);
 
+/* Voxel limit of omni3d_sweep_noalloc (its scratch is sized for it at build time). */
+#define OMNI3D_NOALLOC_MAX_VOXELS (64LL * 64 * 64)
+
+/* omni3d_sweep without any device allocation, for callers that cannot call cudaMalloc at
+ * that point: a solver step running inside a CUDA-graph capture, a framework whose own
+ * memory pool owns the device, a real-time loop that cannot take cudaMalloc's implicit
+ * synchronisation.  No counterpart in the reference.  Same arguments and result as
+ * omni3d_sweep with device pointers (pn and count are added to), FP32 gradient storage
+ * only, at most OMNI3D_NOALLOC_MAX_VOXELS voxels (larger grids are rejected with
+ * OMNI3D_ERR_RANGE).  The packed field and the (pn, count) accumulator live in static
+ * device arrays of that size that every GPU loading the library keeps until exit.  The
+ * call only enqueues work on `stream` (NULL: the context's stream); the results are ready
+ * when that stream reaches them.  All calls share the static arrays: calls that overlap on
+ * the GPU (other streams, other contexts, other threads) race and must be serialised by
+ * the caller.  The first call on a device looks up the arrays' device addresses, so make
+ * it before any stream capture. */
+int omni3d_sweep_noalloc(omni3d_ctx *ctx, const float *ax, const float *ay, const float *az,
+                         const float *curl, const float *p, float *pn, float *count,
+                         void *stream);
+
 /* ---------------------------------------------------------------- batches of snapshots */
 
 /* A batch solves several snapshots, each with its own context (grid sizes may differ), in

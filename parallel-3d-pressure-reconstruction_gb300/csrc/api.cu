@@ -810,6 +810,18 @@ int omni3d_adjoint(omni3d_ctx *ctx, const float *grad_p, float *grad_ax, float *
     return OMNI3D_OK;
 }
 
+}  // extern "C"
+
+// Context accessors for the translation units that do not see struct omni3d_ctx.
+namespace omni3d {
+const Geometry *context_geometry(const omni3d_ctx *ctx) { return &ctx->geo; }
+const omni3d_params *context_params(const omni3d_ctx *ctx) { return &ctx->prm; }
+cudaStream_t context_stream(const omni3d_ctx *ctx) { return ctx->st; }
+void context_set_error(omni3d_ctx *ctx, const std::string &msg) { ctx->err = msg; }
+}  // namespace omni3d
+
+extern "C" {
+
 // ------------------------------------------------------------------------- batches
 
 int omni3d_batch_create(omni3d_ctx *const *ctxs, int n, omni3d_batch **out)

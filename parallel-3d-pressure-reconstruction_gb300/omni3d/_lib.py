@@ -66,6 +66,7 @@ SIGNATURES = {
     "omni3d_set_stream": (_i, [_vp, _vp]),
     "omni3d_solve": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, C.POINTER(Stats)]),
     "omni3d_sweep": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i]),
+    "omni3d_sweep_noalloc": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "omni3d_curl": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _i]),
     "omni3d_gauge": (_i, [_vp, _vp, _vp, _ll, _i, _ll, _i]),
     "omni3d_adjoint": (_i, [_vp, _vp, _vp, _vp, _vp, _i]),
