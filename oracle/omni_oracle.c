@@ -460,6 +460,48 @@ DEFINE_LINE_PLAIN(f64, double, 0)
 DEFINE_LINE_SELECT(f32, float, 1)
 DEFINE_LINE_SELECT(f64, double, 0)
 
+/* Weighted method along one line (K:1993-2135): the plain walk from the entry (no
+ * contribution to the entry itself), every step adds its increment, and a step's voxel
+ * receives (p0 + I)/C*n in pn and 1/C*n in count while C = sum(curl/1e4) != 0. */
+#define DEFINE_LINE_WEIGHTED(SUFFIX, REAL, EXACT)                                                 \
+    static void line_weighted_##SUFFIX(const orc_grid *g, const int in[3], const int out[3],     \
+                                       const signed char *ax, int n, const float *au,             \
+                                       const float *av, const float *aw, const float *curl,       \
+                                       const REAL *p, REAL *pn, REAL *cnt)                        \
+    {                                                                                             \
+        long X = g->X, XY = g->X * g->Y;                                                          \
+        int sg[3];                                                                                \
+        axis_signs(in, out, sg);                                                                  \
+        long e = in[0] + in[1] * X + in[2] * XY;                                                  \
+        long last = e;                                                                            \
+        const long stride[3] = {1, X, XY};                                                        \
+        const float *comp[3] = {au, av, aw};                                                      \
+        const float dl[3] = {g->dx, g->dy, g->dz};                                                \
+        REAL pint = 0, ctmp = 0, ntmp = 0;                                                        \
+        for (int s = 0; s < n; s++) {                                                             \
+            int a = ax[s];                                                                        \
+            long nx = last + sg[a] * stride[a];                                                   \
+            if (EXACT) {                                                                          \
+                float h = (-g->rho * (float)sg[a]) * dl[a];                                       \
+                float as = comp[a][nx] + comp[a][last];                                           \
+                pint = (REAL)((double)pint + ((double)h * 0.5) * (double)as);                    \
+                ctmp += (REAL)(curl[nx] / 10000);                                                 \
+            } else {                                                                              \
+                pint += -(double)g->rho * (double)sg[a] * (double)dl[a] * 0.5 *                  \
+                        ((double)comp[a][nx] + (double)comp[a][last]);                            \
+                ctmp += (double)curl[nx] / 10000.0;                                               \
+            }                                                                                     \
+            ntmp += 1;                                                                            \
+            if (ctmp != 0) {                                                                      \
+                pn[nx] += (p[e] + pint) * 1 / ctmp * ntmp;                                        \
+                cnt[nx] += 1 / ctmp * ntmp;                                                       \
+            }                                                                                     \
+            last = nx;                                                                            \
+        }                                                                                         \
+    }
+DEFINE_LINE_WEIGHTED(f32, float, 1)
+DEFINE_LINE_WEIGHTED(f64, double, 0)
+
 /* ------------------------------------------------------------------------------------ */
 /* full sweep, normalisation, iteration                                                   */
 /* ------------------------------------------------------------------------------------ */
@@ -469,7 +511,7 @@ typedef struct {
     float dx, dy, dz, rho, ls, thr;
     int nv;
     const float *k1, *k2, *k3;
-    int mode;          /* 0 plain, 1 select */
+    int mode;          /* 0 plain, 1 select, 2 weighted */
     int geom_cpu_twin; /* 1: CPU-twin geometry (no pole guard, NoGrid without spacing) */
 } orc_problem;
 
@@ -503,6 +545,8 @@ static long max_path(long X, long Y, long Z) { return X + Y + Z + 4; }
                 if (n < 0) { errors++; n = -n - 1; }                                               \
                 if (P->mode == 0)                                                                  \
                     line_plain_##SUFFIX(&g, in, out, ax, n, au, av, aw, p, pn, cnt);               \
+                else if (P->mode == 2)                                                             \
+                    line_weighted_##SUFFIX(&g, in, out, ax, n, au, av, aw, curl, p, pn, cnt);      \
                 else                                                                               \
                     line_select_##SUFFIX(&g, in, out, ax, n, au, av, aw, curl, p, pn, cnt);        \
             }                                                                                      \

@@ -33,6 +33,11 @@ float bodyIntegralInnerSelect(long Xsize, long Ysize, long Zsize, int iin, int j
                               float k2, float k3, float deltx, float delty, float deltz,
                               float density, float *DuDt, float *DvDt, float *DwDt, float *p,
                               float *pn, float *curl, float *pcountinner, float threshold);
+float bodyIntegralInnerWeighted(long Xsize, long Ysize, long Zsize, int iin, int jin, int kin,
+                                int iout, int jout, int kout, float x, float y, float z, float k1,
+                                float k2, float k3, float deltx, float delty, float deltz,
+                                float density, float *DuDt, float *DvDt, float *DwDt, float *curl,
+                                float *p, float *pn, float *pcountinner);
 void calIndex(long *index, long Xsize, long Ysize, long Zsize);
 void omni3dparallellinesESInnerCPU(long Xsize, long Ysize, long Zsize, int NoAngles,
                                    float linespacing, float *k1_d, float *k2_d, float *k3_d,
@@ -57,7 +62,7 @@ struct Problem {
     float dx, dy, dz, rho, ls, thr;
     int nv;
     const float *k1, *k2, *k3;
-    int mode;  // 0 plain, 1 select
+    int mode;  // 0 plain, 1 select, 2 weighted
 };
 
 // Geometry of the GPU kernel (kernel.cu:6159-6194) with libm trigonometry.
@@ -101,6 +106,10 @@ long long sweep_range(const Problem &P, int d0, int d1, long *index, float *au, 
                         bodyIntegralInner(P.X, P.Y, P.Z, iin, jin, kin, iout, jout, kout, x, y, z,
                                           k1, k2, k3, P.dx, P.dy, P.dz, P.rho, au, av, aw, p, pn,
                                           cnt);
+                    else if (P.mode == 2)
+                        bodyIntegralInnerWeighted(P.X, P.Y, P.Z, iin, jin, kin, iout, jout, kout, x,
+                                                  y, z, k1, k2, k3, P.dx, P.dy, P.dz, P.rho, au, av,
+                                                  aw, curl, p, pn, cnt);
                     else
                         bodyIntegralInnerSelect(P.X, P.Y, P.Z, iin, jin, kin, iout, jout, kout, x,
                                                 y, z, k1, k2, k3, P.dx, P.dy, P.dz, P.rho, au, av,

@@ -12,6 +12,9 @@ outputs of the reference functions:
            the GPU normalisation (count > 0), starting from a nonzero j = 0 face
   select   14x12x10 grid with a masked sphere, 42 directions, 3 iterations of
            bodyIntegralInnerSelect, threshold at the 80th percentile of the curl
+  weighted 13x11x9 grid with a masked sphere, 42 directions, 3 iterations of
+           bodyIntegralInnerWeighted (curl-weighted, no entry contribution; voxels outside
+           the mask have curl 0, so lines that start there skip their first steps)
   ls07     10x9x8 grid, 42 directions, line spacing 0.7, 2 plain iterations
   cputwin  10x10x10 grid, 42 directions, 2 iterations of the reference's own CPU loop
            omni3dparallellinesESInnerCPU + devidecountInnerCPU (no pole guard, count > 1)
@@ -69,6 +72,16 @@ def main():
                 "select_ax": f["ax"].reshape(-1), "select_ay": f["ay"].reshape(-1), "select_az": f["az"].reshape(-1),
                 "select_mask": f["mask"].reshape(-1), "select_curl": curl, "select_thr": np.array(thr),
                 "select_p0": p0, "select_p": p, "select_count": c})
+    # weighted
+    d = (13, 11, 9)
+    f = field(d, 7, sphere=3.0)
+    p0 = pinit(d, 8)
+    curl = R.curl(d, f["spacing"], f["ax"], f["ay"], f["az"], f["mask"])
+    p, c = R.solve(d, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p0, 3, mode=2, curl=curl)
+    out.update({"weighted_dims": np.array(d), "weighted_spacing": np.array(f["spacing"], np.float32),
+                "weighted_ax": f["ax"].reshape(-1), "weighted_ay": f["ay"].reshape(-1),
+                "weighted_az": f["az"].reshape(-1), "weighted_mask": f["mask"].reshape(-1),
+                "weighted_curl": curl, "weighted_p0": p0, "weighted_p": p, "weighted_count": c})
     # line spacing 0.7
     d = (10, 9, 8)
     f = field(d, 5)

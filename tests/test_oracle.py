@@ -45,6 +45,17 @@ def test_golden_select_bit_exact(orc, gold):
     np.testing.assert_array_equal(_bits(p), _bits(g["select_p"]))
 
 
+def test_golden_weighted_bit_exact(orc, gold):
+    g = gold
+    d = _dims(g, "weighted")
+    curl = orc.curl(d, _sp(g, "weighted"), g["weighted_ax"], g["weighted_ay"], g["weighted_az"], g["weighted_mask"])
+    np.testing.assert_array_equal(_bits(curl), _bits(g["weighted_curl"]))
+    p, c = orc.solve(d, _sp(g, "weighted"), g["dirs"], g["weighted_ax"], g["weighted_ay"], g["weighted_az"],
+                     g["weighted_p0"], 3, mode=2, curl=curl)
+    np.testing.assert_array_equal(_bits(c), _bits(g["weighted_count"]))
+    np.testing.assert_array_equal(_bits(p), _bits(g["weighted_p"]))
+
+
 def test_golden_line_spacing(orc, gold):
     g = gold
     d = _dims(g, "ls07")
@@ -77,7 +88,7 @@ def test_golden_cpu_twin_loop(orc, gold):
 
 
 def test_oracle_matches_reference_functions(orc, reflib):
-    """Direct comparison with the reference functions on a non-cubic grid, both methods."""
+    """Direct comparison with the reference functions on a non-cubic grid, all three methods."""
     from omni3d import synthetic
     from omni3d.solver import icosphere
 
@@ -94,6 +105,10 @@ def test_oracle_matches_reference_functions(orc, reflib):
     thr = float(np.percentile(curl[curl > 0], 70))
     a, ca = orc.solve(dims, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p0, 2, mode=1, thr=thr, curl=curl)
     b, cb = reflib.solve(dims, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p0, 2, mode=1, thr=thr, curl=curl)
+    np.testing.assert_array_equal(_bits(ca), _bits(cb))
+    np.testing.assert_array_equal(_bits(a), _bits(b))
+    a, ca = orc.solve(dims, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p0, 2, mode=2, curl=curl)
+    b, cb = reflib.solve(dims, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p0, 2, mode=2, curl=curl)
     np.testing.assert_array_equal(_bits(ca), _bits(cb))
     np.testing.assert_array_equal(_bits(a), _bits(b))
 
