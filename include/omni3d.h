@@ -36,8 +36,13 @@ extern "C" {
 #define OMNI3D_ERR_NUMERIC (-7)  /* non-finite result or a line walk that failed */
 
 /* Integration method (Tutorial p.1 "Standard / Selected"). */
-#define OMNI3D_METHOD_PLAIN 0   /* bodyIntegralInner, K:1743-1863 */
-#define OMNI3D_METHOD_SELECT 1  /* bodyIntegralInnerSelect, K:2280-2537 (what main runs) */
+#define OMNI3D_METHOD_PLAIN 0     /* bodyIntegralInner, K:1743-1863 */
+#define OMNI3D_METHOD_SELECT 1    /* bodyIntegralInnerSelect, K:2280-2537 (what main runs) */
+#define OMNI3D_METHOD_WEIGHTED 2  /* bodyIntegralInnerWeighted, K:1993-2135, launched by
+                                     omni3dparallellinesESInnerWeighted K:6281-6345 (the
+                                     commented-out alternative of main, K:8844): every step
+                                     weighted by n / sum(curl/1e4) from the entry, no
+                                     contribution to the entry itself */
 
 /* Solver form.  Both produce the reference iteration's result; they differ in cost. */
 #define OMNI3D_SOLVER_ANCHOR 0  /* iterate only the voxels whose values feed back (line
@@ -118,7 +123,7 @@ int omni3d_set_stream(omni3d_ctx *ctx, void *stream);
 /* Solve one snapshot: the whole per-file block of main(), K:8794-8863 (initial state,
  * NoItr x {omni sweep, devidecountInner}, read back p and count).
  *   ax, ay, az   material acceleration Du/Dt, Dv/Dt, Dw/Dt (grad p = -rho a)
- *   curl         |curl a| x mask (OMNI3D_METHOD_SELECT; NULL: computed on the device
+ *   curl         |curl a| x mask (SELECT and WEIGHTED methods; NULL: computed on the device
  *                from ax..az and mask), see omni3d_curl
  *   mask         mask column of the input file (NULL: all ones); used only when curl is NULL
  *   p_init       initial pressure (NULL: zero), e.g. omni3d_bernoulli_face()

@@ -362,3 +362,40 @@ def load_reference_directions(level_file: str) -> np.ndarray | None:
         return None
     rows = open(path).read().replace("\r", "").strip().split("\n")
     return np.array([[float(x) for x in r.split()] for r in rows[:-1]], np.float32)
+
+
+def icosphere(level: int) -> np.ndarray:
+    """Direction vertices of the shipped GridIcosahedronDivide<level>.dat sets (12, 42, 162,
+    642, ... vertices), restated in numpy for the CPU arms: recursive midpoint subdivision of
+    the icosahedron with poles at +-z, the lower ring at z = -1/sqrt(5) and the upper ring,
+    rotated by pi/5, at z = 0.46000602 (the shipped files' value), printed with six decimals
+    and read back as the reference reads its direction file, sorted lexicographically."""
+    zl, rl = -1.0 / np.sqrt(5.0), 2.0 / np.sqrt(5.0)
+    zu = 0.46000602
+    ru = np.sqrt(1.0 - zu * zu)
+    verts = [(0.0, 0.0, 1.0), (0.0, 0.0, -1.0)]
+    verts += [(rl * np.cos(2 * np.pi * k / 5), rl * np.sin(2 * np.pi * k / 5), zl) for k in range(5)]
+    verts += [(ru * np.cos(2 * np.pi * k / 5 + np.pi / 5), ru * np.sin(2 * np.pi * k / 5 + np.pi / 5), zu)
+              for k in range(5)]
+    faces = []
+    for k in range(5):
+        a, b, ua, ub = 2 + k, 2 + (k + 1) % 5, 7 + k, 7 + (k + 1) % 5
+        faces += [(1, b, a), (0, ua, ub), (a, b, ua), (b, ub, ua)]
+    for _ in range(1, level):
+        mid = {}
+
+        def midpoint(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in mid:
+                m = np.add(verts[a], verts[b])
+                verts.append(tuple(m / np.sqrt(float(np.dot(m, m)))))
+                mid[key] = len(verts) - 1
+            return mid[key]
+
+        nxt = []
+        for t in faces:
+            ab, bc, ca = midpoint(t[0], t[1]), midpoint(t[1], t[2]), midpoint(t[2], t[0])
+            nxt += [(t[0], ab, ca), (t[1], bc, ab), (t[2], ca, bc), (ab, bc, ca)]
+        faces = nxt
+    rows = sorted(tuple(float(s) for s in ("%f %f %f" % v).split()) for v in verts)
+    return np.array(rows, np.float32)

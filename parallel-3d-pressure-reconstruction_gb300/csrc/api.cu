@@ -164,7 +164,10 @@ int check_params(const omni3d_params *p, std::string *why)
     if (!(p->line_spacing > 0.0f) || !std::isfinite(p->line_spacing)) { *why = "line_spacing must be > 0"; return OMNI3D_ERR_ARG; }
     if (p->n_dirs <= 0 || !p->dirs) { *why = "no directions"; return OMNI3D_ERR_ARG; }
     if (p->max_iter < 0) { *why = "max_iter must be >= 0"; return OMNI3D_ERR_ARG; }
-    if (p->method != OMNI3D_METHOD_PLAIN && p->method != OMNI3D_METHOD_SELECT) { *why = "unknown method"; return OMNI3D_ERR_ARG; }
+    if (p->method != OMNI3D_METHOD_PLAIN && p->method != OMNI3D_METHOD_SELECT && p->method != OMNI3D_METHOD_WEIGHTED) {
+        *why = "unknown method";
+        return OMNI3D_ERR_ARG;
+    }
     if (p->solver != OMNI3D_SOLVER_ANCHOR && p->solver != OMNI3D_SOLVER_SWEEP) { *why = "unknown solver"; return OMNI3D_ERR_ARG; }
     if (p->grad_storage != OMNI3D_GRAD_F32 && p->grad_storage != OMNI3D_GRAD_BF16) { *why = "unknown grad_storage"; return OMNI3D_ERR_ARG; }
     if (p->gauge < OMNI3D_GAUGE_NONE || p->gauge > OMNI3D_GAUGE_MEAN) { *why = "unknown gauge"; return OMNI3D_ERR_ARG; }
@@ -209,9 +212,8 @@ int prepare_field(omni3d_ctx *ctx, const float *ax, const float *ay, const float
     if ((rc = stage(ctx, ax, dev, ctx->in_ax, V, &dax))) return rc;
     if ((rc = stage(ctx, ay, dev, ctx->in_ay, V, &day))) return rc;
     if ((rc = stage(ctx, az, dev, ctx->in_az, V, &daz))) return rc;
-    const bool select = ctx->prm.method == OMNI3D_METHOD_SELECT;
     const float *dcurl = nullptr;
-    if (select) {
+    if (method_uses_curl(ctx->prm.method)) {
         if (curl) {
             if ((rc = stage(ctx, curl, dev, ctx->in_aux, V, &daux))) return rc;
             dcurl = daux;
@@ -535,7 +537,8 @@ int omni3d_sweep(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
                  float *pn, float *count, int device_ptrs)
 {
     if (!ctx || !ax || !ay || !az || !p || !pn || !count) return fail(ctx, OMNI3D_ERR_ARG, "NULL argument");
-    if (ctx->prm.method == OMNI3D_METHOD_SELECT && !curl) return fail(ctx, OMNI3D_ERR_ARG, "select method needs curl");
+    if (method_uses_curl(ctx->prm.method) && !curl)
+        return fail(ctx, OMNI3D_ERR_ARG, "the selected and weighted methods need curl");
     cudaSetDevice(ctx->prm.device);
     const long long V = ctx->geo.grid.V;
     const bool dev = device_ptrs != 0;

@@ -7,7 +7,7 @@
 // separators in the parameter file are accepted.  Defaults follow the reference main(): the
 // selected method, exactly NoItr iterations, no gauge.
 //
-// Options: --params PATH  --method select|plain  --solver anchor|sweep  --tol T
+// Options: --params PATH  --method select|plain|weighted  --solver anchor|sweep  --tol T
 //          --gauge none|point|mean  --ref I,J,K  --grad f32|bf16  --device N
 #include <dirent.h>
 #include <sys/stat.h>
@@ -59,7 +59,7 @@ void list_files(const std::string &dir, std::vector<std::string> &out)
 int usage()
 {
     std::fprintf(stderr,
-                 "usage: omni3d [--params PATH] [--method select|plain] [--solver anchor|sweep] [--tol T]\n"
+                 "usage: omni3d [--params PATH] [--method select|plain|weighted] [--solver anchor|sweep] [--tol T]\n"
                  "              [--gauge none|point|mean] [--ref I,J,K] [--grad f32|bf16] [--device N]\n");
     return 2;
 }
@@ -79,7 +79,13 @@ int main(int argc, char **argv)
             return argv[++a];
         };
         if (k == "--params") params_path = val();
-        else if (k == "--method") { std::string v = val(); prm.method = v == "plain" ? OMNI3D_METHOD_PLAIN : OMNI3D_METHOD_SELECT; }
+        else if (k == "--method") {
+            std::string v = val();
+            if (v == "plain") prm.method = OMNI3D_METHOD_PLAIN;
+            else if (v == "select") prm.method = OMNI3D_METHOD_SELECT;
+            else if (v == "weighted") prm.method = OMNI3D_METHOD_WEIGHTED;
+            else return usage();
+        }
         else if (k == "--solver") { std::string v = val(); prm.solver = v == "sweep" ? OMNI3D_SOLVER_SWEEP : OMNI3D_SOLVER_ANCHOR; }
         else if (k == "--tol") prm.tol = std::atof(val().c_str());
         else if (k == "--gauge") {

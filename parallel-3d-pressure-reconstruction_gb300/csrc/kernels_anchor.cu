@@ -2,8 +2,10 @@
 //
 // In one iteration of the reference (K:8840-8861) a voxel v receives, from every line
 // segment through it, w * (p[start] + I(v)) in pn and w in count (w = 1 for the plain
-// method; the start is the line entry, K:1760-1761; for the selected method the start is
-// the voxel where the segment began or restarted, K:2301-2411, and w = n / sum(curl/1e4)).
+// method; the start is the line entry, K:1760-1761; for the weighted method the start is
+// the entry and w = n / sum(curl/1e4) along the line, K:2086-2130; for the selected method
+// the start is the voxel where the segment began or restarted, K:2301-2411, and
+// w = n / sum(curl/1e4) along the segment).
 // I(v) and w depend only on the gradient field, so
 //     p_new(v) = (b(v) + sum_j w_j p_old(start_j)) / c(v),  b = sum w I,  c = sum w.
 // Only the start voxels ("anchors") are ever read, so the iteration closes on the anchors:
@@ -149,6 +151,42 @@ __global__ void __launch_bounds__(256, 6) k_anchor_plain(Grid g, const LineRec *
                 gl = gv;
             }
             emit<PASS>(S, L.v, e, 1.0f, I);
+        }
+    }
+}
+
+// Weighted method: the walk of k_sweep_weighted (K:1993-2135); anchors are the entries
+// (the marking pass is the plain method's), the entry itself receives nothing.
+template <int PASS, bool BF16>
+__global__ void __launch_bounds__(256, 6) k_anchor_weighted(Grid g, const LineRec *__restrict__ lines,
+                                                         const uint32_t *__restrict__ gbase,
+                                                         const uint32_t *__restrict__ desc, long long n_lines,
+                                                         const float4 *__restrict__ f32,
+                                                         const uint2 *__restrict__ b16,
+                                                         const float *__restrict__ curl, Sink S)
+{
+    static_assert(PASS == kFill, "the weighted operator has only a filling pass");
+    long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= n_lines) return;
+    LineRec r = lines[li];
+    Walk L;
+    L.init(g, r, gbase, desc, li);
+    const long long e = r.e;
+    float4 gl = load_grad<BF16>(f32, b16, e);
+    float I = 0.0f, comp = 0.0f, csum = 0.0f, nseg = 0.0f;
+    for (int s0 = 0; s0 < L.m; s0 += 16) {
+        uint32_t w = __ldg(L.dp + 32 * (s0 >> 4));
+        int n = min(16, L.m - s0);
+        for (int t = 0; t < n; t++, w >>= 2) {
+            int a = (int)(w & 3u);
+            L.v += a == 0 ? L.d0 : (a == 1 ? L.d1 : L.d2);
+            float4 gv = load_grad<BF16>(f32, b16, L.v);
+            float cn = BF16 ? __ldg(curl + L.v) : gv.w;
+            kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
+            csum += __fdiv_rn(cn, 1.0e4f);  // the weights as in k_sweep_weighted
+            nseg += 1.0f;
+            if (csum != 0.0f) emit<PASS>(S, L.v, e, __frcp_rn(csum) * nseg, I);
+            gl = gv;
         }
     }
 }
@@ -431,11 +469,21 @@ cudaError_t run_pass(const Geometry &geo, const Field &f, int method, bool bf16,
     else ok = ok && S.bits && S.id && S.b;
     if (PASS == kFill) ok = ok && S.rowptr && S.cursor && S.col && S.w && S.c;
     if (need_field) ok = ok && (bf16 ? f.bf16 != nullptr : f.f32 != nullptr);
-    if (method == OMNI3D_METHOD_SELECT) ok = ok && f.curl && (bf16 || f.f32);
+    if (method == OMNI3D_METHOD_SELECT || (method == OMNI3D_METHOD_WEIGHTED && PASS == kFill))
+        ok = ok && f.curl && (bf16 || f.f32);
+    if (method == OMNI3D_METHOD_WEIGHTED && PASS == kRhs) ok = false;  // no cached weighted operator
     if (!ok) return cudaErrorInvalidValue;
     unsigned blocks = (unsigned)((geo.n_lines + 255) / 256);
     const Grid &g = geo.grid;
-    if (method == OMNI3D_METHOD_SELECT) {
+    if (method == OMNI3D_METHOD_WEIGHTED && PASS == kFill) {
+        if (bf16)
+            k_anchor_weighted<kFill, true><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
+                                                                   geo.n_lines, f.f32, f.bf16, f.curl, S);
+        else
+            k_anchor_weighted<kFill, false><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
+                                                                    geo.n_lines, f.f32, f.bf16, f.curl, S);
+        OM_COUNT_LAUNCH();
+    } else if (method == OMNI3D_METHOD_SELECT) {
         if (bf16)
             k_anchor_select<PASS, true><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
                                                                 f.f32, f.bf16, f.curl, S);
@@ -443,7 +491,7 @@ cudaError_t run_pass(const Geometry &geo, const Field &f, int method, bool bf16,
             k_anchor_select<PASS, false><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
                                                                  f.f32, f.bf16, f.curl, S);
         OM_COUNT_LAUNCH();
-    } else {
+    } else {  // plain method, and the weighted method's marking pass (anchors = entries)
         if (bf16)
             k_anchor_plain<PASS, true><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
                                                                f.f32, f.bf16, S);

@@ -1,5 +1,6 @@
 // Omni sweep over the traced lines: the accumulation half of bodyIntegralInner
-// (K:1743-1863) and bodyIntegralInnerSelect (K:2280-2537), the normalisation
+// (K:1743-1863), bodyIntegralInnerWeighted (K:1993-2135) and bodyIntegralInnerSelect
+// (K:2280-2537), the normalisation
 // devidecountInner (K:6746-6759), the curl indicator (K:8352-8378) and the gauge.
 //
 // One thread walks one line by decoding its 2-bit staircase; a warp holds 32 neighbouring
@@ -100,6 +101,48 @@ __global__ void __launch_bounds__(256, 6) k_sweep_plain(Grid g, const LineRec *_
             float term = sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z));
             kahan_add(I, comp, term);
             atomicAdd(pncnt + L.v, make_float2(pe + I, 1.0f));
+            gl = gv;
+        }
+    }
+}
+
+// Weighted method (K:1993-2135): the entry receives nothing; step s of the line (s = 1..m)
+// adds w_s (p[entry] + I_s) and w_s, w_s = s / sum_{t<=s} curl_t/1e4, once that sum is
+// nonzero.  Each curl/1e4 term is the reference's correctly rounded float division, so the
+// "sum != 0" decision (all curls so far zero) is the reference's.
+template <bool BF16>
+__global__ void __launch_bounds__(256, 6) k_sweep_weighted(Grid g, const LineRec *__restrict__ lines,
+                                                        const uint32_t *__restrict__ gbase,
+                                                        const uint32_t *__restrict__ desc, long long n_lines,
+                                                        const float4 *__restrict__ f32,
+                                                        const uint2 *__restrict__ b16,
+                                                        const float *__restrict__ curl,
+                                                        const float *__restrict__ p, float2 *pncnt)
+{
+    long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= n_lines) return;
+    LineRec r = lines[li];
+    LineWalk L;
+    L.init(g, r, gbase, desc, li);
+    const float pe = __ldg(p + r.e);
+    float4 gl = load_grad<BF16>(f32, b16, L.v);
+    float I = 0.0f, comp = 0.0f, csum = 0.0f, nseg = 0.0f;
+    for (int s0 = 0; s0 < L.m; s0 += 16) {
+        uint32_t w = __ldg(L.dp + 32 * (s0 >> 4));
+        int n = min(16, L.m - s0);
+        for (int t = 0; t < n; t++, w >>= 2) {
+            int a = (int)(w & 3u);
+            L.v += a == 0 ? L.d0 : (a == 1 ? L.d1 : L.d2);
+            float4 gv = load_grad<BF16>(f32, b16, L.v);
+            float cn = BF16 ? __ldg(curl + L.v) : gv.w;
+            float term = sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z));
+            kahan_add(I, comp, term);
+            csum += __fdiv_rn(cn, 1.0e4f);
+            nseg += 1.0f;
+            if (csum != 0.0f) {
+                float wc = __frcp_rn(csum) * nseg;
+                atomicAdd(pncnt + L.v, make_float2((pe + I) * wc, wc));
+            }
             gl = gv;
         }
     }
@@ -306,10 +349,18 @@ cudaError_t sweep_full(const Geometry &geo, const Field &f, int method, bool bf1
     if (geo.n_lines == 0) return cudaSuccess;
     // every pointer the kernels dereference must be set: refuse to launch otherwise
     if (!geo.d_lines || !geo.d_gbase || !geo.d_desc || !p || !pncnt || (bf16 ? !f.bf16 : !f.f32) ||
-        (method == OMNI3D_METHOD_SELECT && !f.curl))
+        (method_uses_curl(method) && !f.curl))
         return cudaErrorInvalidValue;
     unsigned blocks = (unsigned)((geo.n_lines + 255) / 256);
-    if (method == OMNI3D_METHOD_SELECT) {
+    if (method == OMNI3D_METHOD_WEIGHTED) {
+        if (bf16)
+            k_sweep_weighted<true><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
+                                                           geo.n_lines, f.f32, f.bf16, f.curl, p, pncnt);
+        else
+            k_sweep_weighted<false><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
+                                                            geo.n_lines, f.f32, f.bf16, f.curl, p, pncnt);
+        OM_COUNT_LAUNCH();
+    } else if (method == OMNI3D_METHOD_SELECT) {
         if (bf16)
             k_sweep_select<true><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
                                                          f.f32, f.bf16, f.curl, p, pncnt);

@@ -75,7 +75,8 @@ extern "C" int omni3d_sweep_noalloc(omni3d_ctx *ctx, const float *ax, const floa
     if (!ctx || !ax || !ay || !az || !p || !pn || !count) return fail(OMNI3D_ERR_ARG, "NULL argument");
     const omni3d_params *P = context_params(ctx);
     const Geometry *geo = context_geometry(ctx);
-    if (P->method == OMNI3D_METHOD_SELECT && !curl) return fail(OMNI3D_ERR_ARG, "the selected method needs curl");
+    if (method_uses_curl(P->method) && !curl)
+        return fail(OMNI3D_ERR_ARG, "the selected and weighted methods need curl");
     if (P->grad_storage != OMNI3D_GRAD_F32)
         return fail(OMNI3D_ERR_STATE, "omni3d_sweep_noalloc supports FP32 gradient storage only");
     if (geo->grid.V > kMaxVoxels)

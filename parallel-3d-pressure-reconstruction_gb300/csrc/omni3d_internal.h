@@ -96,6 +96,12 @@ cudaError_t curl_field(const Grid &g, const float *ax, const float *ay, const fl
                        const float *mask, float *out, cudaStream_t st);
 
 // One full sweep: pncnt[v] += (sum of contributions, sum of weights) over all lines.
+// The selected and weighted methods read the curl indicator; the plain method does not.
+inline bool method_uses_curl(int method)
+{
+    return method == OMNI3D_METHOD_SELECT || method == OMNI3D_METHOD_WEIGHTED;
+}
+
 // method: OMNI3D_METHOD_*; p is read at line entries / segment starts.
 cudaError_t sweep_full(const Geometry &geo, const Field &f, int method, bool bf16,
                        const float *p, float2 *pncnt, cudaStream_t st);

@@ -18,7 +18,7 @@ ERR_STATE = -5
 ERR_RANGE = -6
 ERR_NUMERIC = -7
 
-METHOD_PLAIN, METHOD_SELECT = 0, 1
+METHOD_PLAIN, METHOD_SELECT, METHOD_WEIGHTED = 0, 1, 2
 SOLVER_ANCHOR, SOLVER_SWEEP = 0, 1
 GRAD_F32, GRAD_BF16 = 0, 1
 GAUGE_NONE, GAUGE_POINT, GAUGE_MEAN = 0, 1, 2

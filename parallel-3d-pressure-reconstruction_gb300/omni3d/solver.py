@@ -14,7 +14,7 @@ import numpy as np
 from . import _lib as L
 from ._lib import check, lib
 
-_METHODS = {"plain": L.METHOD_PLAIN, "select": L.METHOD_SELECT}
+_METHODS = {"plain": L.METHOD_PLAIN, "select": L.METHOD_SELECT, "weighted": L.METHOD_WEIGHTED}
 _SOLVERS = {"anchor": L.SOLVER_ANCHOR, "sweep": L.SOLVER_SWEEP}
 _GRADS = {"f32": L.GRAD_F32, "bf16": L.GRAD_BF16}
 _GAUGES = {"none": L.GAUGE_NONE, "point": L.GAUGE_POINT, "mean": L.GAUGE_MEAN}

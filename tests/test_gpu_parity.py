@@ -132,6 +132,71 @@ def test_select_solve_matches_oracle(omni, orc, solver):
     assert synthetic.relative_l2(r.p, ep, gauge="none") < TOL_P_SELECT
 
 
+def test_weighted_sweep_matches_oracle(omni, orc):
+    """One weighted sweep (K:1993-2135): the entry receives nothing, a step's weight is
+    n / sum(curl/1e4) once that sum is nonzero; voxels inside the masked sphere have curl 0."""
+    dims = (18, 15, 12)
+    f = _field(dims, seed=21, sphere=3.5)
+    dirs = omni.icosphere(3)
+    p = _pinit(dims, seed=3)
+    curl = orc.curl(dims, f["spacing"], f["ax"], f["ay"], f["az"], f["mask"])
+    with omni.Omni3D(dims, f["spacing"], dirs, max_iter=1, method="weighted") as s:
+        pn, cnt = s.sweep(f["ax"], f["ay"], f["az"], p, curl=curl)
+    epn, ecnt = orc.sweep(dims, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p, mode=2, curl=curl, precision="f64")
+    _, fcnt = orc.sweep(dims, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p, mode=2, curl=curl)
+    np.testing.assert_array_equal(cnt.reshape(-1) > 0, fcnt > 0)  # which voxels receive: exact
+    assert synthetic.relative_l2(cnt, ecnt, gauge="none") < TOL_PN
+    assert synthetic.relative_l2(pn, epn, gauge="none") < TOL_PN
+
+
+@pytest.mark.parametrize("solver", ["sweep", "anchor"])
+@pytest.mark.parametrize("niter", [1, 4])
+def test_weighted_solve_matches_oracle(omni, orc, solver, niter):
+    dims = (20, 17, 15)
+    f = _field(dims, seed=22, noise=0.1, sphere=4.0)
+    dirs = omni.icosphere(3)
+    p0 = _pinit(dims, seed=4)
+    curl = orc.curl(dims, f["spacing"], f["ax"], f["ay"], f["az"], f["mask"])
+    with omni.Omni3D(dims, f["spacing"], dirs, max_iter=niter, solver=solver, method="weighted") as s:
+        r = s.solve(f["ax"], f["ay"], f["az"], mask=f["mask"], p_init=p0)  # curl computed on the device
+    assert r.stats["solver_used"] == (0 if solver == "anchor" else 1)
+    ep, ecnt = orc.solve(dims, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p0, niter, mode=2, curl=curl,
+                         precision="f64")
+    fp, fcnt = orc.solve(dims, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p0, niter, mode=2, curl=curl)
+    np.testing.assert_array_equal(r.count.reshape(-1) > 0, fcnt > 0)
+    assert synthetic.relative_l2(r.count, ecnt, gauge="none") < 1e-5
+    assert synthetic.relative_l2(r.p, ep, gauge="none") < TOL_P_SELECT
+    assert synthetic.relative_l2(r.p, fp, gauge="none") < TOL_P_SELECT
+
+
+def test_weighted_tolerance_bf16_and_zero_curl(omni, orc):
+    """Weighted method: the tolerance stop agrees between the solvers, BF16 storage stays
+    close to FP32, and a zero-curl field gives no contribution at all."""
+    dims = (16, 16, 16)
+    f = _field(dims, seed=23, sphere=4.0)
+    dirs = omni.icosphere(3)
+    curl = orc.curl(dims, f["spacing"], f["ax"], f["ay"], f["az"], f["mask"])
+    its = []
+    for solver in ("sweep", "anchor"):
+        with omni.Omni3D(dims, f["spacing"], dirs, max_iter=200, tol=1e-4, gauge="point", solver=solver,
+                         method="weighted") as s:
+            r = s.solve(f["ax"], f["ay"], f["az"], curl=curl)
+            its.append(r.stats["iterations"])
+            assert r.stats["rel_change"] < 1e-4
+    assert abs(its[0] - its[1]) <= 1
+    out = {}
+    for g in ("f32", "bf16"):
+        with omni.Omni3D(dims, f["spacing"], dirs, max_iter=4, grad=g, method="weighted") as s:
+            out[g] = s.solve(f["ax"], f["ay"], f["az"], curl=curl)
+    assert synthetic.relative_l2(out["bf16"].count, out["f32"].count, gauge="none") < 1e-6
+    assert 0 < synthetic.relative_l2(out["bf16"].p, out["f32"].p) < 1e-2
+    with omni.Omni3D(dims, f["spacing"], dirs, max_iter=2, method="weighted") as s:
+        p0 = _pinit(dims)
+        r = s.solve(f["ax"], f["ay"], f["az"], curl=np.zeros_like(curl), p_init=p0)
+    assert (r.count == 0).all()
+    np.testing.assert_array_equal(r.p.reshape(-1), p0.reshape(-1))
+
+
 def test_select_without_threshold_splits_at_mask(omni, orc):
     """Config-3 form: threshold above every curl, so only the masked voxels are excluded."""
     dims = (18, 18, 18)

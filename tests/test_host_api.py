@@ -50,6 +50,15 @@ def test_icosphere_matches_reference_vertex_sets(omni):
         assert set(map(tuple, mine.tolist())) == set(map(tuple, ref.tolist()))
 
 
+def test_oracle_icosphere_equals_library(omni):
+    """The CPU arms take their directions from the oracle's numpy icosphere, never from the
+    library: the two must give the same arrays."""
+    import oracle
+
+    for level in (1, 2, 3, 4, 5):
+        np.testing.assert_array_equal(oracle.icosphere(level), omni.icosphere(level))
+
+
 def test_icosphere_is_stable(omni):
     h = {lv: hashlib.sha256(omni.icosphere(lv).tobytes()).hexdigest() for lv in (3, 4)}
     golden = os.path.join(REPO, "tests", "golden", "icosphere_sha256.txt")
