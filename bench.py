@@ -279,6 +279,7 @@ def main():
     ap.add_argument("--iters", type=int, default=0, help="iterations per solve (0: calibrate)")
     ap.add_argument("--grad", default="f32", choices=["f32", "bf16"])
     ap.add_argument("--solver", default="anchor", choices=["anchor", "sweep"])
+    ap.add_argument("--engine", default="auto", choices=["auto", "lines", "bricks"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="only the warm-up and timed solves (for ncu): no calibration, e2e, variants or CPU arm")
@@ -313,16 +314,15 @@ def main():
     dirs = omni3d.icosphere(args.level)
     dev = torch.device("cuda", local)
 
-    def make(iters, tol=0.0):
-        return omni3d.Omni3D(dims, f["spacing"], dirs, max_iter=iters, method="select", threshold=FLT_MAX,
-                             solver=args.solver, grad=args.grad, tol=tol, gauge="mean", device=local)
+    def make(iters, tol=0.0, **kw):
+        opts = dict(solver=args.solver, grad=args.grad, engine=args.engine)
+        opts.update(kw)
+        return omni3d.Omni3D(dims, f["spacing"], dirs, max_iter=iters, method="select", threshold=FLT_MAX, tol=tol,
+                             gauge="mean", device=local, **opts)
 
     # device inputs
     d_in = [torch.from_numpy(f[k].reshape(-1)).to(dev) for k in ("ax", "ay", "az", "mask")]
-    solver = make(args.iters)
-    stream = torch.cuda.Stream(device=dev)
-    solver.set_stream(stream.cuda_stream)
-    geo = solver.geometry_info()
+    # contexts are created one at a time (a brick-engine context at 256^3 holds about 110 GB)
     calib = {}
     if not args.profile:
         # converged solution (gauged relative change < 1e-7) and the error after k iterations
@@ -339,7 +339,8 @@ def main():
             errs[k] = synthetic.relative_l2(rk.p.cpu().numpy(), p_conv, gauge="mean", weights=sel)
             if k > args.iters and errs[k] < 1e-4:
                 break
-        r = solver.solve(*d_in[:3], mask=d_in[3])
+        with make(args.iters) as s:
+            r = s.solve(*d_in[:3], mask=d_in[3])
         err_conv = synthetic.relative_l2(r.p.cpu().numpy(), p_conv, gauge="mean", weights=sel)
         err_true = synthetic.relative_l2(r.p.cpu().numpy(), f["p_true"], gauge="mean",
                                          weights=(sel & (f["mask"].reshape(-1) > 0)))
@@ -350,6 +351,10 @@ def main():
                  "calibration_s": time.time() - t0,
                  "converged_reference": "this FP32 solver run to a gauged relative change < 1e-7"}
 
+    solver = make(args.iters)
+    stream = torch.cuda.Stream(device=dev)
+    solver.set_stream(stream.cuda_stream)
+    geo = solver.geometry_info()
     # fresh input buffers rewritten each step (defeats L2 reuse across steps)
     src = [t.clone() for t in d_in]
 
@@ -395,18 +400,22 @@ def main():
             if it >= max(1, args.warmup):
                 e2e_times.append(t1 - t0)
         t_e2e = float(np.mean(e2e_times))
+    engine_used = stats["engine_used"]
+    solver.close()
     variants = {}
     if not args.profile and not args.no_variants:
-        # the direct GPU counterpart of the reference loop (K full sweeps) and BF16 storage
-        for name, kw in (("sweep_solver_f32", dict(solver="sweep")), ("anchor_solver_bf16", dict(grad="bf16"))):
-            with omni3d.Omni3D(dims, f["spacing"], dirs, max_iter=args.iters, method="select", threshold=FLT_MAX,
-                               gauge="mean", device=local, **{"solver": args.solver, "grad": args.grad, **kw}) as s:
+        # the direct GPU counterpart of the reference loop (K full sweeps), BF16 storage and
+        # the line engine
+        for name, kw in (("sweep_solver_f32", dict(solver="sweep")), ("anchor_solver_bf16", dict(grad="bf16")),
+                         ("line_engine_f32", dict(engine="lines"))):
+            with make(args.iters, **kw) as s:
                 s.solve(*d_in[:3], mask=d_in[3])
                 torch.cuda.synchronize()
                 tt0 = time.perf_counter()
                 rv = s.solve(*d_in[:3], mask=d_in[3])
                 torch.cuda.synchronize()
-                variants[name] = {"seconds": time.perf_counter() - tt0, "device_ms": rv.stats["ms_total"]}
+                variants[name] = {"seconds": time.perf_counter() - tt0, "device_ms": rv.stats["ms_total"],
+                                  "engine_used": ["auto", "lines", "bricks"][rv.stats["engine_used"]]}
                 if calib:
                     variants[name]["rel_l2_vs_converged"] = synthetic.relative_l2(
                         rv.p.cpu().numpy(), p_conv, gauge="mean", weights=sel)
@@ -438,6 +447,7 @@ def main():
         "breakdown_ms": {k: stats[k] for k in ("ms_setup", "ms_iterate", "ms_final", "ms_sweep", "ms_total")},
         "geometry_ms": stats["ms_geometry"], "n_anchors": stats["n_anchors"], "n_links": stats["n_links"],
     }
+    line["config"]["engine"] = ["auto", "lines", "bricks"][engine_used]
     line["clocks"] = clk.summary()
     if rank == 0 and not args.no_cpu and not args.profile:
         try:
@@ -450,7 +460,6 @@ def main():
             line["cpu_baseline"] = {"value": None, "unavailable": str(e)}
     if rank == 0:
         print(json.dumps(line))
-    solver.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0

@@ -53,6 +53,14 @@ extern "C" {
 #define OMNI3D_GRAD_F32 0
 #define OMNI3D_GRAD_BF16 1
 
+/* Sweep engine.  Both give the same contributions; they differ in how the volume is read. */
+#define OMNI3D_ENGINE_AUTO 0    /* the faster engine for the solve: lines (measured on GB300
+                                   at 256^3 / 642 directions: lines 97 ms per sweep, bricks
+                                   145 ms + 95 ms of per-field passes) */
+#define OMNI3D_ENGINE_LINES 1   /* one thread per line, gathers and reductions through L2 */
+#define OMNI3D_ENGINE_BRICKS 2  /* lines cut into 16^3-brick segments; each brick's field is
+                                   staged in shared memory by TMA and its sums kept there */
+
 /* Gauge applied to the output (the reference applies none; K:8879-8915 is commented out). */
 #define OMNI3D_GAUGE_NONE 0
 #define OMNI3D_GAUGE_POINT 1    /* p -= p(ref voxel) */
@@ -84,6 +92,7 @@ typedef struct {
     long long anchor_max_links;/* anchor operator entries allowed before the solve falls back
                                   to the sweep form (0: what 80 % of the free device memory
                                   holds) */
+    int engine;                /* OMNI3D_ENGINE_* */
 } omni3d_params;
 
 typedef struct {
@@ -103,6 +112,7 @@ typedef struct {
     long long kernel_launches; /* CUDA kernels this library launched during the call */
     int solver_used;           /* OMNI3D_SOLVER_*: the anchor solver falls back to the sweep
                                   solver when its operator would exceed anchor_max_links */
+    int engine_used;           /* OMNI3D_ENGINE_LINES or OMNI3D_ENGINE_BRICKS */
 } omni3d_stats;
 
 /* Fill *p with the reference's defaults (K:8512-8535) and this implementation's. */

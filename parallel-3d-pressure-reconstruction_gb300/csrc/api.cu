@@ -65,6 +65,9 @@ struct omni3d_ctx {
     DeviceBuf pvol_a, pvol_b, pout, cnt, pncnt, scratch, flags;
     Anchor anc;
     bool anc_cached = false;  // plain method: operator structure built for this geometry
+    Bricks bricks;            // brick segments of the geometry (built on first use)
+    bool bricks_failed = false;
+    std::string bricks_why;
     AdjointBuffers adj;
     DeviceBuf adj_g, adj_out;  // staging of the adjoint's host arguments
     int last_iterations = -1;  // iterations of the last solve (-1: no solve yet)
@@ -178,6 +181,7 @@ int check_params(const omni3d_params *p, std::string *why)
     }
     if (!(p->tol >= 0.0)) { *why = "tol must be >= 0"; return OMNI3D_ERR_ARG; }
     if (p->anchor_max_links < 0) { *why = "anchor_max_links must be >= 0"; return OMNI3D_ERR_ARG; }
+    if (p->engine < OMNI3D_ENGINE_AUTO || p->engine > OMNI3D_ENGINE_BRICKS) { *why = "unknown engine"; return OMNI3D_ERR_ARG; }
     double ng = std::max(std::max(p->nx, p->ny), p->nz) * 1.732 / (double)p->line_spacing;
     if (ng * ng * (double)p->n_dirs / 256.0 > 2.0e9) { *why = "too many lines (lattice x directions)"; return OMNI3D_ERR_RANGE; }
     return OMNI3D_OK;
@@ -233,6 +237,68 @@ int prepare_field(omni3d_ctx *ctx, const float *ax, const float *ay, const float
     }
     F->curl = const_cast<float *>(dcurl);
     CK(ctx, pack_field(g, dax, day, daz, dcurl, F, bf16, ctx->st));
+    return OMNI3D_OK;
+}
+
+// The sweep engine of a solve on ctx: bricks when asked for (FP32 storage, the segments
+// built), else lines; automatic selection takes lines, the faster engine as measured.
+// *rc is set when bricks were required but are unavailable.
+int choose_engine(omni3d_ctx *ctx, bool bf16, int *rc)
+{
+    const int want = ctx->prm.engine;
+    *rc = OMNI3D_OK;
+    if (want == OMNI3D_ENGINE_LINES || want == OMNI3D_ENGINE_AUTO) return OMNI3D_ENGINE_LINES;
+    if (bf16) {
+        if (want == OMNI3D_ENGINE_BRICKS)
+            *rc = fail(ctx, OMNI3D_ERR_STATE, "the brick engine needs FP32 gradient storage");
+        return OMNI3D_ENGINE_LINES;
+    }
+    if (!ctx->bricks.built && !ctx->bricks_failed) {
+        std::string why;
+        cudaError_t e = build_bricks(ctx->geo, &ctx->bricks, ctx->st, &why);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            free_bricks(&ctx->bricks);
+            ctx->bricks_failed = true;
+            ctx->bricks_why = why;
+        }
+    }
+    if (ctx->bricks.built) return OMNI3D_ENGINE_BRICKS;
+    if (want == OMNI3D_ENGINE_BRICKS) *rc = fail(ctx, OMNI3D_ERR_STATE, "brick engine unavailable: " + ctx->bricks_why);
+    return OMNI3D_ENGINE_LINES;
+}
+
+// Per-field brick passes (B1 + L) when the engine is bricks.  Automatic selection falls back
+// to lines when the per-segment buffers do not fit in device memory.
+int engine_prepare(omni3d_ctx *ctx, int *engine, const Field &F, int method)
+{
+    if (*engine != OMNI3D_ENGINE_BRICKS) return OMNI3D_OK;
+    std::string why;
+    cudaError_t e = brick_prepare(ctx->geo, &ctx->bricks, F, method, ctx->st, &why);
+    if (e == cudaSuccess) return OMNI3D_OK;
+    cudaGetLastError();
+    if (e == cudaErrorMemoryAllocation && ctx->prm.engine == OMNI3D_ENGINE_AUTO) {
+        *engine = OMNI3D_ENGINE_LINES;
+        return OMNI3D_OK;
+    }
+    return fail(ctx, e == cudaErrorMemoryAllocation ? OMNI3D_ERR_NOMEM : OMNI3D_ERR_CUDA, "brick passes: " + why);
+}
+
+// One full sweep with the chosen engine.
+cudaError_t engine_sweep(omni3d_ctx *ctx, int engine, const Field &F, int method, bool bf16, const float *p,
+                         float2 *acc, cudaStream_t st)
+{
+    if (engine == OMNI3D_ENGINE_BRICKS) return brick_sweep(ctx->geo, &ctx->bricks, method, p, acc, st);
+    return sweep_full(ctx->geo, F, method, bf16, p, acc, st);
+}
+
+// The brick passes' error flag (a TMA wait that gave up) as a status.
+int engine_check(omni3d_ctx *ctx, int engine)
+{
+    if (engine != OMNI3D_ENGINE_BRICKS) return OMNI3D_OK;
+    int flag = 0;
+    CK(ctx, brick_error(ctx->bricks, &flag, ctx->st));
+    if (flag) return fail(ctx, OMNI3D_ERR_CUDA, "brick pass: a shared-memory staging copy did not complete");
     return OMNI3D_OK;
 }
 
@@ -415,6 +481,7 @@ int omni3d_destroy(omni3d_ctx *ctx)
     free_geometry(&ctx->geo);
     cudaFree(ctx->geo.d_dirs);
     anchor_free(&ctx->anc);
+    free_bricks(&ctx->bricks);
     adjoint_free(&ctx->adj);
     ctx->adj_g.release();
     ctx->adj_out.release();
@@ -549,8 +616,12 @@ int omni3d_sweep(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
     if ((rc = stage(ctx, p, dev, ctx->in_pinit, V, &dp))) return rc;
     CK(ctx, ctx->pncnt.ensure(sizeof(float2) * (size_t)V));
     float2 *acc = ctx->pncnt.as<float2>();
+    const bool bf16 = ctx->prm.grad_storage == OMNI3D_GRAD_BF16;
+    int engine = choose_engine(ctx, bf16, &rc);
+    if (rc) return rc;
+    if ((rc = engine_prepare(ctx, &engine, F, ctx->prm.method))) return rc;
     CK(ctx, init_accum(V, nullptr, false, acc, ctx->st));
-    CK(ctx, sweep_full(ctx->geo, F, ctx->prm.method, ctx->prm.grad_storage == OMNI3D_GRAD_BF16, dp, acc, ctx->st));
+    CK(ctx, engine_sweep(ctx, engine, F, ctx->prm.method, bf16, dp, acc, ctx->st));
     // add (pn, count) to the caller's arrays
     float *dpn = pn, *dcount = count;
     if (!dev) {
@@ -567,7 +638,7 @@ int omni3d_sweep(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
         CK(ctx, cudaMemcpyAsync(count, dcount, sizeof(float) * (size_t)V, cudaMemcpyDeviceToHost, ctx->st));
     }
     CK(ctx, cudaStreamSynchronize(ctx->st));
-    return OMNI3D_OK;
+    return engine_check(ctx, engine);
 }
 
 int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float *az, const float *curl,
@@ -589,6 +660,12 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
     Field F;
     int rc = prepare_field(ctx, ax, ay, az, curl, mask, dev, &F);
     if (rc) return rc;
+    int engine = OMNI3D_ENGINE_LINES;
+    if (P.max_iter > 0) {
+        engine = choose_engine(ctx, bf16, &rc);
+        if (rc) return rc;
+        if ((rc = engine_prepare(ctx, &engine, F, P.method))) return rc;
+    }
     // initial pressure (zero when not given)
     const float *dpinit;
     if (p_init) {
@@ -671,7 +748,7 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
         for (int it = 1; it <= K; it++) {
             CK(ctx, init_accum(V, dpinit, seed && it == 1, acc, st));
             cudaEventRecord(ctx->ev[5], st);
-            CK(ctx, sweep_full(ctx->geo, F, P.method, bf16, pc, acc, st));
+            CK(ctx, engine_sweep(ctx, engine, F, P.method, bf16, pc, acc, st));
             cudaEventRecord(ctx->ev[6], st);
             CK(ctx, normalize(V, acc, pc, pn, dcnt, st));
             done = it;
@@ -718,7 +795,7 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
         CK(ctx, anchor_scatter(A, pc, vol, st));
         CK(ctx, init_accum(V, dpinit, seed && its == 0, acc, st));
         cudaEventRecord(ctx->ev[5], st);
-        CK(ctx, sweep_full(ctx->geo, F, P.method, bf16, vol, acc, st));
+        CK(ctx, engine_sweep(ctx, engine, F, P.method, bf16, vol, acc, st));
         cudaEventRecord(ctx->ev[6], st);
         CK(ctx, normalize(V, acc, dpinit, dout, dcnt, st));
         done = its + 1;
@@ -735,6 +812,7 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
     cudaEventRecord(ctx->ev[4], st);
     CK(ctx, cudaStreamSynchronize(st));
     CK(ctx, cudaGetLastError());
+    if ((rc = engine_check(ctx, engine))) return rc;
     ctx->last_iterations = done;
     ctx->last_method = P.method;
     if (stats) {
@@ -753,6 +831,7 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
         stats->ms_sweep = ms_between(ctx->ev[5], ctx->ev[6]);
         stats->kernel_launches = (long long)(__atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED) - launches0);
         stats->solver_used = solver;
+        stats->engine_used = engine;
     }
     if (ctx->geo.walk_errors) return fail(ctx, OMNI3D_ERR_NUMERIC, "line walk hit the wrong-point branch");
     return OMNI3D_OK;
@@ -991,6 +1070,7 @@ int omni3d_batch_solve(omni3d_batch *b, const float *const *ax, const float *con
         stats->ms_total = ms;
         stats->kernel_launches = b->launches_per_graph;
         stats->solver_used = OMNI3D_SOLVER_ANCHOR;
+        stats->engine_used = OMNI3D_ENGINE_LINES;
         for (omni3d_ctx *c : b->ctx) {
             stats->n_lines += c->geo.n_lines;
             stats->n_units += c->geo.n_units;

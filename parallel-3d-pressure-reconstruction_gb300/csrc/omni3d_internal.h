@@ -81,12 +81,48 @@ cudaError_t exclusive_scan_u32(const uint32_t *in, uint32_t *out, long long n, u
 cudaError_t exclusive_scan_u64(const unsigned long long *in, unsigned long long *out,
                                long long n, unsigned long long *tmp, cudaStream_t st);
 
+// Brick-staged form of the geometry (kernels_brick.cu): every line cut at the boundaries of
+// 16^3 voxel bricks into segments, stored brick-major; plus the per-solve segment
+// summaries and carry-in states.
+struct Bricks {
+    bool built = false;
+    int nbx = 0, nby = 0, nbz = 0;
+    long long n_bricks = 0, n_segs = 0;
+    uint4 *rec = nullptr;            // 2 x uint4 per segment, grouped by brick
+    uint32_t *brick_off = nullptr;   // n_bricks + 1 segment offsets
+    uint32_t *line_seg = nullptr;    // n_lines + 1: line-major id of each line's first segment
+    uint4 *items = nullptr;          // work items (brick, first segment, end segment, 0)
+    uint32_t n_items = 0;
+    int grid = 0;                    // CTAs per brick pass (one per SM)
+    uint32_t *work = nullptr;        // [0] work counter, [1] error flag (a TMA wait gave up)
+    void *summ = nullptr;            // per-segment summaries of the prepared method
+    void *carry = nullptr;           // per-segment carry-in states
+    size_t summ_cap = 0, carry_cap = 0;
+    int prepared_method = -1;
+    const void *map_for = nullptr;   // field the tensor map describes
+    alignas(64) unsigned char map[128];  // CUtensorMap of the float4 field
+};
+
+// Cut the lines into brick segments (once per geometry); cudaErrorNotSupported when the
+// engine cannot be used (no tensor-map support, more than 2^32 segments).
+cudaError_t build_bricks(const Geometry &geo, Bricks *B, cudaStream_t st, std::string *err);
+void free_bricks(Bricks *B);
+
 // Gradient field on the device: float4 (ax, ay, az, curl) per voxel, or its bf16 copy.
 struct Field {
     float4 *f32 = nullptr;          // always present
     uint2 *bf16 = nullptr;          // (ax, ay, az, 0) as bf16 when grad_storage is BF16
     float *curl = nullptr;          // curl (select method), also in f32[v].w
 };
+
+// Brick passes B1 + L for the field f (FP32) and the method: per-segment carry-in states.
+cudaError_t brick_prepare(const Geometry &geo, Bricks *B, const Field &f, int method, cudaStream_t st,
+                          std::string *err);
+// Brick pass B2: one full sweep from p into pncnt, the same contributions as sweep_full.
+cudaError_t brick_sweep(const Geometry &geo, Bricks *B, int method, const float *p, float2 *pncnt,
+                        cudaStream_t st);
+// The error flag of the brick passes (1: a TMA wait gave up).  Synchronises st.
+cudaError_t brick_error(const Bricks &B, int *flag, cudaStream_t st);
 
 // Pack three component arrays (+ optional curl) into the interleaved field.
 cudaError_t pack_field(const Grid &g, const float *ax, const float *ay, const float *az,

@@ -19,6 +19,7 @@ ERR_RANGE = -6
 ERR_NUMERIC = -7
 
 METHOD_PLAIN, METHOD_SELECT, METHOD_WEIGHTED = 0, 1, 2
+ENGINE_AUTO, ENGINE_LINES, ENGINE_BRICKS = 0, 1, 2
 SOLVER_ANCHOR, SOLVER_SWEEP = 0, 1
 GRAD_F32, GRAD_BF16 = 0, 1
 GAUGE_NONE, GAUGE_POINT, GAUGE_MEAN = 0, 1, 2
@@ -36,14 +37,14 @@ class Params(C.Structure):
                 ("line_spacing", _f), ("n_dirs", _i), ("dirs", _fp), ("max_iter", _i), ("threshold", _f),
                 ("method", _i), ("solver", _i), ("grad_storage", _i), ("tol", _d), ("gauge", _i),
                 ("ref_i", _i), ("ref_j", _i), ("ref_k", _i), ("seed_first_iteration", _i), ("device", _i),
-                ("anchor_max_links", _ll)]
+                ("anchor_max_links", _ll), ("engine", _i)]
 
 
 class Stats(C.Structure):
     _fields_ = [("iterations", _i), ("rel_change", _d), ("n_lines", _ll), ("n_units", _ll), ("walk_errors", _ll),
                 ("n_anchors", _ll), ("n_links", _ll), ("ms_geometry", _d), ("ms_setup", _d), ("ms_iterate", _d),
                 ("ms_final", _d), ("ms_total", _d), ("ms_sweep", _d),
-                ("kernel_launches", _ll), ("solver_used", _i)]
+                ("kernel_launches", _ll), ("solver_used", _i), ("engine_used", _i)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -21,8 +21,8 @@ LIB = os.path.join(BUILD, "libomni3d_gb300.so")
 CLI = os.path.join(BUILD, "omni3d")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-LIB_SOURCES = ["kernels_trace.cu", "kernels_sweep.cu", "kernels_anchor.cu", "kernels_adjoint.cu", "api.cu", "host_io.cpp",
-               "noalloc.cu"]
+LIB_SOURCES = ["kernels_trace.cu", "kernels_sweep.cu", "kernels_anchor.cu", "kernels_adjoint.cu", "kernels_brick.cu",
+               "api.cu", "host_io.cpp", "noalloc.cu"]
 CLI_SOURCES = ["cli.cpp"]
 
 

@@ -16,6 +16,7 @@ from ._lib import check, lib
 
 _METHODS = {"plain": L.METHOD_PLAIN, "select": L.METHOD_SELECT, "weighted": L.METHOD_WEIGHTED}
 _SOLVERS = {"anchor": L.SOLVER_ANCHOR, "sweep": L.SOLVER_SWEEP}
+_ENGINES = {"auto": L.ENGINE_AUTO, "lines": L.ENGINE_LINES, "bricks": L.ENGINE_BRICKS}
 _GRADS = {"f32": L.GRAD_F32, "bf16": L.GRAD_BF16}
 _GAUGES = {"none": L.GAUGE_NONE, "point": L.GAUGE_POINT, "mean": L.GAUGE_MEAN}
 
@@ -45,7 +46,7 @@ class Omni3D:
 
     def __init__(self, dims, spacing, dirs, *, density=1.0, line_spacing=1.0, max_iter=4, threshold=0.0,
                  method="plain", solver="anchor", grad="f32", tol=0.0, gauge="none", ref=(0, 0, 0),
-                 seed_first_iteration=True, device=0, anchor_max_links=0):
+                 seed_first_iteration=True, device=0, anchor_max_links=0, engine="auto"):
         nx, ny, nz = (int(d) for d in dims)
         self.dims = (nx, ny, nz)
         self.V = nx * ny * nz
@@ -70,6 +71,7 @@ class Omni3D:
         P.seed_first_iteration = int(bool(seed_first_iteration))
         P.device = int(device)
         P.anchor_max_links = int(anchor_max_links)
+        P.engine = _ENGINES[engine]
         self.params = P
         self.method = method
         self.solve_count = 0
