@@ -12,9 +12,8 @@
 #
 # Line ranges of kernel.cu (reference file:line):
 #   119-1113   ntoijk, crosspoint, cross2point
-#   1743-1863  bodyIntegralInner
-#   1993-2135  bodyIntegralInnerWeighted
-#   2280-2537  bodyIntegralInnerSelect
+#   1743-3085  bodyIntegralInner and its variants (StepCount, Weighted, WeightedFixedBC,
+#              Select, SelectFixedBC, MiniCurl, WeightedMiniCurl)
 #   8171-8212  calIndex
 #   8271-8378  omni3dparallellinesESInnerCPU, devidecountCPU, devidecountInnerCPU,
 #              calCurlofMaterialAccCPU
@@ -44,7 +43,7 @@ stage() {
         echo '#define __global__'
         echo '#define zero 1e-7'
         echo '#define PI 3.1415926535897932384626433832795'
-        for r in 119,1113 1743,1863 1993,2135 2280,2537 8171,8212 8271,8378; do
+        for r in 119,1113 1743,3085 8171,8212 8271,8378; do
             sed -n "${r}p" "$K/kernel.cu" | tr -d '\r'
         done
     } > "$SRC/ref_kernel_extract.cpp"
@@ -58,6 +57,10 @@ stage() {
     grep -q 'float bodyIntegralInner(' "$SRC/ref_kernel_extract.cpp"
     grep -q 'float bodyIntegralInnerSelect(' "$SRC/ref_kernel_extract.cpp"
     grep -q 'float bodyIntegralInnerWeighted(' "$SRC/ref_kernel_extract.cpp"
+    grep -q 'float bodyIntegralInnerWeightedFixedBC(' "$SRC/ref_kernel_extract.cpp"
+    grep -q 'float bodyIntegralInnerSelectFixedBC(' "$SRC/ref_kernel_extract.cpp"
+    grep -q 'float bodyIntegralInnerMiniCurl(' "$SRC/ref_kernel_extract.cpp"
+    grep -q 'float bodyIntegralInnerWeightedMiniCurl(' "$SRC/ref_kernel_extract.cpp"
     grep -q 'void calIndex(' "$SRC/ref_kernel_extract.cpp"
     grep -q 'void calCurlofMaterialAccCPU(' "$SRC/ref_kernel_extract.cpp"
     grep -q 'RHS=new double' "$SRC/calRHS.cpp" && { echo "build_ref: calRHS patch failed" >&2; return 1; }

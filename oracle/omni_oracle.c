@@ -300,9 +300,20 @@ int orc_line_valid(long X, long Y, long Z, const int in[3], const int out[3])
 /* Greedy staircase walk of K:1762-1861: from the entry voxel, step along the axis whose
  * next voxel centre is nearest the line (ties x, then y, then z), until the exit voxel is
  * reached.  Writes one axis code (0,1,2) per step and returns the number of steps, or
- * -(steps+1) if no candidate qualified ("Error! Wrong Point Found!", K:1841). */
-int orc_walk(long X, long Y, long Z, const int in[3], const int out[3], float x, float y,
-             float z, float k1, float k2, float k3, signed char *axes, int cap)
+ * -(steps+1) if no candidate qualified ("Error! Wrong Point Found!", K:1841).
+ * rule selects the variant walks of the reference:
+ *   0  the nearest-candidate rule above;
+ *   1  bodyIntegralInnerWeightedFixedBC (K:2227): as 0, but a y step may not enter j = 0;
+ *   2  bodyIntegralInnerSelectFixedBC (K:2628, 2675, 2722): ties y, then x, then z; no y
+ *      step into j = 0 and no x or z step on j = 0;
+ *   3  bodyIntegralInner(Weighted)MiniCurl (K:2869-2883, 3010-3024): the candidate with the
+ *      smallest curl, read at the candidate's linear index when that index is inside the
+ *      volume and 1e10 otherwise (the far candidate of an axis already at its exit
+ *      coordinate can land inside the volume at an unrelated voxel), ties x, y, z.
+ * A walk that stops early keeps the steps taken (the reference's loop ends there). */
+int orc_walk_rule(long X, long Y, long Z, const int in[3], const int out[3], float x, float y,
+                  float z, float k1, float k2, float k3, int rule, const float *curl,
+                  signed char *axes, int cap)
 {
     float cx = (float)((X - 1) / 2.0), cy = (float)((Y - 1) / 2.0), cz = (float)((Z - 1) / 2.0);
     x = x + cx; y = y + cy; z = z + cz;
@@ -317,25 +328,48 @@ int orc_walk(long X, long Y, long Z, const int in[3], const int out[3], float x,
         long j2 = jl < jo ? jl + 1 : (jl == jo ? jl - 60000 : jl - 1);
         long k3n = kl < ko ? kl + 1 : (kl == ko ? kl - 60000 : kl - 1);
         float r, xt, yt, zt, d1, d2, d3, a, b, c;
-        r = k1 * (float)i1 - x * k1 + k2 * (float)jl - k2 * y + k3 * (float)kl - k3 * z;
-        xt = x + k1 * r; yt = y + k2 * r; zt = z + k3 * r;
-        a = xt - (float)i1; b = yt - (float)jl; c = zt - (float)kl;
-        d1 = sqrtf(a * a + b * b + c * c);
-        r = k1 * (float)il - x * k1 + k2 * (float)j2 - k2 * y + k3 * (float)kl - k3 * z;
-        xt = x + k1 * r; yt = y + k2 * r; zt = z + k3 * r;
-        a = xt - (float)il; b = yt - (float)j2; c = zt - (float)kl;
-        d2 = sqrtf(a * a + b * b + c * c);
-        r = k1 * (float)il - x * k1 + k2 * (float)jl - k2 * y + k3 * (float)k3n - k3 * z;
-        xt = x + k1 * r; yt = y + k2 * r; zt = z + k3 * r;
-        a = xt - (float)il; b = yt - (float)jl; c = zt - (float)k3n;
-        d3 = sqrtf(a * a + b * b + c * c);
-        int moved = 0;
-        if (d1 <= d2 && d1 <= d3 && i1 >= 0 && i1 < X) { if (n < cap) axes[n] = 0; n++; il = i1; moved = 1; }
-        if (d2 < d1 && d2 <= d3 && j2 >= 0 && j2 < Y) { if (n < cap) axes[n] = 1; n++; jl = j2; moved = 1; }
-        if (d3 < d1 && d3 < d2 && k3n >= 0 && k3n < Z) { if (n < cap) axes[n] = 2; n++; kl = k3n; moved = 1; }
+        if (rule == 3) {
+            const long V = X * Y * Z;
+            const long q1 = i1 + jl * X + kl * X * Y, q2 = il + j2 * X + kl * X * Y, q3 = il + jl * X + k3n * X * Y;
+            d1 = (q1 >= 0 && q1 < V) ? curl[q1] : 1e10f;
+            d2 = (q2 >= 0 && q2 < V) ? curl[q2] : 1e10f;
+            d3 = (q3 >= 0 && q3 < V) ? curl[q3] : 1e10f;
+        } else {
+            r = k1 * (float)i1 - x * k1 + k2 * (float)jl - k2 * y + k3 * (float)kl - k3 * z;
+            xt = x + k1 * r; yt = y + k2 * r; zt = z + k3 * r;
+            a = xt - (float)i1; b = yt - (float)jl; c = zt - (float)kl;
+            d1 = sqrtf(a * a + b * b + c * c);
+            r = k1 * (float)il - x * k1 + k2 * (float)j2 - k2 * y + k3 * (float)kl - k3 * z;
+            xt = x + k1 * r; yt = y + k2 * r; zt = z + k3 * r;
+            a = xt - (float)il; b = yt - (float)j2; c = zt - (float)kl;
+            d2 = sqrtf(a * a + b * b + c * c);
+            r = k1 * (float)il - x * k1 + k2 * (float)jl - k2 * y + k3 * (float)k3n - k3 * z;
+            xt = x + k1 * r; yt = y + k2 * r; zt = z + k3 * r;
+            a = xt - (float)il; b = yt - (float)jl; c = zt - (float)k3n;
+            d3 = sqrtf(a * a + b * b + c * c);
+        }
+        int moved = 0, tx, ty, tz;
+        if (rule == 2) {
+            tx = d1 < d2 && d1 <= d3 && i1 >= 0 && i1 < X && jl != 0;
+            ty = d2 <= d1 && d2 <= d3 && j2 > 0 && j2 < Y;
+            tz = d3 < d1 && d3 < d2 && k3n >= 0 && k3n < Z && jl != 0;
+        } else {
+            tx = d1 <= d2 && d1 <= d3 && i1 >= 0 && i1 < X;
+            ty = d2 < d1 && d2 <= d3 && j2 >= (rule == 1 ? 1 : 0) && j2 < Y;
+            tz = d3 < d1 && d3 < d2 && k3n >= 0 && k3n < Z;
+        }
+        if (tx) { if (n < cap) axes[n] = 0; n++; il = i1; moved = 1; }
+        if (ty) { if (n < cap) axes[n] = 1; n++; jl = j2; moved = 1; }
+        if (tz) { if (n < cap) axes[n] = 2; n++; kl = k3n; moved = 1; }
         if (!moved) return -(n + 1);
     } while ((double)(labs(il - io) + labs(jl - jo) + labs(kl - ko)) > 1e-5);
     return n;
+}
+
+int orc_walk(long X, long Y, long Z, const int in[3], const int out[3], float x, float y,
+             float z, float k1, float k2, float k3, signed char *axes, int cap)
+{
+    return orc_walk_rule(X, Y, Z, in, out, x, y, z, k1, k2, k3, 0, NULL, axes, cap);
 }
 
 /* ------------------------------------------------------------------------------------ */
@@ -354,12 +388,13 @@ static inline void axis_signs(const int in[3], const int out[3], int sg[3])
 }
 
 /* Plain method along one line (K:1743-1863).  REAL = float reproduces the reference's
- * arithmetic bit for bit; REAL = double is the FP64 oracle. */
+ * arithmetic bit for bit; REAL = double is the FP64 oracle.  self = 0 drops the entry's own
+ * contribution, as bodyIntegralInnerMiniCurl does (K:2814). */
 #define DEFINE_LINE_PLAIN(SUFFIX, REAL, EXACT)                                                  \
     static void line_plain_##SUFFIX(const orc_grid *g, const int in[3], const int out[3],      \
                                     const signed char *ax, int n, const float *au,              \
                                     const float *av, const float *aw, const REAL *p, REAL *pn,  \
-                                    REAL *cnt)                                                  \
+                                    REAL *cnt, int self)                                        \
     {                                                                                           \
         long X = g->X, XY = g->X * g->Y;                                                        \
         int sg[3];                                                                              \
@@ -370,8 +405,10 @@ static inline void axis_signs(const int in[3], const int out[3], int sg[3])
         const float *comp[3] = {au, av, aw};                                                    \
         const float dl[3] = {g->dx, g->dy, g->dz};                                              \
         REAL pint = 0;                                                                          \
-        pn[e] += p[e];                                                                          \
-        cnt[e] += 1;                                                                            \
+        if (self) {                                                                             \
+            pn[e] += p[e];                                                                      \
+            cnt[e] += 1;                                                                        \
+        }                                                                                       \
         for (int s = 0; s < n; s++) {                                                           \
             int a = ax[s];                                                                      \
             long nx = last + sg[a] * stride[a];                                                 \
@@ -502,6 +539,48 @@ DEFINE_LINE_SELECT(f64, double, 0)
 DEFINE_LINE_WEIGHTED(f32, float, 1)
 DEFINE_LINE_WEIGHTED(f64, double, 0)
 
+/* Weighted method on the minimum-curl walk (bodyIntegralInnerWeightedMiniCurl, K:2937-3085):
+ * the weight sum starts at the entry's curl, unscaled, and the entry receives p0/C*1; every
+ * step adds its curl (not divided by 1e4) and contributes (p0 + I)/C*n, with no test for a
+ * zero sum (a zero sum gives the reference's infinities). */
+#define DEFINE_LINE_WEIGHTED_MC(SUFFIX, REAL, EXACT)                                              \
+    static void line_weighted_mc_##SUFFIX(const orc_grid *g, const int in[3], const int out[3], \
+                                          const signed char *ax, int n, const float *au,         \
+                                          const float *av, const float *aw, const float *curl,   \
+                                          const REAL *p, REAL *pn, REAL *cnt)                    \
+    {                                                                                             \
+        long X = g->X, XY = g->X * g->Y;                                                          \
+        int sg[3];                                                                                \
+        axis_signs(in, out, sg);                                                                  \
+        long e = in[0] + in[1] * X + in[2] * XY;                                                  \
+        long last = e;                                                                            \
+        const long stride[3] = {1, X, XY};                                                        \
+        const float *comp[3] = {au, av, aw};                                                      \
+        const float dl[3] = {g->dx, g->dy, g->dz};                                                \
+        REAL pint = 0, ctmp = (REAL)curl[e], ntmp = 1;                                            \
+        pn[e] += p[e] * 1 / ctmp * ntmp;                                                          \
+        cnt[e] += 1 / ctmp * ntmp;                                                                \
+        for (int s = 0; s < n; s++) {                                                             \
+            int a = ax[s];                                                                        \
+            long nx = last + sg[a] * stride[a];                                                   \
+            if (EXACT) {                                                                          \
+                float h = (-g->rho * (float)sg[a]) * dl[a];                                       \
+                float as = comp[a][nx] + comp[a][last];                                           \
+                pint = (REAL)((double)pint + ((double)h * 0.5) * (double)as);                    \
+            } else {                                                                              \
+                pint += -(double)g->rho * (double)sg[a] * (double)dl[a] * 0.5 *                  \
+                        ((double)comp[a][nx] + (double)comp[a][last]);                            \
+            }                                                                                     \
+            ctmp += (REAL)curl[nx];                                                               \
+            ntmp += 1;                                                                            \
+            pn[nx] += (p[e] + pint) * 1 / ctmp * ntmp;                                            \
+            cnt[nx] += 1 / ctmp * ntmp;                                                           \
+            last = nx;                                                                            \
+        }                                                                                         \
+    }
+DEFINE_LINE_WEIGHTED_MC(f32, float, 1)
+DEFINE_LINE_WEIGHTED_MC(f64, double, 0)
+
 /* ------------------------------------------------------------------------------------ */
 /* full sweep, normalisation, iteration                                                   */
 /* ------------------------------------------------------------------------------------ */
@@ -511,9 +590,22 @@ typedef struct {
     float dx, dy, dz, rho, ls, thr;
     int nv;
     const float *k1, *k2, *k3;
-    int mode;          /* 0 plain, 1 select, 2 weighted */
+    int mode;          /* 0 plain, 1 select, 2 weighted, 3 weighted fixed-BC, 4 select
+                          fixed-BC, 5 minimum-curl plain, 6 minimum-curl weighted */
     int geom_cpu_twin; /* 1: CPU-twin geometry (no pole guard, NoGrid without spacing) */
 } orc_problem;
+
+/* Walk rule of each mode (see orc_walk_rule). */
+static int orc_mode_walk_rule(int mode)
+{
+    switch (mode) {
+    case 3: return 1;
+    case 4: return 2;
+    case 5:
+    case 6: return 3;
+    default: return 0;
+    }
+}
 
 static long max_path(long X, long Y, long Z) { return X + Y + Z + 4; }
 
@@ -540,13 +632,16 @@ static long max_path(long X, long Y, long Z) { return X + Y + Z + 4; }
                 orc_cross2point(P->X, P->Y, P->Z, xyz[0], xyz[1], xyz[2], P->k1[d], P->k2[d],      \
                                 P->k3[d], in, out);                                                \
                 if (!orc_line_valid(P->X, P->Y, P->Z, in, out)) continue;                          \
-                int n = orc_walk(P->X, P->Y, P->Z, in, out, xyz[0], xyz[1], xyz[2], P->k1[d],      \
-                                 P->k2[d], P->k3[d], ax, (int)cap);                                \
-                if (n < 0) { errors++; n = -n - 1; }                                               \
-                if (P->mode == 0)                                                                  \
-                    line_plain_##SUFFIX(&g, in, out, ax, n, au, av, aw, p, pn, cnt);               \
-                else if (P->mode == 2)                                                             \
+                const int rule = orc_mode_walk_rule(P->mode);                                      \
+                int n = orc_walk_rule(P->X, P->Y, P->Z, in, out, xyz[0], xyz[1], xyz[2], P->k1[d], \
+                                      P->k2[d], P->k3[d], rule, curl, ax, (int)cap);               \
+                if (n < 0) { if (rule == 0) errors++; n = -n - 1; }                                \
+                if (P->mode == 0 || P->mode == 5)                                                  \
+                    line_plain_##SUFFIX(&g, in, out, ax, n, au, av, aw, p, pn, cnt, P->mode == 0); \
+                else if (P->mode == 2 || P->mode == 3)                                             \
                     line_weighted_##SUFFIX(&g, in, out, ax, n, au, av, aw, curl, p, pn, cnt);      \
+                else if (P->mode == 6)                                                             \
+                    line_weighted_mc_##SUFFIX(&g, in, out, ax, n, au, av, aw, curl, p, pn, cnt);   \
                 else                                                                               \
                     line_select_##SUFFIX(&g, in, out, ax, n, au, av, aw, curl, p, pn, cnt);        \
             }                                                                                      \

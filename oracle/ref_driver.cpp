@@ -38,6 +38,26 @@ float bodyIntegralInnerWeighted(long Xsize, long Ysize, long Zsize, int iin, int
                                 float k2, float k3, float deltx, float delty, float deltz,
                                 float density, float *DuDt, float *DvDt, float *DwDt, float *curl,
                                 float *p, float *pn, float *pcountinner);
+float bodyIntegralInnerWeightedFixedBC(long Xsize, long Ysize, long Zsize, int iin, int jin, int kin,
+                                int iout, int jout, int kout, float x, float y, float z, float k1,
+                                float k2, float k3, float deltx, float delty, float deltz,
+                                float density, float *DuDt, float *DvDt, float *DwDt, float *curl,
+                                float *p, float *pn, float *pcountinner);
+float bodyIntegralInnerMiniCurl(long Xsize, long Ysize, long Zsize, int iin, int jin, int kin,
+                                int iout, int jout, int kout, float x, float y, float z, float k1,
+                                float k2, float k3, float deltx, float delty, float deltz,
+                                float density, float *DuDt, float *DvDt, float *DwDt, float *curl,
+                                float *p, float *pn, float *pcountinner);
+float bodyIntegralInnerWeightedMiniCurl(long Xsize, long Ysize, long Zsize, int iin, int jin, int kin,
+                                int iout, int jout, int kout, float x, float y, float z, float k1,
+                                float k2, float k3, float deltx, float delty, float deltz,
+                                float density, float *DuDt, float *DvDt, float *DwDt, float *curl,
+                                float *p, float *pn, float *pcountinner);
+float bodyIntegralInnerSelectFixedBC(long Xsize, long Ysize, long Zsize, int iin, int jin, int kin,
+                              int iout, int jout, int kout, float x, float y, float z, float k1,
+                              float k2, float k3, float deltx, float delty, float deltz,
+                              float density, float *DuDt, float *DvDt, float *DwDt, float *p,
+                              float *pn, float *curl, float *pcountinner, float threshold);
 void calIndex(long *index, long Xsize, long Ysize, long Zsize);
 void omni3dparallellinesESInnerCPU(long Xsize, long Ysize, long Zsize, int NoAngles,
                                    float linespacing, float *k1_d, float *k2_d, float *k3_d,
@@ -62,7 +82,8 @@ struct Problem {
     float dx, dy, dz, rho, ls, thr;
     int nv;
     const float *k1, *k2, *k3;
-    int mode;  // 0 plain, 1 select, 2 weighted
+    int mode;  // 0 plain, 1 select, 2 weighted, 3 weighted fixed-BC, 4 select fixed-BC,
+               // 5 minimum-curl plain, 6 minimum-curl weighted
 };
 
 // Geometry of the GPU kernel (kernel.cu:6159-6194) with libm trigonometry.
@@ -110,6 +131,22 @@ long long sweep_range(const Problem &P, int d0, int d1, long *index, float *au, 
                         bodyIntegralInnerWeighted(P.X, P.Y, P.Z, iin, jin, kin, iout, jout, kout, x,
                                                   y, z, k1, k2, k3, P.dx, P.dy, P.dz, P.rho, au, av,
                                                   aw, curl, p, pn, cnt);
+                    else if (P.mode == 3)
+                        bodyIntegralInnerWeightedFixedBC(P.X, P.Y, P.Z, iin, jin, kin, iout, jout, kout,
+                                                         x, y, z, k1, k2, k3, P.dx, P.dy, P.dz, P.rho,
+                                                         au, av, aw, curl, p, pn, cnt);
+                    else if (P.mode == 4)
+                        bodyIntegralInnerSelectFixedBC(P.X, P.Y, P.Z, iin, jin, kin, iout, jout, kout,
+                                                       x, y, z, k1, k2, k3, P.dx, P.dy, P.dz, P.rho, au,
+                                                       av, aw, p, pn, curl, cnt, P.thr);
+                    else if (P.mode == 5)
+                        bodyIntegralInnerMiniCurl(P.X, P.Y, P.Z, iin, jin, kin, iout, jout, kout, x,
+                                                  y, z, k1, k2, k3, P.dx, P.dy, P.dz, P.rho, au, av,
+                                                  aw, curl, p, pn, cnt);
+                    else if (P.mode == 6)
+                        bodyIntegralInnerWeightedMiniCurl(P.X, P.Y, P.Z, iin, jin, kin, iout, jout,
+                                                          kout, x, y, z, k1, k2, k3, P.dx, P.dy, P.dz,
+                                                          P.rho, au, av, aw, curl, p, pn, cnt);
                     else
                         bodyIntegralInnerSelect(P.X, P.Y, P.Z, iin, jin, kin, iout, jout, kout, x,
                                                 y, z, k1, k2, k3, P.dx, P.dy, P.dz, P.rho, au, av,

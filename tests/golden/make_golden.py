@@ -15,6 +15,11 @@ outputs of the reference functions:
   weighted 13x11x9 grid with a masked sphere, 42 directions, 3 iterations of
            bodyIntegralInnerWeighted (curl-weighted, no entry contribution; voxels outside
            the mask have curl 0, so lines that start there skip their first steps)
+  variants 12x11x9 grid with a masked sphere, 42 directions, 2 iterations of each variant
+           the reference keeps beside its three methods: bodyIntegralInnerWeightedFixedBC
+           (mode 3), bodyIntegralInnerSelectFixedBC (mode 4, threshold at the 75th
+           percentile of the curl), bodyIntegralInnerMiniCurl (mode 5) and
+           bodyIntegralInnerWeightedMiniCurl (mode 6)
   ls07     10x9x8 grid, 42 directions, line spacing 0.7, 2 plain iterations
   cputwin  10x10x10 grid, 42 directions, 2 iterations of the reference's own CPU loop
            omni3dparallellinesESInnerCPU + devidecountInnerCPU (no pole guard, count > 1)
@@ -82,6 +87,19 @@ def main():
                 "weighted_ax": f["ax"].reshape(-1), "weighted_ay": f["ay"].reshape(-1),
                 "weighted_az": f["az"].reshape(-1), "weighted_mask": f["mask"].reshape(-1),
                 "weighted_curl": curl, "weighted_p0": p0, "weighted_p": p, "weighted_count": c})
+    # variants: fixed-boundary and minimum-curl walks
+    d = (12, 11, 9)
+    f = field(d, 9, sphere=2.5)
+    p0 = pinit(d, 10)
+    curl = R.curl(d, f["spacing"], f["ax"], f["ay"], f["az"], f["mask"])
+    thr = np.float32(np.percentile(curl[curl > 0], 75))
+    out.update({"variants_dims": np.array(d), "variants_spacing": np.array(f["spacing"], np.float32),
+                "variants_ax": f["ax"].reshape(-1), "variants_ay": f["ay"].reshape(-1),
+                "variants_az": f["az"].reshape(-1), "variants_curl": curl, "variants_thr": np.array(thr),
+                "variants_p0": p0})
+    for mode in (3, 4, 5, 6):
+        p, c = R.solve(d, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p0, 2, mode=mode, thr=float(thr), curl=curl)
+        out.update({"variants_p_mode%d" % mode: p, "variants_count_mode%d" % mode: c})
     # line spacing 0.7
     d = (10, 9, 8)
     f = field(d, 5)

@@ -56,6 +56,17 @@ def test_golden_weighted_bit_exact(orc, gold):
     np.testing.assert_array_equal(_bits(p), _bits(g["weighted_p"]))
 
 
+@pytest.mark.parametrize("mode", [3, 4, 5, 6])
+def test_golden_variant_walks_bit_exact(orc, gold, mode):
+    """Fixed-boundary walks (modes 3, 4) and minimum-curl walks (modes 5, 6)."""
+    g = gold
+    d = _dims(g, "variants")
+    p, c = orc.solve(d, _sp(g, "variants"), g["dirs"], g["variants_ax"], g["variants_ay"], g["variants_az"],
+                     g["variants_p0"], 2, mode=mode, thr=float(g["variants_thr"]), curl=g["variants_curl"])
+    np.testing.assert_array_equal(_bits(c), _bits(g["variants_count_mode%d" % mode]))
+    np.testing.assert_array_equal(_bits(p), _bits(g["variants_p_mode%d" % mode]))
+
+
 def test_golden_line_spacing(orc, gold):
     g = gold
     d = _dims(g, "ls07")
