@@ -43,6 +43,20 @@ extern "C" {
                                      commented-out alternative of main, K:8844): every step
                                      weighted by n / sum(curl/1e4) from the entry, no
                                      contribution to the entry itself */
+/* Variants the reference keeps beside its three methods.  Fixed boundary: the walk never
+ * steps into the j = 0 face (the Bernoulli face of main(), K:8805-8811), so that face keeps
+ * its initial values.  Minimum curl: each step goes to the candidate voxel with the
+ * smallest curl instead of the one nearest the line, so the paths depend on the field and
+ * are re-walked for every solve. */
+#define OMNI3D_METHOD_WEIGHTED_FIXED_BC 3  /* bodyIntegralInnerWeightedFixedBC, K:2136-2279 */
+#define OMNI3D_METHOD_SELECT_FIXED_BC 4    /* bodyIntegralInnerSelectFixedBC, K:2538-2796 (also
+                                              ties y before x before z) */
+#define OMNI3D_METHOD_MINI_CURL 5          /* bodyIntegralInnerMiniCurl, K:2797-2936: the plain
+                                              accumulation without the entry's own term */
+#define OMNI3D_METHOD_WEIGHTED_MINI_CURL 6 /* bodyIntegralInnerWeightedMiniCurl, K:2937-3085
+                                              (commented out in main, K:8847): weights n / sum
+                                              of raw curl from the entry, the entry included,
+                                              no zero-sum test */
 
 /* Solver form.  Both produce the reference iteration's result; they differ in cost. */
 #define OMNI3D_SOLVER_ANCHOR 0  /* iterate only the voxels whose values feed back (line
@@ -133,7 +147,7 @@ int omni3d_set_stream(omni3d_ctx *ctx, void *stream);
 /* Solve one snapshot: the whole per-file block of main(), K:8794-8863 (initial state,
  * NoItr x {omni sweep, devidecountInner}, read back p and count).
  *   ax, ay, az   material acceleration Du/Dt, Dv/Dt, Dw/Dt (grad p = -rho a)
- *   curl         |curl a| x mask (SELECT and WEIGHTED methods; NULL: computed on the device
+ *   curl         |curl a| x mask (every method but PLAIN; NULL: computed on the device
  *                from ax..az and mask), see omni3d_curl
  *   mask         mask column of the input file (NULL: all ones); used only when curl is NULL
  *   p_init       initial pressure (NULL: zero), e.g. omni3d_bernoulli_face()

@@ -96,6 +96,8 @@ class Oracle:
         L.orc_line_valid.argtypes = [_l, _l, _l, _ip, _ip]
         L.orc_walk.restype = _i
         L.orc_walk.argtypes = [_l, _l, _l, _ip, _ip, _f, _f, _f, _f, _f, _f, _bp, _i]
+        L.orc_walk_rule.restype = _i
+        L.orc_walk_rule.argtypes = [_l, _l, _l, _ip, _ip, _f, _f, _f, _f, _f, _f, _i, _fp, _bp, _i]
         L.orc_trace_direction.restype = _l
         L.orc_trace_direction.argtypes = [_l, _l, _l, _f, _f, _f, _f, _i, _ip, _ip, _ip, _fp]
         for s, ptr in (("f32", _fp), ("f64", _dp)):
@@ -139,17 +141,23 @@ class Oracle:
                                      _ptr(xyz, C.c_float))
         return valid, inout, nsteps, xyz
 
-    def walk(self, dims, inout, xyz, kd) -> np.ndarray:
+    def walk(self, dims, inout, xyz, kd, rule=0, curl=None, allow_early_stop=False) -> np.ndarray:
+        """Staircase of one line under walk rule `rule` (orc_walk_rule; rule 3 reads curl).
+        A walk that stops early raises unless allow_early_stop (the variant rules stop by
+        design)."""
         X, Y, Z = dims
         cap = X + Y + Z + 4
         ax = np.zeros(cap, np.int8)
         i = np.ascontiguousarray(inout[:3], np.int32)
         o = np.ascontiguousarray(inout[3:], np.int32)
-        n = self.lib.orc_walk(X, Y, Z, _ptr(i, C.c_int), _ptr(o, C.c_int), float(xyz[0]), float(xyz[1]),
-                              float(xyz[2]), float(kd[0]), float(kd[1]), float(kd[2]),
-                              _ptr(ax, C.c_byte), cap)
+        c = None if curl is None else np.ascontiguousarray(np.asarray(curl, np.float32).reshape(-1))
+        n = self.lib.orc_walk_rule(X, Y, Z, _ptr(i, C.c_int), _ptr(o, C.c_int), float(xyz[0]), float(xyz[1]),
+                                   float(xyz[2]), float(kd[0]), float(kd[1]), float(kd[2]), int(rule),
+                                   None if c is None else _ptr(c, C.c_float), _ptr(ax, C.c_byte), cap)
         if n < 0:
-            raise RuntimeError("walk failed")
+            if not allow_early_stop:
+                raise RuntimeError("walk failed")
+            n = -n - 1
         return ax[:n].copy()
 
     # -- sweeps ------------------------------------------------------------------------

@@ -167,7 +167,7 @@ int check_params(const omni3d_params *p, std::string *why)
     if (!(p->line_spacing > 0.0f) || !std::isfinite(p->line_spacing)) { *why = "line_spacing must be > 0"; return OMNI3D_ERR_ARG; }
     if (p->n_dirs <= 0 || !p->dirs) { *why = "no directions"; return OMNI3D_ERR_ARG; }
     if (p->max_iter < 0) { *why = "max_iter must be >= 0"; return OMNI3D_ERR_ARG; }
-    if (p->method != OMNI3D_METHOD_PLAIN && p->method != OMNI3D_METHOD_SELECT && p->method != OMNI3D_METHOD_WEIGHTED) {
+    if (p->method < OMNI3D_METHOD_PLAIN || p->method > OMNI3D_METHOD_WEIGHTED_MINI_CURL) {
         *why = "unknown method";
         return OMNI3D_ERR_ARG;
     }
@@ -251,6 +251,10 @@ int choose_engine(omni3d_ctx *ctx, bool bf16, int *rc)
     if (bf16) {
         if (want == OMNI3D_ENGINE_BRICKS)
             *rc = fail(ctx, OMNI3D_ERR_STATE, "the brick engine needs FP32 gradient storage");
+        return OMNI3D_ENGINE_LINES;
+    }
+    if (ctx->geo.walk_rule == 3) {
+        *rc = fail(ctx, OMNI3D_ERR_STATE, "the brick engine does not take minimum-curl walks (they change per field)");
         return OMNI3D_ENGINE_LINES;
     }
     if (!ctx->bricks.built && !ctx->bricks_failed) {
@@ -441,6 +445,7 @@ int omni3d_create(const omni3d_params *params, omni3d_ctx **out)
     int mx = std::max(std::max(g.X, g.Y), g.Z);
     g.ng = (int)(mx * 1.732 / (double)params->line_spacing);  // K:6167
     ctx->geo.nv = params->n_dirs;
+    ctx->geo.walk_rule = method_walk_rule(params->method);
 
     auto bail = [&](cudaError_t ce, const char *what) {
         int r = cuda_fail(ctx, ce, what);
@@ -612,6 +617,7 @@ int omni3d_sweep(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
     Field F;
     int rc = prepare_field(ctx, ax, ay, az, curl, nullptr, dev, &F);
     if (rc) return rc;
+    if (ctx->geo.walk_rule == 3) CK(ctx, run_walk(&ctx->geo, 3, F.curl, ctx->st));  // paths follow this field
     const float *dp;
     if ((rc = stage(ctx, p, dev, ctx->in_pinit, V, &dp))) return rc;
     CK(ctx, ctx->pncnt.ensure(sizeof(float2) * (size_t)V));
@@ -660,6 +666,8 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
     Field F;
     int rc = prepare_field(ctx, ax, ay, az, curl, mask, dev, &F);
     if (rc) return rc;
+    if (ctx->geo.walk_rule == 3 && P.max_iter > 0)
+        CK(ctx, run_walk(&ctx->geo, 3, F.curl, st));  // minimum-curl paths follow this field
     int engine = OMNI3D_ENGINE_LINES;
     if (P.max_iter > 0) {
         engine = choose_engine(ctx, bf16, &rc);

@@ -7,7 +7,9 @@
 // separators in the parameter file are accepted.  Defaults follow the reference main(): the
 // selected method, exactly NoItr iterations, no gauge.
 //
-// Options: --params PATH  --method select|plain|weighted  --solver anchor|sweep  --tol T
+// Options: --params PATH  --method select|plain|weighted|weighted-fixed-bc|select-fixed-bc|
+//                                   mini-curl|weighted-mini-curl
+//          --solver anchor|sweep  --tol T
 //          --gauge none|point|mean  --ref I,J,K  --grad f32|bf16  --device N
 #include <dirent.h>
 #include <sys/stat.h>
@@ -59,7 +61,8 @@ void list_files(const std::string &dir, std::vector<std::string> &out)
 int usage()
 {
     std::fprintf(stderr,
-                 "usage: omni3d [--params PATH] [--method select|plain|weighted] [--solver anchor|sweep] [--tol T]\n"
+                 "usage: omni3d [--params PATH] [--method select|plain|weighted|weighted-fixed-bc|select-fixed-bc|\n"
+                 "              mini-curl|weighted-mini-curl] [--solver anchor|sweep] [--tol T]\n"
                  "              [--gauge none|point|mean] [--ref I,J,K] [--grad f32|bf16] [--device N]\n");
     return 2;
 }
@@ -84,6 +87,10 @@ int main(int argc, char **argv)
             if (v == "plain") prm.method = OMNI3D_METHOD_PLAIN;
             else if (v == "select") prm.method = OMNI3D_METHOD_SELECT;
             else if (v == "weighted") prm.method = OMNI3D_METHOD_WEIGHTED;
+            else if (v == "weighted-fixed-bc") prm.method = OMNI3D_METHOD_WEIGHTED_FIXED_BC;
+            else if (v == "select-fixed-bc") prm.method = OMNI3D_METHOD_SELECT_FIXED_BC;
+            else if (v == "mini-curl") prm.method = OMNI3D_METHOD_MINI_CURL;
+            else if (v == "weighted-mini-curl") prm.method = OMNI3D_METHOD_WEIGHTED_MINI_CURL;
             else return usage();
         }
         else if (k == "--solver") { std::string v = val(); prm.solver = v == "sweep" ? OMNI3D_SOLVER_SWEEP : OMNI3D_SOLVER_ANCHOR; }

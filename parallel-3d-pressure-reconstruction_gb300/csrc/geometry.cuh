@@ -257,13 +257,35 @@ struct OmWalker {
         xk1 = OM_MUL(x, k1); yk2 = OM_MUL(k2, y); zk3 = OM_MUL(k3, z);
     }
 
-    // One step of the nearest-candidate rule (ties x, y, z).  Returns the axis moved along
-    // (0, 1, 2) or -1 when no candidate qualifies.
-    __device__ __forceinline__ int step()
+    // One step of the walk.  Returns the axis moved along (0, 1, 2) or -1 when no candidate
+    // qualifies (the reference's loop ends there).  RULE:
+    //   0  nearest candidate to the line, ties x, y, z (K:1762-1840);
+    //   1  as 0, but no y step into j = 0 (bodyIntegralInnerWeightedFixedBC, K:2227);
+    //   2  nearest candidate, ties y, x, z; no y step into j = 0 and no x or z step on
+    //      j = 0 (bodyIntegralInnerSelectFixedBC, K:2628, 2675, 2722);
+    //   3  the candidate with the smallest curl, read at the candidate's linear index when
+    //      that index lies inside the volume and 1e10 otherwise, ties x, y, z
+    //      (bodyIntegralInner(Weighted)MiniCurl, K:2869-2883).  The far candidate of an axis
+    //      already at its exit coordinate (60000 cells away) may land inside the volume at an
+    //      unrelated voxel, as in the reference; its coordinate test still rejects it.
+    template <int RULE>
+    __device__ __forceinline__ int step(const float *curl, int X, long long XY, long long V)
     {
         int i1 = il < io ? il + 1 : (il == io ? il - 60000 : il - 1);
         int j2 = jl < jo ? jl + 1 : (jl == jo ? jl - 60000 : jl - 1);
         int k3n = kl < ko ? kl + 1 : (kl == ko ? kl - 60000 : kl - 1);
+        if (RULE == 3) {
+            const long long q1 = (long long)i1 + (long long)jl * X + (long long)kl * XY;
+            const long long q2 = (long long)il + (long long)j2 * X + (long long)kl * XY;
+            const long long q3 = (long long)il + (long long)jl * X + (long long)k3n * XY;
+            const float c1 = (q1 >= 0 && q1 < V) ? __ldg(curl + q1) : 1e10f;
+            const float c2 = (q2 >= 0 && q2 < V) ? __ldg(curl + q2) : 1e10f;
+            const float c3 = (q3 >= 0 && q3 < V) ? __ldg(curl + q3) : 1e10f;
+            if (il != io && c1 <= c2 && c1 <= c3) { il = i1; return 0; }
+            if (jl != jo && c2 < c1 && c2 <= c3) { jl = j2; return 1; }
+            if (kl != ko && c3 < c1 && c3 < c2) { kl = k3n; return 2; }
+            return -1;
+        }
         float fil = (float)il, fjl = (float)jl, fkl = (float)kl;
         float fi1 = (float)i1, fj2 = (float)j2, fk3 = (float)k3n;
         float k2jl = OM_MUL(k2, fjl), k3kl = OM_MUL(k3, fkl);
@@ -275,8 +297,14 @@ struct OmWalker {
         float q2 = om_dist2(x, y, z, k1, k2, k3, r2, fil, fj2, fkl);
         float q3 = om_dist2(x, y, z, k1, k2, k3, r3, fil, fjl, fk3);
         // the candidate toward the exit is always inside; the far (-60000) one never is
+        if (RULE == 2) {
+            if (il != io && jl != 0 && om_sqrt_lt(q1, q2) && om_sqrt_le(q1, q3)) { il = i1; return 0; }
+            if (jl != jo && j2 != 0 && om_sqrt_le(q2, q1) && om_sqrt_le(q2, q3)) { jl = j2; return 1; }
+            if (kl != ko && jl != 0 && om_sqrt_lt(q3, q1) && om_sqrt_lt(q3, q2)) { kl = k3n; return 2; }
+            return -1;
+        }
         if (il != io && om_sqrt_le(q1, q2) && om_sqrt_le(q1, q3)) { il = i1; return 0; }
-        if (jl != jo && om_sqrt_lt(q2, q1) && om_sqrt_le(q2, q3)) { jl = j2; return 1; }
+        if (jl != jo && (RULE != 1 || j2 != 0) && om_sqrt_lt(q2, q1) && om_sqrt_le(q2, q3)) { jl = j2; return 1; }
         if (kl != ko && om_sqrt_lt(q3, q1) && om_sqrt_lt(q3, q2)) { kl = k3n; return 2; }
         return -1;
     }

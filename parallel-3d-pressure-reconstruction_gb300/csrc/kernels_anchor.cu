@@ -117,7 +117,8 @@ struct Walk {
 };
 
 // Plain method: anchors are the entries; every voxel of a line takes (p[entry] + I, 1).
-template <int PASS, bool BF16>
+// SELF = false leaves the entry's own term out (the minimum-curl plain variant).
+template <int PASS, bool BF16, bool SELF>
 __global__ void __launch_bounds__(256, 6) k_anchor_plain(Grid g, const LineRec *__restrict__ lines,
                                                       const uint32_t *__restrict__ gbase,
                                                       const uint32_t *__restrict__ desc, long long n_lines,
@@ -134,7 +135,7 @@ __global__ void __launch_bounds__(256, 6) k_anchor_plain(Grid g, const LineRec *
     Walk L;
     L.init(g, r, gbase, desc, li);
     const long long e = r.e;
-    emit<PASS>(S, e, e, 1.0f, 0.0f);
+    if (SELF) emit<PASS>(S, e, e, 1.0f, 0.0f);
     constexpr bool kGrad = PASS == kFill || PASS == kRhs;
     float4 gl = make_float4(0.f, 0.f, 0.f, 0.f);
     if (kGrad) gl = load_grad<BF16>(f32, b16, e);
@@ -186,6 +187,44 @@ __global__ void __launch_bounds__(256, 6) k_anchor_weighted(Grid g, const LineRe
             csum += __fdiv_rn(cn, 1.0e4f);  // the weights as in k_sweep_weighted
             nseg += 1.0f;
             if (csum != 0.0f) emit<PASS>(S, L.v, e, __frcp_rn(csum) * nseg, I);
+            gl = gv;
+        }
+    }
+}
+
+// Weighted method with raw curl sums (the minimum-curl variant): the walk of
+// k_sweep_weighted_raw; anchors are the entries, the entry takes its own term.
+template <int PASS, bool BF16>
+__global__ void __launch_bounds__(256, 6) k_anchor_weighted_raw(Grid g, const LineRec *__restrict__ lines,
+                                                             const uint32_t *__restrict__ gbase,
+                                                             const uint32_t *__restrict__ desc, long long n_lines,
+                                                             const float4 *__restrict__ f32,
+                                                             const uint2 *__restrict__ b16,
+                                                             const float *__restrict__ curl, Sink S)
+{
+    static_assert(PASS == kFill, "the raw-curl weighted operator has only a filling pass");
+    long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= n_lines) return;
+    LineRec r = lines[li];
+    Walk L;
+    L.init(g, r, gbase, desc, li);
+    const long long e = r.e;
+    float4 gl = load_grad<BF16>(f32, b16, e);
+    float csum = BF16 ? __ldg(curl + e) : gl.w, nseg = 1.0f;
+    emit<PASS>(S, e, e, __frcp_rn(csum), 0.0f);
+    float I = 0.0f, comp = 0.0f;
+    for (int s0 = 0; s0 < L.m; s0 += 16) {
+        uint32_t w = __ldg(L.dp + 32 * (s0 >> 4));
+        int n = min(16, L.m - s0);
+        for (int t = 0; t < n; t++, w >>= 2) {
+            int a = (int)(w & 3u);
+            L.v += a == 0 ? L.d0 : (a == 1 ? L.d1 : L.d2);
+            float4 gv = load_grad<BF16>(f32, b16, L.v);
+            float cn = BF16 ? __ldg(curl + L.v) : gv.w;
+            kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
+            csum += cn;
+            nseg += 1.0f;
+            emit<PASS>(S, L.v, e, __frcp_rn(csum) * nseg, I);
             gl = gv;
         }
     }
@@ -317,10 +356,24 @@ __global__ void k_row_capacity(long long n, const uint32_t *vox, const uint32_t 
         out[i] = lines_through[vox[i]];
 }
 
-__global__ void k_u32_to_u64(long long n, const uint32_t *in, unsigned long long *out)
+// Row sums of the anchor iteration: compensated (Kahan) FP32 per lane, the 32 lane sums
+// and the numerator in FP64.  A row gathers about as many terms as lines cross its voxel
+// (~1000 at 642 directions); plain FP32 sums of that many terms leave a rounding floor near
+// 1e-6 in the iteration's relative change, above the tolerances the solver is asked for.
+__device__ __forceinline__ double warp_sum_compensated(float s, float comp)
 {
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        out[i] = in[i];
+    double d = (double)s - (double)comp;
+    for (int o = 16; o; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+    return d;
+}
+
+__device__ __forceinline__ float anchor_update(double sum, long long row, const float *b, const float *c,
+                                               const uint32_t *vox, const float *p_init, int seed, const float *pc)
+{
+    const float cc = c[row];
+    double numer = (double)b[row] + sum;
+    if (seed && p_init) numer += (double)p_init[vox[row]];
+    return cc > 0.0f ? (float)(numer / (double)cc) : pc[row];
 }
 
 // One anchor iteration, a warp per row.
@@ -335,15 +388,10 @@ __global__ void __launch_bounds__(256) k_anchor_spmv(long long n, const unsigned
     int lane = threadIdx.x & 31;
     if (row >= n) return;  // whole warps
     unsigned long long j0 = rowptr[row], j1 = j0 + rowlen[row];
-    float s = 0.0f;
-    for (unsigned long long j = j0 + lane; j < j1; j += 32) s += __ldg(w + j) * __ldg(pc + __ldg(col + j));
-    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) {
-        float cc = c[row];
-        float numer = b[row] + s;
-        if (seed && p_init) numer += p_init[vox[row]];
-        pn[row] = cc > 0.0f ? __fdiv_rn(numer, cc) : pc[row];
-    }
+    float s = 0.0f, comp = 0.0f;
+    for (unsigned long long j = j0 + lane; j < j1; j += 32) kahan_add(s, comp, __ldg(w + j) * __ldg(pc + __ldg(col + j)));
+    const double sum = warp_sum_compensated(s, comp);
+    if (lane == 0) pn[row] = anchor_update(sum, row, b, c, vox, p_init, seed, pc);
 }
 
 // Plain method: every weight is 1, so a row is a plain sum of gathered anchor values.
@@ -358,15 +406,10 @@ __global__ void __launch_bounds__(256) k_anchor_spmv_unit(long long n, const uns
     int lane = threadIdx.x & 31;
     if (row >= n) return;  // whole warps
     unsigned long long j0 = rowptr[row], j1 = j0 + rowlen[row];
-    float s = 0.0f;
-    for (unsigned long long j = j0 + lane; j < j1; j += 32) s += __ldg(pc + __ldg(col + j));
-    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) {
-        float cc = c[row];
-        float numer = b[row] + s;
-        if (seed && p_init) numer += p_init[vox[row]];
-        pn[row] = cc > 0.0f ? __fdiv_rn(numer, cc) : pc[row];
-    }
+    float s = 0.0f, comp = 0.0f;
+    for (unsigned long long j = j0 + lane; j < j1; j += 32) kahan_add(s, comp, __ldg(pc + __ldg(col + j)));
+    const double sum = warp_sum_compensated(s, comp);
+    if (lane == 0) pn[row] = anchor_update(sum, row, b, c, vox, p_init, seed, pc);
 }
 
 constexpr int kRedBlocks = 256, kRedThreads = 256;
@@ -469,13 +512,22 @@ cudaError_t run_pass(const Geometry &geo, const Field &f, int method, bool bf16,
     else ok = ok && S.bits && S.id && S.b;
     if (PASS == kFill) ok = ok && S.rowptr && S.cursor && S.col && S.w && S.c;
     if (need_field) ok = ok && (bf16 ? f.bf16 != nullptr : f.f32 != nullptr);
-    if (method == OMNI3D_METHOD_SELECT || (method == OMNI3D_METHOD_WEIGHTED && PASS == kFill))
-        ok = ok && f.curl && (bf16 || f.f32);
-    if (method == OMNI3D_METHOD_WEIGHTED && PASS == kRhs) ok = false;  // no cached weighted operator
+    const int acc = method_accum(method);
+    const bool weighted = acc == kAccWeighted || acc == kAccWeightedRawCurl;
+    if (acc == kAccSelect || (weighted && PASS == kFill)) ok = ok && f.curl && (bf16 || f.f32);
+    if (PASS == kRhs && acc != kAccPlain) ok = false;  // only the plain operator is cached
     if (!ok) return cudaErrorInvalidValue;
     unsigned blocks = (unsigned)((geo.n_lines + 255) / 256);
     const Grid &g = geo.grid;
-    if (method == OMNI3D_METHOD_WEIGHTED && PASS == kFill) {
+    if (acc == kAccWeightedRawCurl && PASS == kFill) {
+        if (bf16)
+            k_anchor_weighted_raw<kFill, true><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
+                                                                       geo.n_lines, f.f32, f.bf16, f.curl, S);
+        else
+            k_anchor_weighted_raw<kFill, false><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
+                                                                        geo.n_lines, f.f32, f.bf16, f.curl, S);
+        OM_COUNT_LAUNCH();
+    } else if (acc == kAccWeighted && PASS == kFill) {
         if (bf16)
             k_anchor_weighted<kFill, true><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
                                                                    geo.n_lines, f.f32, f.bf16, f.curl, S);
@@ -483,7 +535,7 @@ cudaError_t run_pass(const Geometry &geo, const Field &f, int method, bool bf16,
             k_anchor_weighted<kFill, false><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
                                                                     geo.n_lines, f.f32, f.bf16, f.curl, S);
         OM_COUNT_LAUNCH();
-    } else if (method == OMNI3D_METHOD_SELECT) {
+    } else if (acc == kAccSelect) {
         if (bf16)
             k_anchor_select<PASS, true><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
                                                                 f.f32, f.bf16, f.curl, S);
@@ -491,13 +543,21 @@ cudaError_t run_pass(const Geometry &geo, const Field &f, int method, bool bf16,
             k_anchor_select<PASS, false><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
                                                                  f.f32, f.bf16, f.curl, S);
         OM_COUNT_LAUNCH();
-    } else {  // plain method, and the weighted method's marking pass (anchors = entries)
+    } else if (acc == kAccPlainNoEntry && PASS == kFill) {
         if (bf16)
-            k_anchor_plain<PASS, true><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
-                                                               f.f32, f.bf16, S);
+            k_anchor_plain<PASS, true, false><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
+                                                                      geo.n_lines, f.f32, f.bf16, S);
         else
-            k_anchor_plain<PASS, false><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
-                                                                f.f32, f.bf16, S);
+            k_anchor_plain<PASS, false, false><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
+                                                                       geo.n_lines, f.f32, f.bf16, S);
+        OM_COUNT_LAUNCH();
+    } else {  // plain method, and the marking pass of every method whose anchors are the entries
+        if (bf16)
+            k_anchor_plain<PASS, true, true><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
+                                                                     geo.n_lines, f.f32, f.bf16, S);
+        else
+            k_anchor_plain<PASS, false, true><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
+                                                                      geo.n_lines, f.f32, f.bf16, S);
         OM_COUNT_LAUNCH();
     }
     return cudaGetLastError();
@@ -553,7 +613,7 @@ cudaError_t anchor_build(Geometry &geo, const Field &f, int method, bool bf16, l
     Sink S{};
     S.flag = A->flag;
     bool marked = false;
-    if (method == OMNI3D_METHOD_SELECT) {
+    if (method_accum(method) == kAccSelect) {
         // cheap superset of the segment starts; used when it stays small
         AN_TRY(grow(A->cnt64, cap[8], sizeof(unsigned long long) * 1));
         unsigned long long *dcount = A->cnt64;
@@ -624,7 +684,7 @@ cudaError_t anchor_build(Geometry &geo, const Field &f, int method, bool bf16, l
     S.b = A->b;
     S.c = A->c;
     AN_TRY(run_pass<kFill>(geo, f, method, bf16, S, st));
-    A->unit_weights = method == OMNI3D_METHOD_PLAIN;
+    A->unit_weights = method_accum(method) == kAccPlain || method_accum(method) == kAccPlainNoEntry;
     return cudaGetLastError();
 }
 
@@ -653,7 +713,7 @@ cudaError_t anchor_mark(const Geometry &geo, const Field &f, int method, bool bf
     const long long V = geo.grid.V;
     cudaError_t e;
     bool marked = false;
-    if (method == OMNI3D_METHOD_SELECT) {
+    if (method_accum(method) == kAccSelect) {
         e = cudaMemsetAsync(count1, 0, sizeof(unsigned long long), st);
         if (e != cudaSuccess) return e;
         k_select_candidates<<<grid_for(V), 256, 0, st>>>(geo.grid, f.curl, flag, count1);

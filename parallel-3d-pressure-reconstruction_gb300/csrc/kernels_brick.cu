@@ -700,6 +700,19 @@ __global__ void __launch_bounds__(256) k_line_carry(long long n_lines, const uin
     }
 }
 
+// The brick passes implement the three accumulations; the fixed-boundary variants use
+// their base method's on their own staircases.  -1: not available (minimum-curl walks
+// change with every field, so their segments cannot be cached).
+int brick_method(int method)
+{
+    switch (method_accum(method)) {
+    case kAccPlain: return OMNI3D_METHOD_PLAIN;
+    case kAccSelect: return OMNI3D_METHOD_SELECT;
+    case kAccWeighted: return OMNI3D_METHOD_WEIGHTED;
+    default: return -1;
+    }
+}
+
 size_t summary_bytes(int method)
 {
     return method == OMNI3D_METHOD_SELECT ? 48 : (method == OMNI3D_METHOD_WEIGHTED ? 16 : 4);
@@ -869,6 +882,8 @@ cudaError_t brick_prepare(const Geometry &geo, Bricks *B, const Field &f, int me
     };
     if (!B->built) return fail(cudaErrorInvalidValue, "bricks not built");
     if (!f.f32) return fail(cudaErrorInvalidValue, "brick engine needs the FP32 field");
+    method = brick_method(method);
+    if (method < 0) return fail(cudaErrorNotSupported, "the brick engine does not take minimum-curl walks");
     const Grid &g = geo.grid;
     // tensor map of the float4 field: dims (4 floats, X, Y, Z), box (4, 18, 18, 18)
     if (B->map_for != f.f32) {
@@ -931,6 +946,7 @@ cudaError_t brick_prepare(const Geometry &geo, Bricks *B, const Field &f, int me
 
 cudaError_t brick_sweep(const Geometry &geo, Bricks *B, int method, const float *p, float2 *pncnt, cudaStream_t st)
 {
+    method = brick_method(method);
     if (!B->built || B->prepared_method != method || !p || !pncnt || (B->n_segs > 0 && (!B->summ || !B->carry)))
         return cudaErrorInvalidValue;
     if (B->n_items == 0) return cudaSuccess;

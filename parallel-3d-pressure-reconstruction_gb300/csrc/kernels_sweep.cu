@@ -74,7 +74,8 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x)
 }
 
 // Plain method: every voxel of the line, the entry included, receives p[entry] + I(v).
-template <bool BF16>
+// SELF = false leaves the entry out (the minimum-curl plain variant, K:2797-2936).
+template <bool BF16, bool SELF>
 __global__ void __launch_bounds__(256, 6) k_sweep_plain(Grid g, const LineRec *__restrict__ lines,
                                                      const uint32_t *__restrict__ gbase,
                                                      const uint32_t *__restrict__ desc, long long n_lines,
@@ -88,7 +89,7 @@ __global__ void __launch_bounds__(256, 6) k_sweep_plain(Grid g, const LineRec *_
     LineWalk L;
     L.init(g, r, gbase, desc, li);
     const float pe = __ldg(p + r.e);
-    atomicAdd(pncnt + r.e, make_float2(pe, 1.0f));
+    if (SELF) atomicAdd(pncnt + r.e, make_float2(pe, 1.0f));
     float4 gl = load_grad<BF16>(f32, b16, L.v);
     float I = 0.0f, comp = 0.0f;
     for (int s0 = 0; s0 < L.m; s0 += 16) {
@@ -143,6 +144,50 @@ __global__ void __launch_bounds__(256, 6) k_sweep_weighted(Grid g, const LineRec
                 float wc = __frcp_rn(csum) * nseg;
                 atomicAdd(pncnt + L.v, make_float2((pe + I) * wc, wc));
             }
+            gl = gv;
+        }
+    }
+}
+
+// Weighted method with raw curl sums (the minimum-curl variant, K:2937-3085): the sum starts
+// at the entry's curl and the entry receives (p[entry], 1) / C; step s adds its curl (not
+// divided by 1e4) and contributes w (p[entry] + I), w = (s + 1) / C, with no test for a zero
+// sum: a zero sum gives infinities, as in the reference.
+template <bool BF16>
+__global__ void __launch_bounds__(256, 6) k_sweep_weighted_raw(Grid g, const LineRec *__restrict__ lines,
+                                                            const uint32_t *__restrict__ gbase,
+                                                            const uint32_t *__restrict__ desc, long long n_lines,
+                                                            const float4 *__restrict__ f32,
+                                                            const uint2 *__restrict__ b16,
+                                                            const float *__restrict__ curl,
+                                                            const float *__restrict__ p, float2 *pncnt)
+{
+    long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= n_lines) return;
+    LineRec r = lines[li];
+    LineWalk L;
+    L.init(g, r, gbase, desc, li);
+    const float pe = __ldg(p + r.e);
+    float4 gl = load_grad<BF16>(f32, b16, L.v);
+    float csum = BF16 ? __ldg(curl + L.v) : gl.w, nseg = 1.0f;
+    {
+        const float w0 = __frcp_rn(csum);
+        atomicAdd(pncnt + L.v, make_float2(pe * w0, w0));
+    }
+    float I = 0.0f, comp = 0.0f;
+    for (int s0 = 0; s0 < L.m; s0 += 16) {
+        uint32_t w = __ldg(L.dp + 32 * (s0 >> 4));
+        int n = min(16, L.m - s0);
+        for (int t = 0; t < n; t++, w >>= 2) {
+            int a = (int)(w & 3u);
+            L.v += a == 0 ? L.d0 : (a == 1 ? L.d1 : L.d2);
+            float4 gv = load_grad<BF16>(f32, b16, L.v);
+            float cn = BF16 ? __ldg(curl + L.v) : gv.w;
+            kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
+            csum += cn;
+            nseg += 1.0f;
+            const float wc = __frcp_rn(csum) * nseg;
+            atomicAdd(pncnt + L.v, make_float2((pe + I) * wc, wc));
             gl = gv;
         }
     }
@@ -352,7 +397,8 @@ cudaError_t sweep_full(const Geometry &geo, const Field &f, int method, bool bf1
         (method_uses_curl(method) && !f.curl))
         return cudaErrorInvalidValue;
     unsigned blocks = (unsigned)((geo.n_lines + 255) / 256);
-    if (method == OMNI3D_METHOD_WEIGHTED) {
+    const int acc = method_accum(method);
+    if (acc == kAccWeighted) {
         if (bf16)
             k_sweep_weighted<true><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
                                                            geo.n_lines, f.f32, f.bf16, f.curl, p, pncnt);
@@ -360,7 +406,15 @@ cudaError_t sweep_full(const Geometry &geo, const Field &f, int method, bool bf1
             k_sweep_weighted<false><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
                                                             geo.n_lines, f.f32, f.bf16, f.curl, p, pncnt);
         OM_COUNT_LAUNCH();
-    } else if (method == OMNI3D_METHOD_SELECT) {
+    } else if (acc == kAccWeightedRawCurl) {
+        if (bf16)
+            k_sweep_weighted_raw<true><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
+                                                               geo.n_lines, f.f32, f.bf16, f.curl, p, pncnt);
+        else
+            k_sweep_weighted_raw<false><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
+                                                                geo.n_lines, f.f32, f.bf16, f.curl, p, pncnt);
+        OM_COUNT_LAUNCH();
+    } else if (acc == kAccSelect) {
         if (bf16)
             k_sweep_select<true><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
                                                          f.f32, f.bf16, f.curl, p, pncnt);
@@ -368,13 +422,21 @@ cudaError_t sweep_full(const Geometry &geo, const Field &f, int method, bool bf1
             k_sweep_select<false><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
                                                           f.f32, f.bf16, f.curl, p, pncnt);
         OM_COUNT_LAUNCH();
+    } else if (acc == kAccPlainNoEntry) {
+        if (bf16)
+            k_sweep_plain<true, false><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
+                                                               geo.n_lines, f.f32, f.bf16, p, pncnt);
+        else
+            k_sweep_plain<false, false><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
+                                                                geo.n_lines, f.f32, f.bf16, p, pncnt);
+        OM_COUNT_LAUNCH();
     } else {
         if (bf16)
-            k_sweep_plain<true><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
-                                                        f.f32, f.bf16, p, pncnt);
+            k_sweep_plain<true, true><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
+                                                              geo.n_lines, f.f32, f.bf16, p, pncnt);
         else
-            k_sweep_plain<false><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
-                                                         f.f32, f.bf16, p, pncnt);
+            k_sweep_plain<false, true><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
+                                                               geo.n_lines, f.f32, f.bf16, p, pncnt);
         OM_COUNT_LAUNCH();
     }
     return cudaGetLastError();

@@ -112,11 +112,17 @@ __global__ void k_group_words(const LineRec *lines, long long n_lines, long long
     if ((threadIdx.x & 31) == 0) gw[li >> 5] = (uint32_t)((mx + 15) >> 4);
 }
 
-// Walk every line once (K:1762-1861) and store its staircase, 2 bits per step.
+// Walk every line once (K:1762-1861) and store its staircase, 2 bits per step.  RULE is
+// the walk rule of OmWalker::step; rule 3 reads `curl`.  The full path length
+// |di| + |dj| + |dk| bounds every walk (each step moves one axis toward the exit), so a
+// re-walk with another field fits the words reserved for the line.  counters[0] counts
+// walks that stopped early under rule 0 (the reference's "Wrong Point" error; under the
+// other rules stopping early is their design), counters[1] the voxel visits.
+template <int RULE>
 __global__ void __launch_bounds__(256) k_walk(Grid g, const DirEntry *dirs, LineRec *lines,
                                               const float4 *off, const uint32_t *gbase,
                                               uint32_t *desc, long long n_lines,
-                                              unsigned long long *counters)
+                                              unsigned long long *counters, const float *curl)
 {
     long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned mask = __ballot_sync(0xffffffffu, li < n_lines);
@@ -131,17 +137,16 @@ __global__ void __launch_bounds__(256) k_walk(Grid g, const DirEntry *dirs, Line
     uint32_t *dp = desc + 32ull * gbase[li >> 5] + (li & 31);
     uint32_t word = 0;
     int s = 0;
-    for (; s < r.m; s++) {
-        int a = w.step();
+    const int m = abs(ix - ie) + abs(jx - je) + abs(kx - ke);
+    for (; s < m; s++) {
+        int a = w.step<RULE>(curl, g.X, g.XY, g.V);
         if (a < 0) break;
         word |= (uint32_t)a << (2 * (s & 15));
         if ((s & 15) == 15) { dp[32 * (s >> 4)] = word; word = 0; }
     }
     if (s & 15) dp[32 * (s >> 4)] = word;
-    if (s != r.m) {
-        lines[li].m = s;  // the reference keeps the contributions of the steps taken
-        atomicAdd(&counters[0], 1ull);
-    }
+    if (s != r.m) lines[li].m = s;  // the reference keeps the contributions of the steps taken
+    if (s != m && RULE == 0) atomicAdd(&counters[0], 1ull);
     // voxel-direction updates: entry + one per step
     unsigned u = __reduce_add_sync(mask, (unsigned)(s + 1));
     if ((threadIdx.x & 31) == (__ffs(mask) - 1)) atomicAdd(&counters[1], (unsigned long long)u);
@@ -316,6 +321,8 @@ void free_geometry(Geometry *g)
 {
     cudaFree(g->d_lines_through);
     g->d_lines_through = nullptr;
+    cudaFree(g->d_counters);
+    g->d_counters = nullptr;
     cudaFree(g->d_off);
     cudaFree(g->d_lines);
     cudaFree(g->d_gbase);
@@ -390,19 +397,42 @@ cudaError_t build_geometry(Geometry *g, cudaStream_t st, std::string *err)
     g->n_words = 32LL * words_per_lane_total;
     OM_TRY(cudaMalloc(&g->d_desc, sizeof(uint32_t) * (size_t)std::max(g->n_words, 1LL)));
 
-    unsigned long long *d_err = nullptr;
-    OM_TRY(cudaMalloc(&d_err, 2 * sizeof(unsigned long long)));
-    OM_TRY(cudaMemsetAsync(d_err, 0, 2 * sizeof(unsigned long long), st));
-    k_walk<<<(unsigned)((g->n_lines + 255) / 256), 256, 0, st>>>(G, g->d_dirs, g->d_lines, g->d_off,
-                                                                 g->d_gbase, g->d_desc, g->n_lines, d_err);
+    OM_TRY(cudaMalloc(&g->d_counters, 2 * sizeof(unsigned long long)));
+    // the minimum-curl rule needs a field: its geometry starts from the nearest-candidate
+    // walk and is re-walked per field (rewalk_min_curl)
+    return run_walk(g, g->walk_rule == 3 ? 0 : g->walk_rule, nullptr, st);
+}
+
+cudaError_t run_walk(Geometry *g, int rule, const float *curl, cudaStream_t st)
+{
+    if (g->n_lines == 0) return cudaSuccess;
+    if (!g->d_counters || !g->d_lines || !g->d_desc || (rule == 3 && !curl)) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(g->d_counters, 0, 2 * sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+    const unsigned blocks = (unsigned)((g->n_lines + 255) / 256);
+    const Grid &G = g->grid;
+    switch (rule) {
+    case 1: k_walk<1><<<blocks, 256, 0, st>>>(G, g->d_dirs, g->d_lines, g->d_off, g->d_gbase, g->d_desc, g->n_lines,
+                                              g->d_counters, curl); break;
+    case 2: k_walk<2><<<blocks, 256, 0, st>>>(G, g->d_dirs, g->d_lines, g->d_off, g->d_gbase, g->d_desc, g->n_lines,
+                                              g->d_counters, curl); break;
+    case 3: k_walk<3><<<blocks, 256, 0, st>>>(G, g->d_dirs, g->d_lines, g->d_off, g->d_gbase, g->d_desc, g->n_lines,
+                                              g->d_counters, curl); break;
+    default: k_walk<0><<<blocks, 256, 0, st>>>(G, g->d_dirs, g->d_lines, g->d_off, g->d_gbase, g->d_desc, g->n_lines,
+                                               g->d_counters, curl); break;
+    }
     OM_COUNT_LAUNCH();
-    OM_TRY(cudaGetLastError());
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
     unsigned long long herr[2] = {0, 0};
-    OM_TRY(cudaMemcpyAsync(herr, d_err, sizeof(herr), cudaMemcpyDeviceToHost, st));
-    OM_TRY(cudaStreamSynchronize(st));
-    cudaFree(d_err);
+    if ((e = cudaMemcpyAsync(herr, g->d_counters, sizeof(herr), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess)
+        return e;
     g->walk_errors = (long long)herr[0];
     g->n_units = (long long)herr[1];
+    // anything derived from the staircases is stale
+    cudaFree(g->d_lines_through);
+    g->d_lines_through = nullptr;
+    g->walk_generation++;
     return cudaSuccess;
 }
 

@@ -79,6 +79,8 @@ extern "C" int omni3d_sweep_noalloc(omni3d_ctx *ctx, const float *ax, const floa
         return fail(OMNI3D_ERR_ARG, "the selected and weighted methods need curl");
     if (P->grad_storage != OMNI3D_GRAD_F32)
         return fail(OMNI3D_ERR_STATE, "omni3d_sweep_noalloc supports FP32 gradient storage only");
+    if (method_walk_rule(P->method) == 3)
+        return fail(OMNI3D_ERR_STATE, "omni3d_sweep_noalloc does not re-walk the minimum-curl paths per field");
     if (geo->grid.V > kMaxVoxels)
         return fail(OMNI3D_ERR_RANGE, "omni3d_sweep_noalloc: " + std::to_string(geo->grid.V) +
                                           " voxels exceed its static scratch of OMNI3D_NOALLOC_MAX_VOXELS = " +

@@ -58,6 +58,9 @@ struct Geometry {
     uint32_t *d_gbase = nullptr;    // n_groups + 1 prefix sums of words per lane
     uint32_t *d_desc = nullptr;
     uint32_t *d_lines_through = nullptr;  // per voxel: lines through it (built on first use)
+    unsigned long long *d_counters = nullptr;  // walk counters (early stops, voxel visits)
+    int walk_rule = 0;              // OmWalker rule of the staircases (3: per field, minimum curl)
+    long long walk_generation = 0;  // incremented by every walk
     long long n_lines = 0, n_groups = 0, n_words = 0;
     long long n_units = 0;          // sum over lines of (steps + 1)
     long long walk_errors = 0;
@@ -70,6 +73,9 @@ struct Geometry {
 // g->d_off, g->d_lines, g->d_gbase, g->d_desc; walks every line.  Synchronises `st`.
 cudaError_t build_geometry(Geometry *g, cudaStream_t st, std::string *err);
 void free_geometry(Geometry *g);
+// (Re)walk every line with walk rule `rule` (curl: the field for rule 3).  Synchronises st,
+// updates n_units / walk_errors and drops d_lines_through.
+cudaError_t run_walk(Geometry *g, int rule, const float *curl, cudaStream_t st);
 // Count the lines through every voxel into g->d_lines_through (once per geometry).
 cudaError_t ensure_lines_through(Geometry *g, cudaStream_t st);
 
@@ -132,10 +138,35 @@ cudaError_t curl_field(const Grid &g, const float *ax, const float *ay, const fl
                        const float *mask, float *out, cudaStream_t st);
 
 // One full sweep: pncnt[v] += (sum of contributions, sum of weights) over all lines.
-// The selected and weighted methods read the curl indicator; the plain method does not.
-inline bool method_uses_curl(int method)
+// Every method but the plain one reads the curl indicator.
+inline bool method_uses_curl(int method) { return method != OMNI3D_METHOD_PLAIN; }
+
+// Walk rule of a method (OmWalker::step): 1 and 2 the fixed-boundary walks, 3 the
+// minimum-curl walk (re-walked per field), 0 the nearest-candidate walk.
+inline int method_walk_rule(int method)
 {
-    return method == OMNI3D_METHOD_SELECT || method == OMNI3D_METHOD_WEIGHTED;
+    switch (method) {
+    case OMNI3D_METHOD_WEIGHTED_FIXED_BC: return 1;
+    case OMNI3D_METHOD_SELECT_FIXED_BC: return 2;
+    case OMNI3D_METHOD_MINI_CURL:
+    case OMNI3D_METHOD_WEIGHTED_MINI_CURL: return 3;
+    default: return 0;
+    }
+}
+
+// The accumulation along a line of a method: the variants share their base method's.
+enum Accum { kAccPlain = 0, kAccSelect = 1, kAccWeighted = 2, kAccPlainNoEntry = 3, kAccWeightedRawCurl = 4 };
+inline int method_accum(int method)
+{
+    switch (method) {
+    case OMNI3D_METHOD_SELECT:
+    case OMNI3D_METHOD_SELECT_FIXED_BC: return kAccSelect;
+    case OMNI3D_METHOD_WEIGHTED:
+    case OMNI3D_METHOD_WEIGHTED_FIXED_BC: return kAccWeighted;
+    case OMNI3D_METHOD_MINI_CURL: return kAccPlainNoEntry;
+    case OMNI3D_METHOD_WEIGHTED_MINI_CURL: return kAccWeightedRawCurl;
+    default: return kAccPlain;
+    }
 }
 
 // method: OMNI3D_METHOD_*; p is read at line entries / segment starts.

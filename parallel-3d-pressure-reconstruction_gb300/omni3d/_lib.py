@@ -19,6 +19,7 @@ ERR_RANGE = -6
 ERR_NUMERIC = -7
 
 METHOD_PLAIN, METHOD_SELECT, METHOD_WEIGHTED = 0, 1, 2
+METHOD_WEIGHTED_FIXED_BC, METHOD_SELECT_FIXED_BC, METHOD_MINI_CURL, METHOD_WEIGHTED_MINI_CURL = 3, 4, 5, 6
 ENGINE_AUTO, ENGINE_LINES, ENGINE_BRICKS = 0, 1, 2
 SOLVER_ANCHOR, SOLVER_SWEEP = 0, 1
 GRAD_F32, GRAD_BF16 = 0, 1

@@ -14,7 +14,9 @@ import numpy as np
 from . import _lib as L
 from ._lib import check, lib
 
-_METHODS = {"plain": L.METHOD_PLAIN, "select": L.METHOD_SELECT, "weighted": L.METHOD_WEIGHTED}
+_METHODS = {"plain": L.METHOD_PLAIN, "select": L.METHOD_SELECT, "weighted": L.METHOD_WEIGHTED,
+            "weighted_fixed_bc": L.METHOD_WEIGHTED_FIXED_BC, "select_fixed_bc": L.METHOD_SELECT_FIXED_BC,
+            "mini_curl": L.METHOD_MINI_CURL, "weighted_mini_curl": L.METHOD_WEIGHTED_MINI_CURL}
 _SOLVERS = {"anchor": L.SOLVER_ANCHOR, "sweep": L.SOLVER_SWEEP}
 _ENGINES = {"auto": L.ENGINE_AUTO, "lines": L.ENGINE_LINES, "bricks": L.ENGINE_BRICKS}
 _GRADS = {"f32": L.GRAD_F32, "bf16": L.GRAD_BF16}
