@@ -75,6 +75,10 @@ extern "C" {
 #define OMNI3D_ENGINE_BRICKS 2  /* lines cut into 16^3-brick segments; each brick's field is
                                    staged in shared memory by TMA and its sums kept there */
 
+/* Initial state of a solve when p_init is NULL. */
+#define OMNI3D_INIT_ZERO 0      /* zero, as when main() is given no Bernoulli face */
+#define OMNI3D_INIT_CENTRE 1    /* omni3d_centre_integration (initialIntegration.cpp) */
+
 /* Gauge applied to the output (the reference applies none; K:8879-8915 is commented out). */
 #define OMNI3D_GAUGE_NONE 0
 #define OMNI3D_GAUGE_POINT 1    /* p -= p(ref voxel) */
@@ -107,6 +111,7 @@ typedef struct {
                                   to the sweep form (0: what 80 % of the free device memory
                                   holds) */
     int engine;                /* OMNI3D_ENGINE_* */
+    int initial_guess;         /* OMNI3D_INIT_*: the initial state when p_init is NULL */
 } omni3d_params;
 
 typedef struct {
@@ -140,6 +145,17 @@ int omni3d_create(const omni3d_params *params, omni3d_ctx **out);
 int omni3d_destroy(omni3d_ctx *ctx);
 const char *omni3d_last_error(const omni3d_ctx *ctx);
 const char *omni3d_global_error(void);
+
+/* The reference's initial guess by integration outward from the centre voxel,
+ * initialIntegration.cpp:9-407 (uncalled by its main()): eight octant sweeps from
+ * (nx/2, ny/2, nz/2); each voxel is the mean over its off-centre axes of the neighbour one
+ * step nearer the centre plus the trapezoid increment -rho * a * spacing.  FP64 on the
+ * device (wavefronts of equal distance from the centre), returned as float; bit-identical
+ * to the reference's double result rounded to float.  The centre voxel is 0.  pref is
+ * written to voxel 0 before the sweeps, as the reference does, and overwritten by them, so
+ * it does not change the result (kept for the reference's signature). */
+int omni3d_centre_integration(omni3d_ctx *ctx, const float *ax, const float *ay, const float *az,
+                              double pref, float *p_out, int device_ptrs);
 
 /* Use this CUDA stream (cudaStream_t passed as void*) for all later work on ctx. */
 int omni3d_set_stream(omni3d_ctx *ctx, void *stream);

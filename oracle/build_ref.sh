@@ -4,7 +4,8 @@
 #
 #   stage  (needs the reference tree, default /root/reference; REF_ROOT overrides):
 #          copies the reference functions on the hot path, by line range, from
-#          Omni3D_8.0/Omni3D_8.0/kernel.cu, plus sor3D.cpp and calRHS.cpp, into
+#          Omni3D_8.0/Omni3D_8.0/kernel.cu, plus sor3D.cpp, calRHS.cpp and
+#          initialIntegration.cpp, into
 #          oracle/_ref/src/ (git-ignored build intermediates, never committed).
 #   build  compiles oracle/_ref/src/* with oracle/ref_driver.cpp into
 #          oracle/_ref/libomni_ref.so.  Runs wherever oracle/_ref/src exists, so a
@@ -51,6 +52,8 @@ stage() {
     tr -d '\r' < "$K/sor3D.h" > "$SRC/sor3D.h"
     tr -d '\r' < "$K/calRHS.cpp" | sed '10d' > "$SRC/calRHS.cpp"
     tr -d '\r' < "$K/calRHS.h" > "$SRC/calRHS.h"
+    tr -d '\r' < "$K/initialIntegration.cpp" > "$SRC/initialIntegration.cpp"
+    tr -d '\r' < "$K/initialIntegration.h" > "$SRC/initialIntegration.h"
     printf '#include <cstring>\n#include <cstdlib>\n#include <cmath>\n' > "$SRC/stub/afx.h"
     # the staged files must still hold the functions the driver binds
     grep -q 'bool cross2point' "$SRC/ref_kernel_extract.cpp"
@@ -75,9 +78,10 @@ build() {
     "$CXX" $FLAGS -c "$SRC/ref_kernel_extract.cpp" -o "$OUT/ref_kernel_extract.o"
     "$CXX" $FLAGS -I"$SRC/stub" -I"$SRC" -c "$SRC/sor3D.cpp" -o "$OUT/sor3D.o"
     "$CXX" $FLAGS -I"$SRC/stub" -I"$SRC" -c "$SRC/calRHS.cpp" -o "$OUT/calRHS.o"
+    "$CXX" $FLAGS -I"$SRC/stub" -I"$SRC" -c "$SRC/initialIntegration.cpp" -o "$OUT/initialIntegration.o"
     "$CXX" $FLAGS -Wall -c "$HERE/ref_driver.cpp" -o "$OUT/ref_driver.o"
     "$CXX" -shared -fopenmp -o "$OUT/libomni_ref.so" "$OUT/ref_driver.o" "$OUT/ref_kernel_extract.o" \
-        "$OUT/sor3D.o" "$OUT/calRHS.o"
+        "$OUT/sor3D.o" "$OUT/calRHS.o" "$OUT/initialIntegration.o"
     echo "built $OUT/libomni_ref.so"
 }
 

@@ -921,3 +921,58 @@ void orc_adjoint_f64(const orc_problem *P, int niter, const double *g, double *g
     free(mu);
     free(macc);
 }
+
+/* ------------------------------------------------------------------------------------ */
+/* initial guess by integration outward from the centre (initialIntegration.cpp:9-407)   */
+/* ------------------------------------------------------------------------------------ */
+
+/* The eight octant sweeps of initialIntegration.cpp in its order (No.1-No.8): from the
+ * centre voxel (X/2, Y/2, Z/2) outward, each voxel takes the mean over its off-centre axes,
+ * in x, y, z order, of (the neighbour one step nearer the centre) + or - rho * 0.5 *
+ * (a[voxel] + a[neighbour]) * spacing (+ when the voxel lies on the low side of the
+ * centre along that axis).  The centre keeps its initial value; p[0] = pref is written
+ * first (initialIntegration.cpp:12-13) and then overwritten by the first octant.
+ * Double precision throughout, as the reference. */
+void orc_centre_integration(long X, long Y, long Z, double dx, double dy, double dz, double rho,
+                            const double *au, const double *av, const double *aw, double pref,
+                            double *p)
+{
+    const long XY = X * Y;
+    const long cx = X / 2, cy = Y / 2, cz = Z / 2;
+    memset(p, 0, sizeof(double) * (size_t)(X * Y * Z));
+    p[0] = pref;
+    const int order[8][3] = {{-1, -1, -1}, {1, -1, -1}, {-1, 1, -1}, {1, 1, -1},
+                             {-1, -1, 1},  {1, -1, 1},  {-1, 1, 1},  {1, 1, 1}};
+    for (int o = 0; o < 8; o++) {
+        const int sx = order[o][0], sy = order[o][1], sz = order[o][2];
+        for (long k = cz; k >= 0 && k < Z; k += sz)
+            for (long j = cy; j >= 0 && j < Y; j += sy)
+                for (long i = cx; i >= 0 && i < X; i += sx) {
+                    const long ind = i + j * X + k * XY;
+                    int n = 0;
+                    double v = 0.0;
+                    if (i != cx) {
+                        const long nb = ind - sx;
+                        const double t = 0.5 * (au[ind] + au[nb]) * dx * rho;
+                        v = sx < 0 ? p[nb] + t : p[nb] - t;
+                        n++;
+                    }
+                    if (j != cy) {
+                        const long nb = ind - sy * X;
+                        const double t = 0.5 * (av[ind] + av[nb]) * dy * rho;
+                        const double w = sy < 0 ? p[nb] + t : p[nb] - t;
+                        v = n ? v + w : w;
+                        n++;
+                    }
+                    if (k != cz) {
+                        const long nb = ind - sz * XY;
+                        const double t = 0.5 * (aw[ind] + aw[nb]) * dz * rho;
+                        const double w = sz < 0 ? p[nb] + t : p[nb] - t;
+                        v = n ? v + w : w;
+                        n++;
+                    }
+                    if (n == 0) continue;  /* the centre */
+                    p[ind] = n == 1 ? v : (n == 2 ? v / 2.0 : v / 3.0);
+                }
+    }
+}

@@ -113,6 +113,8 @@ class Oracle:
         L.orc_calindex.argtypes = [_l, _l, _l, _lp]
         L.orc_curl.argtypes = [_l, _l, _l, _f, _f, _f, _fp, _fp, _fp, _fp, _fp]
         L.orc_num_threads.restype = _i
+        L.orc_centre_integration.argtypes = [_l, _l, _l, C.c_double, C.c_double, C.c_double, C.c_double, _dp, _dp,
+                                             _dp, C.c_double, _dp]
 
     # -- geometry ----------------------------------------------------------------------
     def nogrid(self, dims, ls, cpu_twin=False) -> int:
@@ -234,6 +236,17 @@ class Oracle:
                           _ptr(out, C.c_float))
         return out
 
+    def centre_integration(self, dims, spacing, au, av, aw, *, rho=1.0, pref=0.0) -> np.ndarray:
+        """initialIntegration.cpp restated: FP64 p integrated outward from the centre voxel."""
+        X, Y, Z = dims
+        f = lambda a: np.ascontiguousarray(np.asarray(a, np.float64).reshape(-1))
+        au, av, aw = f(au), f(av), f(aw)
+        out = np.zeros(X * Y * Z, np.float64)
+        self.lib.orc_centre_integration(X, Y, Z, float(spacing[0]), float(spacing[1]), float(spacing[2]), float(rho),
+                                        _ptr(au, C.c_double), _ptr(av, C.c_double), _ptr(aw, C.c_double),
+                                        float(pref), _ptr(out, C.c_double))
+        return out
+
     def num_threads(self) -> int:
         return self.lib.orc_num_threads()
 
@@ -261,6 +274,7 @@ class RefLib:
         L.ref_sor.argtypes = [_i, _i, _i, _d, _d, _d, _d, _dp, _dp, _dp, _i, _d, _dp]
         L.ref_calrhs.argtypes = [_i, _i, _i, _d, _d, _d, _d, _dp, _dp, _dp, _dp]
         L.ref_num_threads.restype = _i
+        L.ref_initial_integration.argtypes = [C.c_long, C.c_long, C.c_long, _d, _d, _d, _d, _dp, _dp, _dp, _d, _dp]
 
     @staticmethod
     def _f(a):
@@ -357,6 +371,16 @@ class RefLib:
         p = np.zeros(X * Y * Z, np.float64)
         self.lib.ref_sor(X, Y, Z, spacing[0], spacing[1], spacing[2], rho, _ptr(au, C.c_double),
                          _ptr(av, C.c_double), _ptr(aw, C.c_double), int(niter), float(eps), _ptr(p, C.c_double))
+        return p
+
+    def initial_integration(self, dims, spacing, au, av, aw, *, rho=1.0, pref=0.0) -> np.ndarray:
+        """The reference's initialIntegration (initialIntegration.cpp) on zeroed buffers."""
+        X, Y, Z = dims
+        g = lambda a: np.ascontiguousarray(np.asarray(a, np.float64).reshape(-1))
+        au, av, aw = g(au), g(av), g(aw)
+        p = np.zeros(X * Y * Z, np.float64)
+        self.lib.ref_initial_integration(X, Y, Z, spacing[0], spacing[1], spacing[2], rho, _ptr(au, C.c_double),
+                                         _ptr(av, C.c_double), _ptr(aw, C.c_double), float(pref), _ptr(p, C.c_double))
         return p
 
     def num_threads(self) -> int:

@@ -58,6 +58,9 @@ float bodyIntegralInnerSelectFixedBC(long Xsize, long Ysize, long Zsize, int iin
                               float k2, float k3, float deltx, float delty, float deltz,
                               float density, float *DuDt, float *DvDt, float *DwDt, float *p,
                               float *pn, float *curl, float *pcountinner, float threshold);
+extern "C" void initialIntegration(long Xsize, long Ysize, long Zsize, double deltx, double delty, double deltz,
+                                   double density, double *DuDt, double *DvDt, double *DwDt, double pref,
+                                   double *p, double *pn, double *pBC);
 void calIndex(long *index, long Xsize, long Ysize, long Zsize);
 void omni3dparallellinesESInnerCPU(long Xsize, long Ysize, long Zsize, int NoAngles,
                                    float linespacing, float *k1_d, float *k2_d, float *k3_d,
@@ -298,3 +301,12 @@ int ref_num_threads(void)
 }
 
 }  // extern "C"
+
+// initialIntegration.cpp on zeroed p / pn buffers (the reference leaves them to the caller).
+extern "C" void ref_initial_integration(long X, long Y, long Z, double dx, double dy, double dz, double rho,
+                                        double *au, double *av, double *aw, double pref, double *p)
+{
+    std::vector<double> pn((size_t)(X * Y * Z), 0.0), bc((size_t)(X * Y * Z), 0.0);
+    std::fill(p, p + X * Y * Z, 0.0);
+    initialIntegration(X, Y, Z, dx, dy, dz, rho, au, av, aw, pref, p, pn.data(), bc.data());
+}

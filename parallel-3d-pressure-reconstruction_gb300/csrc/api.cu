@@ -65,6 +65,7 @@ struct omni3d_ctx {
     DeviceBuf pvol_a, pvol_b, pout, cnt, pncnt, scratch, flags;
     Anchor anc;
     bool anc_cached = false;  // plain method: operator structure built for this geometry
+    DeviceBuf centre;         // FP64 scratch of the centre integration
     Bricks bricks;            // brick segments of the geometry (built on first use)
     bool bricks_failed = false;
     std::string bricks_why;
@@ -182,6 +183,10 @@ int check_params(const omni3d_params *p, std::string *why)
     if (!(p->tol >= 0.0)) { *why = "tol must be >= 0"; return OMNI3D_ERR_ARG; }
     if (p->anchor_max_links < 0) { *why = "anchor_max_links must be >= 0"; return OMNI3D_ERR_ARG; }
     if (p->engine < OMNI3D_ENGINE_AUTO || p->engine > OMNI3D_ENGINE_BRICKS) { *why = "unknown engine"; return OMNI3D_ERR_ARG; }
+    if (p->initial_guess != OMNI3D_INIT_ZERO && p->initial_guess != OMNI3D_INIT_CENTRE) {
+        *why = "unknown initial_guess";
+        return OMNI3D_ERR_ARG;
+    }
     double ng = std::max(std::max(p->nx, p->ny), p->nz) * 1.732 / (double)p->line_spacing;
     if (ng * ng * (double)p->n_dirs / 256.0 > 2.0e9) { *why = "too many lines (lattice x directions)"; return OMNI3D_ERR_RANGE; }
     return OMNI3D_OK;
@@ -492,7 +497,7 @@ int omni3d_destroy(omni3d_ctx *ctx)
     ctx->adj_out.release();
     for (DeviceBuf *b : {&ctx->in_ax, &ctx->in_ay, &ctx->in_az, &ctx->in_aux, &ctx->in_pinit, &ctx->f32, &ctx->b16,
                          &ctx->curl, &ctx->pvol_a, &ctx->pvol_b, &ctx->pout, &ctx->cnt, &ctx->pncnt, &ctx->scratch,
-                         &ctx->flags})
+                         &ctx->flags, &ctx->centre})
         b->release();
     for (auto &ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
@@ -605,6 +610,30 @@ int omni3d_curl(omni3d_ctx *ctx, const float *ax, const float *ay, const float *
     return OMNI3D_OK;
 }
 
+int omni3d_centre_integration(omni3d_ctx *ctx, const float *ax, const float *ay, const float *az, double pref,
+                              float *p_out, int device_ptrs)
+{
+    if (!ctx || !ax || !ay || !az || !p_out) return fail(ctx, OMNI3D_ERR_ARG, "NULL argument");
+    cudaSetDevice(ctx->prm.device);
+    const long long V = ctx->geo.grid.V;
+    const bool dev = device_ptrs != 0;
+    const float *dax, *day, *daz;
+    int rc;
+    if ((rc = stage(ctx, ax, dev, ctx->in_ax, V, &dax))) return rc;
+    if ((rc = stage(ctx, ay, dev, ctx->in_ay, V, &day))) return rc;
+    if ((rc = stage(ctx, az, dev, ctx->in_az, V, &daz))) return rc;
+    CK(ctx, ctx->centre.ensure(sizeof(double) * (size_t)V));
+    float *dout = p_out;
+    if (!dev) {
+        CK(ctx, ctx->pvol_a.ensure(sizeof(float) * (size_t)V));
+        dout = ctx->pvol_a.as<float>();
+    }
+    CK(ctx, centre_integration(ctx->geo.grid, dax, day, daz, 1, pref, ctx->centre.as<double>(), dout, ctx->st));
+    if (!dev) CK(ctx, cudaMemcpyAsync(p_out, dout, sizeof(float) * (size_t)V, cudaMemcpyDeviceToHost, ctx->st));
+    CK(ctx, cudaStreamSynchronize(ctx->st));
+    return OMNI3D_OK;
+}
+
 int omni3d_sweep(omni3d_ctx *ctx, const float *ax, const float *ay, const float *az, const float *curl, const float *p,
                  float *pn, float *count, int device_ptrs)
 {
@@ -680,7 +709,14 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
         if ((rc = stage(ctx, p_init, dev, ctx->in_pinit, V, &dpinit))) return rc;
     } else {
         CK(ctx, ctx->in_pinit.ensure(sizeof(float) * (size_t)V));
-        CK(ctx, cudaMemsetAsync(ctx->in_pinit.p, 0, sizeof(float) * (size_t)V, st));
+        if (P.initial_guess == OMNI3D_INIT_CENTRE) {  // initialIntegration.cpp from the packed field
+            CK(ctx, ctx->centre.ensure(sizeof(double) * (size_t)V));
+            const float *f = reinterpret_cast<const float *>(F.f32);
+            CK(ctx, centre_integration(g, f, f + 1, f + 2, 4, 0.0, ctx->centre.as<double>(), ctx->in_pinit.as<float>(),
+                                       st));
+        } else {
+            CK(ctx, cudaMemsetAsync(ctx->in_pinit.p, 0, sizeof(float) * (size_t)V, st));
+        }
         dpinit = ctx->in_pinit.as<float>();
     }
     CK(ctx, ctx->pncnt.ensure(sizeof(float2) * (size_t)V));

@@ -11,6 +11,8 @@
 // integral along the line is a compensated (Kahan) FP32 sum.
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 #include "omni3d_internal.h"
 
 namespace omni3d {
@@ -378,6 +380,61 @@ __global__ void k_shift(long long V, const double *sums, float *p)
 
 __global__ void k_read_point(const float *p, long long ref, double *out) { out[0] = (double)p[ref]; out[1] = 1.0; }
 
+// One wavefront of the centre integration (initialIntegration.cpp:9-407): every voxel at L1
+// distance L = a + b + c from the centre (X/2, Y/2, Z/2), thread (a, b) taking the up to
+// eight voxels (+-a, +-b, +-c).  A voxel's value is the mean over its off-centre axes, in
+// x, y, z order, of (the neighbour one step nearer the centre, at distance L - 1) + or -
+// rho * 0.5 * (a[voxel] + a[neighbour]) * spacing, + on the low side of the centre; FP64
+// with explicit rounding in the reference's C evaluation order.
+__global__ void k_centre_level(Grid g, int L, const float *__restrict__ au, const float *__restrict__ av,
+                               const float *__restrict__ aw, int stride, double *pn)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long w1 = (long long)L + 1;
+    if (t >= w1 * w1) return;
+    const int a = (int)(t / w1), b = (int)(t % w1);
+    if (a + b > L) return;
+    const int c = L - a - b;
+    const int cx = g.X / 2, cy = g.Y / 2, cz = g.Z / 2;
+    const double rho = (double)g.rho, dx = (double)g.dx, dy = (double)g.dy, dz = (double)g.dz;
+    for (int o = 0; o < 8; o++) {
+        const int sx = (o & 1) ? 1 : -1, sy = (o & 2) ? 1 : -1, sz = (o & 4) ? 1 : -1;
+        if ((a == 0 && sx > 0) || (b == 0 && sy > 0) || (c == 0 && sz > 0)) continue;  // each voxel once
+        const int i = cx + sx * a, j = cy + sy * b, k = cz + sz * c;
+        if (i < 0 || i >= g.X || j < 0 || j >= g.Y || k < 0 || k >= g.Z) continue;
+        const long long ind = i + (long long)j * g.X + (long long)k * g.XY;
+        double v = 0.0;
+        int n = 0;
+        if (a) {
+            const long long nb = ind - sx;
+            const double tr = __dmul_rn(__dmul_rn(__dmul_rn(0.5, __dadd_rn((double)au[ind * stride], (double)au[nb * stride])), dx), rho);
+            v = sx < 0 ? __dadd_rn(pn[nb], tr) : __dsub_rn(pn[nb], tr);
+            n = 1;
+        }
+        if (b) {
+            const long long nb = ind - (long long)sy * g.X;
+            const double tr = __dmul_rn(__dmul_rn(__dmul_rn(0.5, __dadd_rn((double)av[ind * stride], (double)av[nb * stride])), dy), rho);
+            const double w = sy < 0 ? __dadd_rn(pn[nb], tr) : __dsub_rn(pn[nb], tr);
+            v = n ? __dadd_rn(v, w) : w;
+            n++;
+        }
+        if (c) {
+            const long long nb = ind - (long long)sz * g.XY;
+            const double tr = __dmul_rn(__dmul_rn(__dmul_rn(0.5, __dadd_rn((double)aw[ind * stride], (double)aw[nb * stride])), dz), rho);
+            const double w = sz < 0 ? __dadd_rn(pn[nb], tr) : __dsub_rn(pn[nb], tr);
+            v = n ? __dadd_rn(v, w) : w;
+            n++;
+        }
+        pn[ind] = n == 1 ? v : __ddiv_rn(v, n == 2 ? 2.0 : 3.0);
+    }
+}
+
+__global__ void k_to_float(long long V, const double *__restrict__ in, float *out)
+{
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x)
+        out[v] = (float)in[v];
+}
+
 unsigned grid_for(long long n, int threads = 256)
 {
     long long b = (n + threads - 1) / threads;
@@ -499,5 +556,26 @@ cudaError_t apply_gauge(long long V, int gauge, long long ref, const float *cnt,
 }
 
 size_t gauge_scratch_doubles() { return 2 + 2 * kRedBlocks; }
+
+cudaError_t centre_integration(const Grid &g, const float *ax, const float *ay, const float *az, int stride,
+                               double pref, double *scratch, float *out, cudaStream_t st)
+{
+    if (!ax || !ay || !az || !scratch || !out) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(double) * (size_t)g.V, st);
+    if (e != cudaSuccess) return e;
+    // voxel 0 takes pref first, as in the reference; its own wavefront overwrites it
+    if ((e = cudaMemcpyAsync(scratch, &pref, sizeof(double), cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;  // pref is a host stack value
+    const int cx = g.X / 2, cy = g.Y / 2, cz = g.Z / 2;
+    const int lmax = std::max(cx, g.X - 1 - cx) + std::max(cy, g.Y - 1 - cy) + std::max(cz, g.Z - 1 - cz);
+    for (int L = 1; L <= lmax; L++) {
+        const long long n = ((long long)L + 1) * ((long long)L + 1);
+        k_centre_level<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g, L, ax, ay, az, stride, scratch);
+        OM_COUNT_LAUNCH();
+    }
+    k_to_float<<<grid_for(g.V), 256, 0, st>>>(g.V, scratch, out);
+    OM_COUNT_LAUNCH();
+    return cudaGetLastError();
+}
 
 }  // namespace omni3d

@@ -130,6 +130,12 @@ cudaError_t brick_sweep(const Geometry &geo, Bricks *B, int method, const float 
 // The error flag of the brick passes (1: a TMA wait gave up).  Synchronises st.
 cudaError_t brick_error(const Bricks &B, int *flag, cudaStream_t st);
 
+// initialIntegration.cpp on the device: p integrated outward from the centre voxel in FP64
+// (scratch: V doubles), written to out as float.  The components are read at
+// ax[v * stride] (stride 1: three arrays; 4: the float4 field).  Synchronises st once.
+cudaError_t centre_integration(const Grid &g, const float *ax, const float *ay, const float *az, int stride,
+                               double pref, double *scratch, float *out, cudaStream_t st);
+
 // Pack three component arrays (+ optional curl) into the interleaved field.
 cudaError_t pack_field(const Grid &g, const float *ax, const float *ay, const float *az,
                        const float *curl, Field *f, bool make_bf16, cudaStream_t st);

@@ -38,7 +38,7 @@ class Params(C.Structure):
                 ("line_spacing", _f), ("n_dirs", _i), ("dirs", _fp), ("max_iter", _i), ("threshold", _f),
                 ("method", _i), ("solver", _i), ("grad_storage", _i), ("tol", _d), ("gauge", _i),
                 ("ref_i", _i), ("ref_j", _i), ("ref_k", _i), ("seed_first_iteration", _i), ("device", _i),
-                ("anchor_max_links", _ll), ("engine", _i)]
+                ("anchor_max_links", _ll), ("engine", _i), ("initial_guess", _i)]
 
 
 class Stats(C.Structure):
@@ -70,6 +70,7 @@ SIGNATURES = {
     "omni3d_sweep": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i]),
     "omni3d_sweep_noalloc": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "omni3d_curl": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _i]),
+    "omni3d_centre_integration": (_i, [_vp, _vp, _vp, _vp, C.c_double, _vp, _i]),
     "omni3d_gauge": (_i, [_vp, _vp, _vp, _ll, _i, _ll, _i]),
     "omni3d_adjoint": (_i, [_vp, _vp, _vp, _vp, _vp, _i]),
     "omni3d_geometry_info": (_i, [_vp, C.POINTER(_ll), C.POINTER(_ll), C.POINTER(_ll)]),

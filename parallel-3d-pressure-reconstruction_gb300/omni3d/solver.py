@@ -19,6 +19,7 @@ _METHODS = {"plain": L.METHOD_PLAIN, "select": L.METHOD_SELECT, "weighted": L.ME
             "mini_curl": L.METHOD_MINI_CURL, "weighted_mini_curl": L.METHOD_WEIGHTED_MINI_CURL}
 _SOLVERS = {"anchor": L.SOLVER_ANCHOR, "sweep": L.SOLVER_SWEEP}
 _ENGINES = {"auto": L.ENGINE_AUTO, "lines": L.ENGINE_LINES, "bricks": L.ENGINE_BRICKS}
+_INITS = {"zero": 0, "centre": 1}
 _GRADS = {"f32": L.GRAD_F32, "bf16": L.GRAD_BF16}
 _GAUGES = {"none": L.GAUGE_NONE, "point": L.GAUGE_POINT, "mean": L.GAUGE_MEAN}
 
@@ -48,7 +49,7 @@ class Omni3D:
 
     def __init__(self, dims, spacing, dirs, *, density=1.0, line_spacing=1.0, max_iter=4, threshold=0.0,
                  method="plain", solver="anchor", grad="f32", tol=0.0, gauge="none", ref=(0, 0, 0),
-                 seed_first_iteration=True, device=0, anchor_max_links=0, engine="auto"):
+                 seed_first_iteration=True, device=0, anchor_max_links=0, engine="auto", initial_guess="zero"):
         nx, ny, nz = (int(d) for d in dims)
         self.dims = (nx, ny, nz)
         self.V = nx * ny * nz
@@ -74,6 +75,7 @@ class Omni3D:
         P.device = int(device)
         P.anchor_max_links = int(anchor_max_links)
         P.engine = _ENGINES[engine]
+        P.initial_guess = _INITS[initial_guess]
         self.params = P
         self.method = method
         self.solve_count = 0
@@ -226,6 +228,21 @@ class Omni3D:
             out = np.empty(self.V, np.float32)
             o = out.ctypes.data
         check(lib().omni3d_curl(self._h, ptrs[0], ptrs[1], ptrs[2], ptrs[3], o, int(dev)), self._h)
+        return out.reshape(self.dims[::-1])
+
+    def centre_integration(self, ax, ay, az, pref=0.0):
+        """The reference's initial guess (initialIntegration.cpp): p integrated outward from
+        the centre voxel, FP64 on the device, returned as float32."""
+        dev, keep, ptrs = self._ptrs([ax, ay, az])
+        if dev:
+            import torch
+
+            out = torch.empty(self.V, dtype=torch.float32, device=keep[0].device)
+            o = out.data_ptr()
+        else:
+            out = np.empty(self.V, np.float32)
+            o = out.ctypes.data
+        check(lib().omni3d_centre_integration(self._h, ptrs[0], ptrs[1], ptrs[2], float(pref), o, int(dev)), self._h)
         return out.reshape(self.dims[::-1])
 
 

@@ -20,6 +20,7 @@ outputs of the reference functions:
            (mode 3), bodyIntegralInnerSelectFixedBC (mode 4, threshold at the 75th
            percentile of the curl), bodyIntegralInnerMiniCurl (mode 5) and
            bodyIntegralInnerWeightedMiniCurl (mode 6)
+  centre   11x8x9 grid: initialIntegration.cpp (FP64, outward from the centre voxel, pref 2.5)
   ls07     10x9x8 grid, 42 directions, line spacing 0.7, 2 plain iterations
   cputwin  10x10x10 grid, 42 directions, 2 iterations of the reference's own CPU loop
            omni3dparallellinesESInnerCPU + devidecountInnerCPU (no pole guard, count > 1)
@@ -100,6 +101,14 @@ def main():
     for mode in (3, 4, 5, 6):
         p, c = R.solve(d, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p0, 2, mode=mode, thr=float(thr), curl=curl)
         out.update({"variants_p_mode%d" % mode: p, "variants_count_mode%d" % mode: c})
+    # centre integration
+    d = (11, 8, 9)
+    f = field(d, 11)
+    sp32 = tuple(float(np.float32(x)) for x in f["spacing"])  # the spacing the library holds (float)
+    pc = R.initial_integration(d, sp32, f["ax"], f["ay"], f["az"], rho=1.25, pref=2.5)
+    out.update({"centre_dims": np.array(d), "centre_spacing": np.array(f["spacing"], np.float32),
+                "centre_ax": f["ax"].reshape(-1), "centre_ay": f["ay"].reshape(-1), "centre_az": f["az"].reshape(-1),
+                "centre_p": pc})
     # line spacing 0.7
     d = (10, 9, 8)
     f = field(d, 5)

@@ -67,6 +67,24 @@ def test_golden_variant_walks_bit_exact(orc, gold, mode):
     np.testing.assert_array_equal(_bits(p), _bits(g["variants_p_mode%d" % mode]))
 
 
+def test_golden_centre_integration_bit_exact(orc, gold):
+    """initialIntegration.cpp: FP64 p integrated outward from the centre voxel."""
+    g = gold
+    p = orc.centre_integration(_dims(g, "centre"), _sp(g, "centre"), g["centre_ax"], g["centre_ay"], g["centre_az"],
+                               rho=1.25, pref=2.5)
+    np.testing.assert_array_equal(p.view(np.uint64), g["centre_p"].view(np.uint64))
+
+
+def test_centre_integration_matches_reference(orc, reflib):
+    from omni3d import synthetic
+
+    for dims in [(12, 10, 8), (7, 9, 11), (2, 3, 2), (16, 5, 13)]:
+        f = synthetic.blobs(dims=dims, count=3, sigma_range=(2.0, 4.0), noise=0.05, seed=sum(dims))
+        a = orc.centre_integration(dims, f["spacing"], f["ax"], f["ay"], f["az"], rho=1.2, pref=3.5)
+        b = reflib.initial_integration(dims, f["spacing"], f["ax"], f["ay"], f["az"], rho=1.2, pref=3.5)
+        np.testing.assert_array_equal(a.view(np.uint64), b.view(np.uint64))
+
+
 def test_golden_line_spacing(orc, gold):
     g = gold
     d = _dims(g, "ls07")
