@@ -18,7 +18,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "omni3d.h"
@@ -155,40 +157,68 @@ int main(int argc, char **argv)
     std::vector<std::string> files;
     list_files(acc_dir, files);
 
-    std::vector<float> x(V), y(V), z(V), u(V), v(V), w(V), ax(V), ay(V), az(V), mask(V), p0(V), p(V), cnt(V), curl(V);
+    // Two slots of host buffers: while snapshot n is solved on the GPU, snapshot n + 1 is
+    // parsed into the other slot and snapshot n - 1's output is written from it.
+    struct Slot {
+        std::vector<float> x, y, z, u, v, w, ax, ay, az, mask, p0, p, cnt;
+        int ncol = -1;
+        std::string err;
+    };
+    Slot slot[2];
+    for (Slot &s : slot)
+        for (auto *a : {&s.x, &s.y, &s.z, &s.u, &s.v, &s.w, &s.ax, &s.ay, &s.az, &s.mask, &s.p0, &s.p, &s.cnt})
+            a->resize((size_t)V);
+    std::vector<float> curl((size_t)V);
+    auto read_into = [&](size_t fi, Slot &s) {
+        s.ncol = omni3d_read_tecplot(files[fi].c_str(), &fp, s.x.data(), s.y.data(), s.z.data(), s.u.data(),
+                                     s.v.data(), s.w.data(), s.ax.data(), s.ay.data(), s.az.data(), s.mask.data());
+        s.err = s.ncol < 0 ? omni3d_global_error() : "";
+    };
     std::printf("Processing Starts\n");
     if (log) std::fprintf(log, "Processing Starts\n");
     int rc_all = 0;
+    std::thread reader, writer;
+    if (!files.empty()) reader = std::thread(read_into, (size_t)0, std::ref(slot[0]));
     for (size_t fi = 0; fi < files.size(); fi++) {
+        Slot &s = slot[fi % 2];
+        reader.join();  // snapshot fi is parsed
+        if (writer.joinable()) writer.join();  // the other slot is free again
+        if (fi + 1 < files.size()) reader = std::thread(read_into, fi + 1, std::ref(slot[(fi + 1) % 2]));
         std::string name = files[fi].substr(files[fi].find_last_of('/') + 1);
         std::printf("%s\n", name.c_str());
         if (log) std::fprintf(log, "%s", name.c_str());
-        if (omni3d_read_tecplot(files[fi].c_str(), &fp, x.data(), y.data(), z.data(), u.data(), v.data(), w.data(),
-                                ax.data(), ay.data(), az.data(), mask.data()) < 0) {
+        if (s.ncol < 0) {
             if (log) std::fprintf(log, " failed to open\n");
             continue;
         }
         if (log) std::fprintf(log, "\n");
-        omni3d_bernoulli_face(nx, ny, nz, fp.pref, fp.density, u.data(), v.data(), w.data(), p0.data());
+        omni3d_bernoulli_face(nx, ny, nz, fp.pref, fp.density, s.u.data(), s.v.data(), s.w.data(), s.p0.data());
         omni3d_stats stt;
-        int rc = omni3d_solve(ctx, ax.data(), ay.data(), az.data(), nullptr, mask.data(), p0.data(), p.data(),
-                              cnt.data(), 0, &stt);
+        int rc = omni3d_solve(ctx, s.ax.data(), s.ay.data(), s.az.data(), nullptr, s.mask.data(), s.p0.data(),
+                              s.p.data(), s.cnt.data(), 0, &stt);
         if (rc != OMNI3D_OK) {
             std::printf("CUDA error: %s\n", omni3d_last_error(ctx));
             rc_all = 1;
             continue;
         }
-        char out[4096];
-        std::snprintf(out, sizeof(out), "%s%sPressureOmni3D_%05d.dat", out_dir.c_str(),
-                      (!out_dir.empty() && out_dir.back() != '/') ? "/" : "", (int)fi);
-        if (omni3d_write_pressure(out, nx, ny, nz, x.data(), y.data(), z.data(), p.data(), cnt.data()) != OMNI3D_OK)
-            std::printf("%s\n", omni3d_global_error());
         if (fi == 0) {
-            omni3d_curl(ctx, ax.data(), ay.data(), az.data(), mask.data(), curl.data(), 0);
-            omni3d_write_curl("CurlofMaterialAcc_Sample.dat", nx, ny, nz, x.data(), y.data(), z.data(), curl.data());
+            omni3d_curl(ctx, s.ax.data(), s.ay.data(), s.az.data(), s.mask.data(), curl.data(), 0);
+            omni3d_write_curl("CurlofMaterialAcc_Sample.dat", nx, ny, nz, s.x.data(), s.y.data(), s.z.data(),
+                              curl.data());
         }
+        std::string out = out_dir + ((!out_dir.empty() && out_dir.back() != '/') ? "/" : "");
+        char name_buf[64];
+        std::snprintf(name_buf, sizeof(name_buf), "PressureOmni3D_%05d.dat", (int)fi);
+        out += name_buf;
+        writer = std::thread([&s, out, nx, ny, nz]() {
+            if (omni3d_write_pressure(out.c_str(), nx, ny, nz, s.x.data(), s.y.data(), s.z.data(), s.p.data(),
+                                      s.cnt.data()) != OMNI3D_OK)
+                std::printf("%s\n", omni3d_global_error());
+        });
         std::printf("  %d iterations, %lld lines, %.1f ms\n", stt.iterations, stt.n_lines, stt.ms_total);
     }
+    if (reader.joinable()) reader.join();
+    if (writer.joinable()) writer.join();
     omni3d_destroy(ctx);
     if (log) std::fclose(log);
     return rc_all;

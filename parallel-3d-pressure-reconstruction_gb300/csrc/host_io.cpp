@@ -3,6 +3,14 @@
 // (K:8615-8649), the Tecplot acceleration reader (K:8708-8792), the Bernoulli initial face
 // (K:8805-8811) and the pressure / curl writers (K:8916-8958).  Also an icosphere
 // generator that reproduces the direction sets the reference ships.
+//
+// The Tecplot files hold one text row per voxel (about 160 bytes at 10 columns: 2.7 GB at
+// 256^3), so the reader and the writers are parallel: the reader takes the file in 256 MB
+// blocks, cuts each block's complete lines into one chunk per thread, counts the chunks'
+// lines, then parses every chunk in place (strtod on the row text, rounded to float, as
+// the reference's _wtof into float arrays); the writers format blocks of rows in parallel
+// and write them in order.  OMNI3D_IO_THREADS sets the thread count (default: all
+// hardware threads), OMNI3D_IO_BLOCK the reader's block size in bytes (default 256 MB).
 #include <algorithm>
 #include <array>
 #include <cmath>
@@ -10,7 +18,9 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <string>
+#include <thread>
 #include <utility>
 #include <vector>
 
@@ -52,6 +62,132 @@ void copy_str(char *dst, size_t cap, const std::string &s)
     size_t n = std::min(cap - 1, s.size());
     std::memcpy(dst, s.data(), n);
     dst[n] = 0;
+}
+
+// Threads of the text readers and writers.
+int io_threads()
+{
+    const char *e = std::getenv("OMNI3D_IO_THREADS");
+    int n = e ? std::atoi(e) : (int)std::thread::hardware_concurrency();
+    return std::max(1, std::min(n, 256));
+}
+
+// f(t) for t in [0, n): t = 0 on the calling thread.
+template <typename F>
+void parallel_for(int n, F &&f)
+{
+    if (n <= 1) {
+        f(0);
+        return;
+    }
+    std::vector<std::thread> th;
+    th.reserve((size_t)n - 1);
+    for (int t = 1; t < n; t++) th.emplace_back([&f, t]() { f(t); });
+    f(0);
+    for (auto &x : th) x.join();
+}
+
+inline bool is_sep(char c) { return c == ' ' || c == '\t' || c == ','; }
+
+// Where a Tecplot reader puts each voxel's columns, and what it found.
+struct TecplotJob {
+    const omni3d_file_params *fp;
+    float *out[10];          // x y z u v w ax ay az mask (any may be NULL)
+    long long rows_org;      // rows of the uncropped grid
+};
+
+struct ChunkResult {
+    int ncol = -1;            // columns of the chunk's first row inside the crop
+    long long bad_row = -1;   // first row inside the crop whose column count differs
+};
+
+// Parse the complete lines in [b, e) -- the chunk's first line is body row row0 -- into the
+// job's arrays.  Rows outside the crop are skipped without being read, as in the reference.
+ChunkResult parse_rows(const char *b, const char *e, long long row0, const TecplotJob &J)
+{
+    ChunkResult R;
+    const omni3d_file_params *fp = J.fp;
+    const long long nxo = fp->nx_org, nyo = fp->ny_org;
+    const int i0 = fp->roi[0], i1 = fp->roi[1], j0 = fp->roi[2], j1 = fp->roi[3], k0 = fp->roi[4], k1 = fp->roi[5];
+    const long long nx = i1 - i0 + 1, ny = j1 - j0 + 1;
+    long long row = row0;
+    for (const char *p = b; p < e && row < J.rows_org; row++) {
+        const char *nl = static_cast<const char *>(std::memchr(p, '\n', (size_t)(e - p)));
+        const char *le = nl ? nl : e;
+        const char *next = nl ? nl + 1 : e;
+        const long long i = row % nxo, j = (row / nxo) % nyo, k = row / (nxo * nyo);
+        if (i >= i0 && i <= i1 && j >= j0 && j <= j1 && k >= k0 && k <= k1) {
+            const char *te = le;
+            while (te > p && te[-1] == '\r') te--;  // the line's end, as read_line strips it
+            const char *tok[11];
+            int n = 0;
+            for (const char *q = p; q < te;) {
+                while (q < te && is_sep(*q)) q++;
+                if (q >= te) break;
+                if (n < 11) tok[n] = q;
+                n++;
+                while (q < te && !is_sep(*q)) q++;
+            }
+            if (R.ncol < 0) R.ncol = n;
+            if (n != R.ncol || (n != 10 && n != 7)) {
+                R.bad_row = row;
+                return R;
+            }
+            const long long ind = (i - i0) + (j - j0) * nx + (k - k0) * nx * ny;
+            // strtod stops at the separator or line end that follows each token
+            auto val = [&](int c) { return (float)std::strtod(tok[c], nullptr); };
+            float **o = const_cast<float **>(J.out);
+            if (o[0]) o[0][ind] = val(0);
+            if (o[1]) o[1][ind] = val(1);
+            if (o[2]) o[2][ind] = val(2);
+            const int a = n == 10 ? 6 : 3;
+            for (int c = 0; c < 3; c++)
+                if (o[3 + c]) o[3 + c][ind] = n == 10 ? val(3 + c) : 0.0f;
+            for (int c = 0; c < 4; c++)
+                if (o[6 + c]) o[6 + c][ind] = val(a + c);
+        }
+        p = next;
+    }
+    return R;
+}
+
+// Rows [r0, r1) of `cols` columns printed "%15.9f" and separated by blanks, one per line.
+void format_rows(std::string &buf, const float *const *cols, int ncols, long long r0, long long r1)
+{
+    buf.clear();
+    buf.reserve((size_t)(r1 - r0) * (size_t)(16 * ncols + 1));
+    char tmp[96];
+    for (long long r = r0; r < r1; r++)
+        for (int c = 0; c < ncols; c++) {
+            int len = std::snprintf(tmp, sizeof(tmp), c + 1 < ncols ? "%15.9f " : "%15.9f\n", (double)cols[c][r]);
+            if (len < (int)sizeof(tmp)) {
+                buf.append(tmp, (size_t)len);
+            } else {  // very large values print more than the buffer holds
+                std::vector<char> big((size_t)len + 1);
+                std::snprintf(big.data(), big.size(), c + 1 < ncols ? "%15.9f " : "%15.9f\n", (double)cols[c][r]);
+                buf.append(big.data(), (size_t)len);
+            }
+        }
+}
+
+// The body of a Tecplot writer: V rows, formatted in parallel blocks, written in order.
+bool write_rows(FILE *f, const float *const *cols, int ncols, long long V)
+{
+    const int T = io_threads();
+    const long long block = 1LL << 20;
+    std::vector<std::string> bufs((size_t)T);
+    for (long long b0 = 0; b0 < V; b0 += block) {
+        const long long b1 = std::min(V, b0 + block);
+        const long long per = (b1 - b0 + T - 1) / T;
+        parallel_for(T, [&](int t) {
+            const long long r0 = std::min(b1, b0 + per * t), r1 = std::min(b1, r0 + per);
+            format_rows(bufs[(size_t)t], cols, ncols, r0, r1);
+        });
+        for (int t = 0; t < T; t++)
+            if (!bufs[(size_t)t].empty() && std::fwrite(bufs[(size_t)t].data(), 1, bufs[(size_t)t].size(), f) != bufs[(size_t)t].size())
+                return false;
+    }
+    return true;
 }
 
 std::vector<std::string> tokens(const std::string &s)
@@ -144,48 +280,109 @@ int omni3d_read_tecplot(const char *path, const omni3d_file_params *fp, float *x
     if (!path || !fp) return io_fail(OMNI3D_ERR_ARG, "bad arguments");
     FILE *f = std::fopen(path, "rb");
     if (!f) return io_fail(OMNI3D_ERR_IO, std::string(path) + " failed to open");
-    std::string s;
-    for (int h = 0; h < 3; h++)
-        if (!read_line(f, s)) { std::fclose(f); return io_fail(OMNI3D_ERR_IO, std::string(path) + ": short header"); }
-    const int i0 = fp->roi[0], i1 = fp->roi[1], j0 = fp->roi[2], j1 = fp->roi[3], k0 = fp->roi[4], k1 = fp->roi[5];
-    const long long nx = i1 - i0 + 1, ny = j1 - j0 + 1;
+    TecplotJob J;
+    J.fp = fp;
+    float *outs[10] = {x, y, z, u, v, w, ax, ay, az, mask};
+    std::copy(outs, outs + 10, J.out);
+    J.rows_org = (long long)fp->nx_org * fp->ny_org * fp->nz_org;
+    const int T = io_threads();
+    const char *eb = std::getenv("OMNI3D_IO_BLOCK");
+    size_t kBlock = eb ? std::max<size_t>(16, (size_t)std::strtoull(eb, nullptr, 10)) : ((size_t)256 << 20);
+    if (std::fseek(f, 0, SEEK_END) == 0) {  // no larger than the file
+        const long sz = std::ftell(f);
+        if (sz >= 0) kBlock = std::min(kBlock, (size_t)sz + 1);
+        std::fseek(f, 0, SEEK_SET);
+    }
+    // an uninitialised buffer (a zero-filled one would cost a pass over every block)
+    size_t cap = kBlock;
+    std::unique_ptr<char[]> buf(new char[cap]);
+    size_t have = 0;            // bytes of buf holding unprocessed text
+    int header = 0;             // header lines consumed
+    long long rows = 0;         // body rows consumed
     int ncol = -1;
-    for (long long k = 0; k < fp->nz_org; k++)
-        for (long long j = 0; j < fp->ny_org; j++)
-            for (long long i = 0; i < fp->nx_org; i++) {
-                if (!read_line(f, s)) {
-                    std::fclose(f);
-                    return io_fail(OMNI3D_ERR_IO, std::string(path) + ": fewer rows than the grid");
-                }
-                if (!(i >= i0 && i <= i1 && j >= j0 && j <= j1 && k >= k0 && k <= k1)) continue;
-                std::vector<std::string> t = tokens(s);
-                if (ncol < 0) ncol = (int)t.size();
-                if ((int)t.size() != ncol || (ncol != 10 && ncol != 7)) {
-                    std::fclose(f);
-                    return io_fail(OMNI3D_ERR_IO, std::string(path) + ": rows must have 10 (x y z u v w Du Dv Dw mask) "
-                                                                      "or 7 (x y z Du Dv Dw mask) columns");
-                }
-                long long ind = (i - i0) + (j - j0) * nx + (k - k0) * nx * ny;
-                auto val = [&](int c) { return (float)to_double(t[c]); };
-                if (x) x[ind] = val(0);
-                if (y) y[ind] = val(1);
-                if (z) z[ind] = val(2);
-                int o = ncol == 10 ? 6 : 3;
-                if (ncol == 10) {
-                    if (u) u[ind] = val(3);
-                    if (v) v[ind] = val(4);
-                    if (w) w[ind] = val(5);
-                } else {
-                    if (u) u[ind] = 0.0f;
-                    if (v) v[ind] = 0.0f;
-                    if (w) w[ind] = 0.0f;
-                }
-                if (ax) ax[ind] = val(o);
-                if (ay) ay[ind] = val(o + 1);
-                if (az) az[ind] = val(o + 2);
-                if (mask) mask[ind] = val(o + 3);
+    long long bad_row = -1;
+    bool eof = false;
+    std::vector<ChunkResult> res((size_t)T);
+    std::vector<long long> first((size_t)T + 1);
+    std::vector<size_t> cut((size_t)T + 1);
+    while (rows < J.rows_org && bad_row < 0) {
+        if (!eof) {
+            if (have + kBlock > cap) {  // a line longer than a block: grow
+                std::unique_ptr<char[]> bigger(new char[have + kBlock]);
+                std::memcpy(bigger.get(), buf.get(), have);
+                buf.swap(bigger);
+                cap = have + kBlock;
             }
+            const size_t got = std::fread(buf.get() + have, 1, kBlock, f);
+            have += got;
+            if (got < kBlock) eof = true;
+        }
+        const char *base = buf.get();
+        // complete lines end at the last newline; at end of file the rest is a line too
+        size_t end = have;
+        if (!eof) {
+            const char *lastnl = nullptr;
+            for (size_t q = have; q > 0; q--)
+                if (base[q - 1] == '\n') { lastnl = base + q - 1; break; }
+            if (!lastnl) {
+                if (have > ((size_t)1 << 31)) { std::fclose(f); return io_fail(OMNI3D_ERR_IO, std::string(path) + ": line too long"); }
+                continue;  // read more
+            }
+            end = (size_t)(lastnl - base) + 1;
+        }
+        size_t pos = 0;
+        while (header < 3 && pos < end) {  // the three header lines
+            const char *nl = static_cast<const char *>(std::memchr(base + pos, '\n', end - pos));
+            pos = nl ? (size_t)(nl - base) + 1 : end;
+            header++;
+        }
+        if (header < 3) {
+            if (eof) { std::fclose(f); return io_fail(OMNI3D_ERR_IO, std::string(path) + ": short header"); }
+        } else if (pos < end) {
+            // one chunk per thread, cut after a newline; count lines, then parse in parallel
+            cut[0] = pos;
+            for (int t = 1; t < T; t++) {
+                size_t c = pos + (end - pos) * (size_t)t / (size_t)T;
+                c = std::max(c, cut[(size_t)t - 1]);
+                const char *nl = c < end ? static_cast<const char *>(std::memchr(base + c, '\n', end - c)) : nullptr;
+                cut[(size_t)t] = nl ? (size_t)(nl - base) + 1 : end;
+            }
+            cut[(size_t)T] = end;
+            std::vector<long long> nlines((size_t)T, 0);
+            parallel_for(T, [&](int t) {
+                long long n = 0;
+                const char *p = base + cut[(size_t)t], *e = base + cut[(size_t)t + 1];
+                while (p < e) {
+                    const char *nl = static_cast<const char *>(std::memchr(p, '\n', (size_t)(e - p)));
+                    n++;
+                    p = nl ? nl + 1 : e;
+                }
+                nlines[(size_t)t] = n;
+            });
+            first[0] = rows;
+            for (int t = 0; t < T; t++) first[(size_t)t + 1] = first[(size_t)t] + nlines[(size_t)t];
+            parallel_for(T, [&](int t) {
+                res[(size_t)t] = parse_rows(base + cut[(size_t)t], base + cut[(size_t)t + 1], first[(size_t)t], J);
+            });
+            for (int t = 0; t < T && bad_row < 0; t++) {  // the first inconsistency in row order
+                const ChunkResult &r = res[(size_t)t];
+                if (r.ncol < 0) continue;
+                if (ncol < 0) ncol = r.ncol;
+                if (r.ncol != ncol) bad_row = first[(size_t)t];
+                else if (r.bad_row >= 0) bad_row = r.bad_row;
+            }
+            rows = first[(size_t)T];
+        }
+        // keep the incomplete last line for the next block
+        std::memmove(buf.get(), buf.get() + end, have - end);
+        have -= end;
+        if (eof && have == 0) break;
+    }
     std::fclose(f);
+    if (bad_row >= 0 || (ncol >= 0 && ncol != 10 && ncol != 7))
+        return io_fail(OMNI3D_ERR_IO, std::string(path) + ": rows must have 10 (x y z u v w Du Dv Dw mask) "
+                                                          "or 7 (x y z Du Dv Dw mask) columns");
+    if (rows < J.rows_org) return io_fail(OMNI3D_ERR_IO, std::string(path) + ": fewer rows than the grid");
     return ncol;
 }
 
@@ -213,9 +410,9 @@ int omni3d_write_pressure(const char *path, int nx, int ny, int nz, const float 
     std::fprintf(f, "VARIABLES = \"X\",\"Y\",\"Z\",\"P\",\"Count\"\n");
     std::fprintf(f, "ZONE I=%i, J=%i, K=%i,F=POINT\n", nx, ny, nz);
     long long V = (long long)nx * ny * nz;
-    for (long long i = 0; i < V; i++)
-        std::fprintf(f, "%15.9f %15.9f %15.9f %15.9f %15.9f\n", x[i], y[i], z[i], p[i], count[i]);
-    int bad = std::ferror(f);
+    const float *cols[5] = {x, y, z, p, count};
+    bool ok = write_rows(f, cols, 5, V);  // rows "%15.9f %15.9f %15.9f %15.9f %15.9f\n" (K:8929)
+    int bad = !ok || std::ferror(f);
     std::fclose(f);
     return bad ? io_fail(OMNI3D_ERR_IO, std::string(path) + ": write error") : OMNI3D_OK;
 }
@@ -230,8 +427,9 @@ int omni3d_write_curl(const char *path, int nx, int ny, int nz, const float *x, 
     std::fprintf(f, "VARIABLES = \"X\",\"Y\",\"Z\",\"Curl of Acceleration\"\n");
     std::fprintf(f, "ZONE I=%i, J=%i, K=%i,F=POINT\n", nx, ny, nz);
     long long V = (long long)nx * ny * nz;
-    for (long long i = 0; i < V; i++) std::fprintf(f, "%15.9f %15.9f %15.9f %15.9f\n", x[i], y[i], z[i], curl[i]);
-    int bad = std::ferror(f);
+    const float *cols[4] = {x, y, z, curl};
+    bool ok = write_rows(f, cols, 4, V);  // rows "%15.9f %15.9f %15.9f %15.9f\n" (K:8954)
+    int bad = !ok || std::ferror(f);
     std::fclose(f);
     return bad ? io_fail(OMNI3D_ERR_IO, std::string(path) + ": write error") : OMNI3D_OK;
 }

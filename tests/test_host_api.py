@@ -180,6 +180,63 @@ def test_read_tecplot_errors(omni, tmp_path):
         omni.read_tecplot(str(tmp_path / "none.dat"), fp)
 
 
+def test_read_tecplot_parallel_matches_serial_and_python(omni, tmp_path, monkeypatch):
+    """The block-parallel reader: 1 and 7 threads give identical arrays, and every value is
+    the float rounding of the correctly rounded double of its text (the reference's _wtof
+    into float arrays), with blanks, tabs and commas as separators and CRLF line ends."""
+    dims = (37, 23, 19)
+    n = int(np.prod(dims))
+    rng = np.random.default_rng(7)
+    vals = [rng.normal(size=n) * 10.0 ** rng.integers(-8, 8, n) for _ in range(10)]
+    seps = [" ", "\t", ", ", "  "]
+    path = tmp_path / "acc.dat"
+    with open(path, "w", newline="") as fh:
+        fh.write('TITLE = "acc"\r\nVARIABLES = "X"\r\nZONE I=37, J=23, K=19\r\n')
+        for r in range(n):
+            sep = seps[r % 4]
+            fh.write(sep.join(repr(float(vals[c][r])) if c % 3 else "%.9e" % vals[c][r] for c in range(10)) + "\r\n")
+    pf = tmp_path / "P.dat"
+    pf.write_text(PARAMS.replace("64\n48\n32", "37\n23\n19").format(extra="\n2\n30\n1\n20\n3\n18"))
+    fp = omni.read_params(str(pf))
+    monkeypatch.setenv("OMNI3D_IO_THREADS", "1")
+    one = omni.read_tecplot(str(path), fp)
+    monkeypatch.setenv("OMNI3D_IO_THREADS", "7")
+    many = omni.read_tecplot(str(path), fp)
+    monkeypatch.setenv("OMNI3D_IO_BLOCK", "97")  # lines and header lines span many blocks
+    monkeypatch.setenv("OMNI3D_IO_THREADS", "2")
+    small = omni.read_tecplot(str(path), fp)
+    monkeypatch.delenv("OMNI3D_IO_BLOCK")
+    names = ["x", "y", "z", "u", "v", "w", "ax", "ay", "az", "mask"]
+    rows = [l for l in path.read_text().replace("\r", "").split("\n")[3:] if l]
+    table = np.array([[float(t) for t in l.replace(",", " ").split()] for l in rows]).reshape(19, 23, 37, 10)
+    crop = table[3:19, 1:21, 2:31]
+    for c, nm in enumerate(names):
+        np.testing.assert_array_equal(one[nm].view(np.uint32), many[nm].view(np.uint32))
+        np.testing.assert_array_equal(one[nm].view(np.uint32), small[nm].view(np.uint32))
+        np.testing.assert_array_equal(one[nm], crop[..., c].reshape(-1).astype(np.float32))
+
+
+def test_writers_parallel_bytes_equal_serial(omni, tmp_path, monkeypatch):
+    dims = (41, 30, 11)
+    n = int(np.prod(dims))
+    rng = np.random.default_rng(8)
+    cols = [(rng.normal(size=n) * 10.0 ** rng.integers(-6, 6, n)).astype(np.float32) for _ in range(5)]
+    cols[3][5] = np.float32(3e30)  # a row wider than the usual formatting buffer
+    out = {}
+    for t in ("1", "5"):
+        monkeypatch.setenv("OMNI3D_IO_THREADS", t)
+        path = tmp_path / ("p%s.dat" % t)
+        omni.write_pressure(str(path), dims, *cols)
+        out[t] = path.read_bytes()
+        cpath = tmp_path / ("c%s.dat" % t)
+        omni.write_curl(str(cpath), dims, *cols[:4])
+        out["c" + t] = cpath.read_bytes()
+    assert out["1"] == out["5"] and out["c1"] == out["c5"]
+    lines = out["5"].decode().split("\n")
+    for r in (0, 5, n - 1):
+        assert lines[3 + r] == " ".join("%15.9f" % float(c[r]) for c in cols)
+
+
 def test_bernoulli_face(omni):
     dims = (4, 3, 2)
     n = 24
