@@ -21,8 +21,11 @@
 #include <algorithm>
 
 #include "omni3d_internal.h"
+#include "walk.cuh"
 
 namespace omni3d {
+
+constexpr int kWalkBatch = 4;  // steps whose gathers a walk issues together (walk.cuh)
 
 namespace {
 
@@ -72,7 +75,25 @@ struct Sink {
 };
 
 // Record one contribution of weight wt and integral I into voxel v from the segment that
-// started at voxel `start`.
+// started at voxel `start`.  `word` is the anchor bitmap's word of v when the caller has
+// loaded it (emit_w), else emit loads it.
+template <int PASS>
+__device__ __forceinline__ void emit_w(const Sink &S, long long v, long long start, float wt, float I, uint32_t word)
+{
+    if (PASS == kMark) return;
+    if (!((word >> (v & 31)) & 1u)) return;
+    int row = __ldg(S.id + v);
+    if (PASS == kRhs) {  // plain method, operator cached: only b = sum I is field-dependent
+        atomicAdd(S.b + row, I);
+        return;
+    }
+    unsigned long long slot = S.rowptr[row] + atomicAdd(S.cursor + row, 1u);
+    S.col[slot] = (uint32_t)__ldg(S.id + start);
+    S.w[slot] = wt;
+    atomicAdd(S.b + row, wt * I);
+    atomicAdd(S.c + row, wt);
+}
+
 template <int PASS>
 __device__ __forceinline__ void emit(const Sink &S, long long v, long long start, float wt, float I)
 {
@@ -233,7 +254,7 @@ __global__ void __launch_bounds__(256, 6) k_anchor_weighted_raw(Grid g, const Li
 // Selected method: the state machine of k_sweep_select (K:2280-2537); anchors are the
 // segment starts.
 template <int PASS, bool BF16>
-__global__ void __launch_bounds__(256, 6) k_anchor_select(Grid g, const LineRec *__restrict__ lines,
+__global__ void __launch_bounds__(256, 4) k_anchor_select(Grid g, const LineRec *__restrict__ lines,
                                                        const uint32_t *__restrict__ gbase,
                                                        const uint32_t *__restrict__ desc, long long n_lines,
                                                        const float4 *__restrict__ f32,
@@ -256,19 +277,15 @@ __global__ void __launch_bounds__(256, 6) k_anchor_select(Grid g, const LineRec 
     long long start = L.v;
     if (PASS == kMark && started) S.flag[start] = 1;
     float I = 0.0f, comp = 0.0f, csum = 0.0f, nseg = 0.0f;
-    for (int s0 = 0; s0 < L.m; s0 += 16) {
-        uint32_t w = __ldg(L.dp + 32 * (s0 >> 4));
-        int n = min(16, L.m - s0);
-        for (int t = 0; t < n; t++, w >>= 2) {
-            int a = (int)(w & 3u);
-            L.v += a == 0 ? L.d0 : (a == 1 ? L.d1 : L.d2);
-            float4 gv = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (PASS == kFill) gv = load_grad<BF16>(f32, b16, L.v);
-            float cn = kW ? gv.w : __ldg(curl + L.v);
+    // the filling pass gathers the field and the anchor bitmap word of every voxel in batches
+    constexpr int kGrad = PASS == kFill ? (BF16 ? kGradBF16 : kGradF32) : kNoGrad;
+    walk_steps<kWalkBatch, kGrad, PASS == kFill>(
+        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, long long v, const float4 &gv, uint32_t word) {
+            const float cn = kW ? gv.w : __ldg(curl + v);
             if (!started) {
                 bool ok = (a == 0) ? (cn != 0.0f && cn < thr) : (cn != 0.0f);
                 if (ok) {
-                    start = L.v;
+                    start = v;
                     if (PASS == kMark) S.flag[start] = 1;
                     started = true;
                     I = 0.0f; comp = 0.0f; nseg = 0.0f; csum = 0.0f;
@@ -280,12 +297,13 @@ __global__ void __launch_bounds__(256, 6) k_anchor_select(Grid g, const LineRec 
                         kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
                     csum += cn * 1.0e-4f;  // the weights as in k_sweep_select
                     nseg += 1.0f;
-                    emit<PASS>(S, L.v, start, __frcp_rn(csum) * nseg, I);
+                    if (PASS == kFill) emit_w<PASS>(S, v, start, __frcp_rn(csum) * nseg, I, word);
+                    else emit<PASS>(S, v, start, __frcp_rn(csum) * nseg, I);
                 }
                 bool enter_bad = (a == 0) ? ((!paused && cn >= thr) || cn == 0.0f) : (!paused && cn >= thr);
                 if (enter_bad) paused = true;
                 if (paused && good) {
-                    start = L.v;
+                    start = v;
                     if (PASS == kMark) S.flag[start] = 1;
                     I = 0.0f; comp = 0.0f;
                     paused = false;
@@ -293,8 +311,7 @@ __global__ void __launch_bounds__(256, 6) k_anchor_select(Grid g, const LineRec 
                 }
             }
             gl = gv;
-        }
-    }
+        });
 }
 
 // Selected method: a voxel can start a segment only if it is on the boundary (a line entry)

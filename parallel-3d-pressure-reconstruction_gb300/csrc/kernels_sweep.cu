@@ -14,8 +14,13 @@
 #include <algorithm>
 
 #include "omni3d_internal.h"
+#include "walk.cuh"
 
 namespace omni3d {
+
+// Steps whose gathers a walk issues together (walk.cuh); the batched kernels run 4 CTAs of
+// 256 threads per SM (64 registers: the batch's gathers stay in registers).
+constexpr int kWalkBatch = 4;
 
 namespace {
 
@@ -202,7 +207,7 @@ __global__ void __launch_bounds__(256, 6) k_sweep_weighted_raw(Grid g, const Lin
 // increment); a good voxel after a pause restarts the segment at that voxel; the z
 // branch keeps the running curl/count sums on restart.
 template <bool BF16>
-__global__ void __launch_bounds__(256, 6) k_sweep_select(Grid g, const LineRec *__restrict__ lines,
+__global__ void __launch_bounds__(256, 4) k_sweep_select(Grid g, const LineRec *__restrict__ lines,
                                                       const uint32_t *__restrict__ gbase,
                                                       const uint32_t *__restrict__ desc, long long n_lines,
                                                       const float4 *__restrict__ f32,
@@ -222,18 +227,13 @@ __global__ void __launch_bounds__(256, 6) k_sweep_select(Grid g, const LineRec *
     bool paused = false;
     float p0 = started ? __ldg(p + L.v) : 0.0f;
     float I = 0.0f, comp = 0.0f, csum = 0.0f, nseg = 0.0f;
-    for (int s0 = 0; s0 < L.m; s0 += 16) {
-        uint32_t w = __ldg(L.dp + 32 * (s0 >> 4));
-        int n = min(16, L.m - s0);
-        for (int t = 0; t < n; t++, w >>= 2) {
-            int a = (int)(w & 3u);
-            L.v += a == 0 ? L.d0 : (a == 1 ? L.d1 : L.d2);
-            float4 gv = load_grad<BF16>(f32, b16, L.v);
-            float cn = BF16 ? __ldg(curl + L.v) : gv.w;
+    walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, false>(
+        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, nullptr, [&](int a, long long v, const float4 &gv, uint32_t) {
+            const float cn = BF16 ? __ldg(curl + v) : gv.w;
             if (!started) {
                 bool ok = (a == 0) ? (cn != 0.0f && cn < thr) : (cn != 0.0f);
                 if (ok) {
-                    p0 = __ldg(p + L.v);
+                    p0 = __ldg(p + v);
                     started = true;
                     I = 0.0f; comp = 0.0f; nseg = 0.0f; csum = 0.0f;
                 }
@@ -247,20 +247,19 @@ __global__ void __launch_bounds__(256, 6) k_sweep_select(Grid g, const LineRec *
                     csum += cn * 1.0e-4f;
                     nseg += 1.0f;
                     float wc = __frcp_rn(csum) * nseg;
-                    atomicAdd(pncnt + L.v, make_float2((p0 + I) * wc, wc));
+                    atomicAdd(pncnt + v, make_float2((p0 + I) * wc, wc));
                 }
                 bool enter_bad = (a == 0) ? ((!paused && cn >= thr) || cn == 0.0f) : (!paused && cn >= thr);
                 if (enter_bad) paused = true;
                 if (paused && good) {
-                    p0 = __ldg(p + L.v);
+                    p0 = __ldg(p + v);
                     I = 0.0f; comp = 0.0f;
                     paused = false;
                     if (a != 2) { nseg = 0.0f; csum = 0.0f; }
                 }
             }
             gl = gv;
-        }
-    }
+        });
 }
 
 __global__ void k_normalize(long long V, const float2 *__restrict__ pncnt, const float *__restrict__ p_keep,
