@@ -140,7 +140,7 @@ struct Walk {
 // Plain method: anchors are the entries; every voxel of a line takes (p[entry] + I, 1).
 // SELF = false leaves the entry's own term out (the minimum-curl plain variant).
 template <int PASS, bool BF16, bool SELF>
-__global__ void __launch_bounds__(256, 6) k_anchor_plain(Grid g, const LineRec *__restrict__ lines,
+__global__ void __launch_bounds__(256, 4) k_anchor_plain(Grid g, const LineRec *__restrict__ lines,
                                                       const uint32_t *__restrict__ gbase,
                                                       const uint32_t *__restrict__ desc, long long n_lines,
                                                       const float4 *__restrict__ f32,
@@ -157,30 +157,21 @@ __global__ void __launch_bounds__(256, 6) k_anchor_plain(Grid g, const LineRec *
     L.init(g, r, gbase, desc, li);
     const long long e = r.e;
     if (SELF) emit<PASS>(S, e, e, 1.0f, 0.0f);
-    constexpr bool kGrad = PASS == kFill || PASS == kRhs;
-    float4 gl = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (kGrad) gl = load_grad<BF16>(f32, b16, e);
+    float4 gl = load_grad<BF16>(f32, b16, e);
     float I = 0.0f, comp = 0.0f;
-    for (int s0 = 0; s0 < L.m; s0 += 16) {
-        uint32_t w = __ldg(L.dp + 32 * (s0 >> 4));
-        int n = min(16, L.m - s0);
-        for (int t = 0; t < n; t++, w >>= 2) {
-            int a = (int)(w & 3u);
-            L.v += a == 0 ? L.d0 : (a == 1 ? L.d1 : L.d2);
-            if (kGrad) {
-                float4 gv = load_grad<BF16>(f32, b16, L.v);
-                kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
-                gl = gv;
-            }
-            emit<PASS>(S, L.v, e, 1.0f, I);
-        }
-    }
+    // the field and the anchor bitmap word of every voxel gathered in batches
+    walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, true>(
+        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, long long v, const float4 &gv, uint32_t word) {
+            kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
+            gl = gv;
+            emit_w<PASS>(S, v, e, 1.0f, I, word);
+        });
 }
 
 // Weighted method: the walk of k_sweep_weighted (K:1993-2135); anchors are the entries
 // (the marking pass is the plain method's), the entry itself receives nothing.
 template <int PASS, bool BF16>
-__global__ void __launch_bounds__(256, 6) k_anchor_weighted(Grid g, const LineRec *__restrict__ lines,
+__global__ void __launch_bounds__(256, 4) k_anchor_weighted(Grid g, const LineRec *__restrict__ lines,
                                                          const uint32_t *__restrict__ gbase,
                                                          const uint32_t *__restrict__ desc, long long n_lines,
                                                          const float4 *__restrict__ f32,
@@ -196,27 +187,21 @@ __global__ void __launch_bounds__(256, 6) k_anchor_weighted(Grid g, const LineRe
     const long long e = r.e;
     float4 gl = load_grad<BF16>(f32, b16, e);
     float I = 0.0f, comp = 0.0f, csum = 0.0f, nseg = 0.0f;
-    for (int s0 = 0; s0 < L.m; s0 += 16) {
-        uint32_t w = __ldg(L.dp + 32 * (s0 >> 4));
-        int n = min(16, L.m - s0);
-        for (int t = 0; t < n; t++, w >>= 2) {
-            int a = (int)(w & 3u);
-            L.v += a == 0 ? L.d0 : (a == 1 ? L.d1 : L.d2);
-            float4 gv = load_grad<BF16>(f32, b16, L.v);
-            float cn = BF16 ? __ldg(curl + L.v) : gv.w;
+    walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, true>(
+        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, long long v, const float4 &gv, uint32_t word) {
+            float cn = BF16 ? __ldg(curl + v) : gv.w;
             kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
             csum += __fdiv_rn(cn, 1.0e4f);  // the weights as in k_sweep_weighted
             nseg += 1.0f;
-            if (csum != 0.0f) emit<PASS>(S, L.v, e, __frcp_rn(csum) * nseg, I);
+            if (csum != 0.0f) emit_w<PASS>(S, v, e, __frcp_rn(csum) * nseg, I, word);
             gl = gv;
-        }
-    }
+        });
 }
 
 // Weighted method with raw curl sums (the minimum-curl variant): the walk of
 // k_sweep_weighted_raw; anchors are the entries, the entry takes its own term.
 template <int PASS, bool BF16>
-__global__ void __launch_bounds__(256, 6) k_anchor_weighted_raw(Grid g, const LineRec *__restrict__ lines,
+__global__ void __launch_bounds__(256, 4) k_anchor_weighted_raw(Grid g, const LineRec *__restrict__ lines,
                                                              const uint32_t *__restrict__ gbase,
                                                              const uint32_t *__restrict__ desc, long long n_lines,
                                                              const float4 *__restrict__ f32,
@@ -234,21 +219,15 @@ __global__ void __launch_bounds__(256, 6) k_anchor_weighted_raw(Grid g, const Li
     float csum = BF16 ? __ldg(curl + e) : gl.w, nseg = 1.0f;
     emit<PASS>(S, e, e, __frcp_rn(csum), 0.0f);
     float I = 0.0f, comp = 0.0f;
-    for (int s0 = 0; s0 < L.m; s0 += 16) {
-        uint32_t w = __ldg(L.dp + 32 * (s0 >> 4));
-        int n = min(16, L.m - s0);
-        for (int t = 0; t < n; t++, w >>= 2) {
-            int a = (int)(w & 3u);
-            L.v += a == 0 ? L.d0 : (a == 1 ? L.d1 : L.d2);
-            float4 gv = load_grad<BF16>(f32, b16, L.v);
-            float cn = BF16 ? __ldg(curl + L.v) : gv.w;
+    walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, true>(
+        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, long long v, const float4 &gv, uint32_t word) {
+            float cn = BF16 ? __ldg(curl + v) : gv.w;
             kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
             csum += cn;
             nseg += 1.0f;
-            emit<PASS>(S, L.v, e, __frcp_rn(csum) * nseg, I);
+            emit_w<PASS>(S, v, e, __frcp_rn(csum) * nseg, I, word);
             gl = gv;
-        }
-    }
+        });
 }
 
 // Selected method: the state machine of k_sweep_select (K:2280-2537); anchors are the

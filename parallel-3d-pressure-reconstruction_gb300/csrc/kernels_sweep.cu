@@ -83,7 +83,7 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x)
 // Plain method: every voxel of the line, the entry included, receives p[entry] + I(v).
 // SELF = false leaves the entry out (the minimum-curl plain variant, K:2797-2936).
 template <bool BF16, bool SELF>
-__global__ void __launch_bounds__(256, 6) k_sweep_plain(Grid g, const LineRec *__restrict__ lines,
+__global__ void __launch_bounds__(256, 4) k_sweep_plain(Grid g, const LineRec *__restrict__ lines,
                                                      const uint32_t *__restrict__ gbase,
                                                      const uint32_t *__restrict__ desc, long long n_lines,
                                                      const float4 *__restrict__ f32,
@@ -99,19 +99,13 @@ __global__ void __launch_bounds__(256, 6) k_sweep_plain(Grid g, const LineRec *_
     if (SELF) atomicAdd(pncnt + r.e, make_float2(pe, 1.0f));
     float4 gl = load_grad<BF16>(f32, b16, L.v);
     float I = 0.0f, comp = 0.0f;
-    for (int s0 = 0; s0 < L.m; s0 += 16) {
-        uint32_t w = __ldg(L.dp + 32 * (s0 >> 4));
-        int n = min(16, L.m - s0);
-        for (int t = 0; t < n; t++, w >>= 2) {
-            int a = (int)(w & 3u);
-            L.v += a == 0 ? L.d0 : (a == 1 ? L.d1 : L.d2);
-            float4 gv = load_grad<BF16>(f32, b16, L.v);
+    walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, false>(
+        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, nullptr, [&](int a, long long v, const float4 &gv, uint32_t) {
             float term = sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z));
             kahan_add(I, comp, term);
-            atomicAdd(pncnt + L.v, make_float2(pe + I, 1.0f));
+            atomicAdd(pncnt + v, make_float2(pe + I, 1.0f));
             gl = gv;
-        }
-    }
+        });
 }
 
 // Weighted method (K:1993-2135): the entry receives nothing; step s of the line (s = 1..m)
@@ -119,7 +113,7 @@ __global__ void __launch_bounds__(256, 6) k_sweep_plain(Grid g, const LineRec *_
 // nonzero.  Each curl/1e4 term is the reference's correctly rounded float division, so the
 // "sum != 0" decision (all curls so far zero) is the reference's.
 template <bool BF16>
-__global__ void __launch_bounds__(256, 6) k_sweep_weighted(Grid g, const LineRec *__restrict__ lines,
+__global__ void __launch_bounds__(256, 4) k_sweep_weighted(Grid g, const LineRec *__restrict__ lines,
                                                         const uint32_t *__restrict__ gbase,
                                                         const uint32_t *__restrict__ desc, long long n_lines,
                                                         const float4 *__restrict__ f32,
@@ -135,25 +129,19 @@ __global__ void __launch_bounds__(256, 6) k_sweep_weighted(Grid g, const LineRec
     const float pe = __ldg(p + r.e);
     float4 gl = load_grad<BF16>(f32, b16, L.v);
     float I = 0.0f, comp = 0.0f, csum = 0.0f, nseg = 0.0f;
-    for (int s0 = 0; s0 < L.m; s0 += 16) {
-        uint32_t w = __ldg(L.dp + 32 * (s0 >> 4));
-        int n = min(16, L.m - s0);
-        for (int t = 0; t < n; t++, w >>= 2) {
-            int a = (int)(w & 3u);
-            L.v += a == 0 ? L.d0 : (a == 1 ? L.d1 : L.d2);
-            float4 gv = load_grad<BF16>(f32, b16, L.v);
-            float cn = BF16 ? __ldg(curl + L.v) : gv.w;
+    walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, false>(
+        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, nullptr, [&](int a, long long v, const float4 &gv, uint32_t) {
+            float cn = BF16 ? __ldg(curl + v) : gv.w;
             float term = sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z));
             kahan_add(I, comp, term);
             csum += __fdiv_rn(cn, 1.0e4f);
             nseg += 1.0f;
             if (csum != 0.0f) {
                 float wc = __frcp_rn(csum) * nseg;
-                atomicAdd(pncnt + L.v, make_float2((pe + I) * wc, wc));
+                atomicAdd(pncnt + v, make_float2((pe + I) * wc, wc));
             }
             gl = gv;
-        }
-    }
+        });
 }
 
 // Weighted method with raw curl sums (the minimum-curl variant, K:2937-3085): the sum starts
@@ -161,7 +149,7 @@ __global__ void __launch_bounds__(256, 6) k_sweep_weighted(Grid g, const LineRec
 // divided by 1e4) and contributes w (p[entry] + I), w = (s + 1) / C, with no test for a zero
 // sum: a zero sum gives infinities, as in the reference.
 template <bool BF16>
-__global__ void __launch_bounds__(256, 6) k_sweep_weighted_raw(Grid g, const LineRec *__restrict__ lines,
+__global__ void __launch_bounds__(256, 4) k_sweep_weighted_raw(Grid g, const LineRec *__restrict__ lines,
                                                             const uint32_t *__restrict__ gbase,
                                                             const uint32_t *__restrict__ desc, long long n_lines,
                                                             const float4 *__restrict__ f32,
@@ -182,22 +170,16 @@ __global__ void __launch_bounds__(256, 6) k_sweep_weighted_raw(Grid g, const Lin
         atomicAdd(pncnt + L.v, make_float2(pe * w0, w0));
     }
     float I = 0.0f, comp = 0.0f;
-    for (int s0 = 0; s0 < L.m; s0 += 16) {
-        uint32_t w = __ldg(L.dp + 32 * (s0 >> 4));
-        int n = min(16, L.m - s0);
-        for (int t = 0; t < n; t++, w >>= 2) {
-            int a = (int)(w & 3u);
-            L.v += a == 0 ? L.d0 : (a == 1 ? L.d1 : L.d2);
-            float4 gv = load_grad<BF16>(f32, b16, L.v);
-            float cn = BF16 ? __ldg(curl + L.v) : gv.w;
+    walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, false>(
+        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, nullptr, [&](int a, long long v, const float4 &gv, uint32_t) {
+            float cn = BF16 ? __ldg(curl + v) : gv.w;
             kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
             csum += cn;
             nseg += 1.0f;
             const float wc = __frcp_rn(csum) * nseg;
-            atomicAdd(pncnt + L.v, make_float2((pe + I) * wc, wc));
+            atomicAdd(pncnt + v, make_float2((pe + I) * wc, wc));
             gl = gv;
-        }
-    }
+        });
 }
 
 // Selected method (K:2280-2537), state machine and asymmetries included: the entry is a
