@@ -45,6 +45,21 @@ FLT_MAX = float(np.finfo(np.float32).max)
 # bytes per voxel-direction update of the full sweep (selected method): the gradient
 # component read (3 x 4 B), the curl read (4 B) and the accumulator read + write (8 B)
 ALG_BYTES_PER_UNIT = {"f32": 24.0, "bf16": 18.0}
+PROFILE_SUMMARY = os.path.join(REPO, "profiles", "k_sweep_select_k_anchor_select_blobs192.md")
+
+
+def measured_traffic(workload, grad, engine):
+    """DRAM read + write bytes of one final-sweep launch, from the ncu summary committed
+    under profiles/ (a line 'traffic_bytes_per_launch k_sweep_select <workload> <grad>
+    <engine>: <bytes>'), or None when no capture covers this configuration."""
+    key = "traffic_bytes_per_launch k_sweep_select %s %s %s:" % (workload, grad, engine)
+    try:
+        for line in open(PROFILE_SUMMARY):
+            if line.startswith(key):
+                return float(line.split(":")[1]), os.path.relpath(PROFILE_SUMMARY, REPO)
+    except OSError:
+        pass
+    return None, None
 
 
 def workload(args, rank=0):
@@ -427,6 +442,8 @@ def main():
     peak, peak_kind = measured_peak_hbm()
     alg = ALG_BYTES_PER_UNIT[args.grad] * units
     achieved = alg / t_sweep / 1e9
+    eng_name = ["auto", "lines", "bricks"][engine_used]
+    traffic, traffic_src = measured_traffic(config_dict(args)["workload"], args.grad, eng_name)
 
     line = {
         "metric": METRIC, "value": t_dev, "unit": "s", "n_gpus": world,
@@ -438,7 +455,8 @@ def main():
         "variants": variants,
         "gpu_launches": int(stats["kernel_launches"]),
         "roofline": {"bound": "hbm", "kernel": "k_sweep_select (final full sweep)", "achieved": achieved,
-                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                     "traffic_source": traffic_src,
                      "peak_source": peak_kind, "alg_bytes_per_unit": ALG_BYTES_PER_UNIT[args.grad],
                      "units_per_launch": units, "sweep_ms": t_sweep * 1e3},
         "updates_per_s": args.iters * units / t_dev,
