@@ -266,6 +266,86 @@ def run_reference(args):
     return 0
 
 
+def _event_time(fn, stream=None):
+    """Device seconds of fn() between CUDA events on the current stream."""
+    import torch
+
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    out = fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3, out
+
+
+def run_config4(args):
+    """64 snapshots of uneven seeded sizes (each dimension ~ U[32, 160]), a vortex-ring core
+    per snapshot, 5 % noise, 162 directions, plain method, K iterations: the whole batch in
+    one CUDA-graph launch (omni3d_batch_solve) against the same 64 solves issued one by one,
+    inputs resident on the device."""
+    import torch
+
+    import omni3d
+    from omni3d import synthetic
+
+    K = 20
+    snaps = synthetic.batch_snapshots(count=64, lo=32, hi=160, seed=4)
+    dirs = omni3d.icosphere(3)
+    solvers = [omni3d.Omni3D(s["dims"], s["spacing"], dirs, max_iter=K) for s in snaps]
+    dev = [tuple(torch.from_numpy(s[k].reshape(-1)).cuda() for k in ("ax", "ay", "az")) for s in snaps]
+    out = [(torch.empty(s.V, device="cuda"), torch.empty(s.V, device="cuda")) for s in solvers]
+    units = sum(s.geometry_info()["n_units"] for s in solvers)
+    with omni3d.Batch(solvers) as b:
+        for _ in range(max(args.warmup, 1)):
+            b.solve(dev, out=out)
+        t_graph = [_event_time(lambda: b.solve(dev, out=out))[0] for _ in range(args.steps)]
+    for s, d in zip(solvers, dev):  # warm each context for the sequential form
+        s.solve(*d)
+    t_seq = [_event_time(lambda: [s.solve(*d) for s, d in zip(solvers, dev)])[0] for _ in range(args.steps)]
+    for s in solvers:
+        s.close()
+    tg, ts = float(np.mean(t_graph)), float(np.mean(t_seq))
+    print(json.dumps({"metric": "batch time, 64 uneven snapshots (plain, %d iterations)" % K, "value": tg, "unit": "s",
+                      "higher_is_better": False, "sequential_solves_s": ts, "speedup_vs_sequential": ts / tg,
+                      "snapshots_per_s": 64 / tg, "units_per_sweep_all": units,
+                      "updates_per_s": K * units / tg, "steps": args.steps, "warmup": args.warmup,
+                      "config": {"workload": "batch64_vortex_ring", "snapshots": 64, "sizes": "each dim U[32,160]",
+                                 "direction_vertices": 162, "iterations": K, "method": "plain", "solver": "anchor",
+                                 "form": "one CUDA-graph launch (omni3d_batch_solve)"},
+                      "data": "synthetic (seeded vortex rings, 5% noise)"}))
+    return 0
+
+
+def run_config5(args):
+    """96^3 Gaussian blobs, 5 % noise, 642 directions, exactly 200 iterations, plain method:
+    the forward solve and the adjoint (gradient of <g, p> with respect to the field)."""
+    import torch
+
+    import omni3d
+    from omni3d import synthetic
+
+    f = synthetic.blobs(n=96, count=8, sigma_range=(3.0, 9.0), noise=0.05, seed=5)
+    dirs = omni3d.icosphere(4)
+    d = [torch.from_numpy(f[k].reshape(-1)).cuda() for k in ("ax", "ay", "az")]
+    g = torch.randn(96 ** 3, device="cuda")
+    with omni3d.Omni3D(f["dims"], f["spacing"], dirs, max_iter=200, gauge="mean") as s:
+        for _ in range(max(args.warmup, 1)):
+            s.solve(*d)
+            s.adjoint(g)
+        tf = [_event_time(lambda: s.solve(*d))[0] for _ in range(args.steps)]
+        tb = [_event_time(lambda: s.adjoint(g))[0] for _ in range(args.steps)]
+        units = s.geometry_info()["n_units"]
+    print(json.dumps({"metric": "adjoint time, 96^3, 642 directions, 200 iterations", "value": float(np.mean(tb)),
+                      "unit": "s", "higher_is_better": False, "forward_s": float(np.mean(tf)),
+                      "units_per_sweep": units, "steps": args.steps, "warmup": args.warmup,
+                      "config": {"workload": "blobs96_adjoint", "grid": [96, 96, 96], "direction_vertices": 642,
+                                 "iterations": 200, "method": "plain", "solver": "anchor"},
+                      "data": "synthetic (seeded Gaussian blobs, 5% noise)"}))
+    return 0
+
+
 def icosphere_numpy(level):
     """The direction set for the CPU arms, from the oracle's numpy restatement (equal to the
     library's omni3d_icosphere), so that the reference arm never loads the CUDA library."""
@@ -300,6 +380,12 @@ def main():
                     help="only the warm-up and timed solves (for ncu): no calibration, e2e, variants or CPU arm")
     ap.add_argument("--no-variants", action="store_true", help="skip timing the sweep-solver and BF16 forms")
     ap.add_argument("--sor", action="store_true", help="only the reference CPU SOR baseline (JSON line)")
+    ap.add_argument("--config4", action="store_true",
+                    help="the batched-snapshot workload instead: 64 volumes of 32-160 cells per side, 162 "
+                         "directions, one CUDA-graph launch, against the same solves one by one (JSON line)")
+    ap.add_argument("--config5", action="store_true",
+                    help="the adjoint workload instead: 96^3, 642 directions, 200 iterations, forward solve and "
+                         "adjoint (JSON line)")
     args = ap.parse_args()
     if args.iters <= 0:
         args.iters = DEFAULT_ITERS.get((args.n, args.level), 12)
@@ -308,6 +394,10 @@ def main():
     if args.sor:
         print(json.dumps({"metric": METRIC, "cpu_sor_baseline": sor_baseline(args)}))
         return 0
+    if args.config4:
+        return run_config4(args)
+    if args.config5:
+        return run_config5(args)
 
     import torch
 
