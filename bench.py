@@ -504,7 +504,7 @@ def main():
             t1 = time.perf_counter()
             if it >= max(1, args.warmup):
                 e2e_times.append(t1 - t0)
-        t_e2e = float(np.mean(e2e_times))
+        t_e2e = max_over_ranks(float(np.mean(e2e_times)), dev)  # the job's end-to-end time: its slowest rank
     engine_used = stats["engine_used"]
     solver.close()
     variants = {}
@@ -557,7 +557,7 @@ def main():
     }
     line["config"]["engine"] = ["auto", "lines", "bricks"][engine_used]
     line["clocks"] = clk.summary()
-    if rank == 0 and not args.no_cpu and not args.profile:
+    if rank == 0 and world == 1 and not args.no_cpu and not args.profile:  # the CPU sample at N = 1 only
         try:
             ups, dt, cu, kind, threads, nd = cpu_reference_sample(args, f, dirs)
             line["cpu_baseline"] = {"value": args.iters * dt * len(dirs) / nd, "unit": "s", "cores": threads,
