@@ -147,10 +147,25 @@ class Omni3D:
         hosts = [None if a is None else _as_host(a, self.V) for a in arrays]
         return False, hosts, [None if a is None else a.ctypes.data for a in hosts]
 
-    def solve(self, ax, ay, az, *, curl=None, mask=None, p_init=None) -> SolveResult:
+    def solve(self, ax, ay, az, *, curl=None, mask=None, p_init=None, out=None) -> SolveResult:
+        """out: optional (p, count) output arrays of V float32 each, CUDA tensors for device
+        inputs or contiguous host arrays otherwise (e.g. views of pinned memory, which the
+        device-to-host copy reaches without a bounce buffer)."""
         dev, keep, ptrs = self._ptrs([ax, ay, az, curl, mask, p_init])
         st = L.Stats()
-        if dev:
+        if out is not None:
+            p, cnt = out
+            if dev:
+                if not (_is_cuda_tensor(p) and _is_cuda_tensor(cnt) and p.numel() == self.V and cnt.numel() == self.V):
+                    raise ValueError("out must be two CUDA tensors of V elements for device inputs")
+                pp, cp = p.data_ptr(), cnt.data_ptr()
+            else:
+                for a in (p, cnt):
+                    if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.size == self.V
+                            and a.flags.c_contiguous):
+                        raise ValueError("out must be two contiguous float32 arrays of V elements")
+                pp, cp = p.ctypes.data, cnt.ctypes.data
+        elif dev:
             import torch
 
             p = torch.empty(self.V, dtype=torch.float32, device=keep[0].device)

@@ -293,6 +293,27 @@ def test_device_pointers_match_host(omni):
     assert synthetic.relative_l2(rd.p.cpu().numpy(), rh.p, gauge="none") < 1e-6
 
 
+def test_solve_into_caller_buffers(omni):
+    """out=(p, count): pinned host arrays for host inputs, CUDA tensors for device inputs."""
+    torch = pytest.importorskip("torch")
+    dims = (15, 13, 11)
+    f = _field(dims, seed=14)
+    dirs = omni.icosphere(2)
+    with omni.Omni3D(dims, f["spacing"], dirs, max_iter=3) as s:
+        ref = s.solve(f["ax"], f["ay"], f["az"])
+        host = [torch.empty(s.V, dtype=torch.float32).pin_memory().numpy() for _ in range(2)]
+        r = s.solve(f["ax"], f["ay"], f["az"], out=host)
+        assert r.p.base is not None or r.p.size == s.V
+        np.testing.assert_array_equal(host[1], ref.count.reshape(-1))
+        assert synthetic.relative_l2(host[0], ref.p, gauge="none") < 1e-6
+        t = [torch.from_numpy(f[k].reshape(-1)).cuda() for k in ("ax", "ay", "az")]
+        dev = [torch.empty(s.V, device="cuda") for _ in range(2)]
+        s.solve(*t, out=dev)
+        np.testing.assert_array_equal(dev[1].cpu().numpy(), ref.count.reshape(-1))
+        with pytest.raises(ValueError):
+            s.solve(f["ax"], f["ay"], f["az"], out=[np.empty(3, np.float32)] * 2)
+
+
 def test_counts_deterministic(omni):
     dims = (20, 20, 20)
     f = _field(dims, seed=12)
