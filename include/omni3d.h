@@ -112,6 +112,10 @@ typedef struct {
                                   holds) */
     int engine;                /* OMNI3D_ENGINE_* */
     int initial_guess;         /* OMNI3D_INIT_*: the initial state when p_init is NULL */
+    int sweep_fp64;            /* 1: full sweeps accumulate (pn, count) in FP64 and normalise in
+                                  FP64 -- for the anchor solver its one final sweep, a
+                                  defect-correction step from the FP32 iteration; for the sweep
+                                  solver every sweep.  Line integrals stay FP32 Kahan sums. */
 } omni3d_params;
 
 typedef struct {

@@ -66,6 +66,7 @@ struct omni3d_ctx {
     Anchor anc;
     bool anc_cached = false;  // plain method: operator structure built for this geometry
     DeviceBuf centre;         // FP64 scratch of the centre integration
+    DeviceBuf pncnt64;        // FP64 accumulators of the sweep_fp64 sweeps
     Bricks bricks;            // brick segments of the geometry (built on first use)
     bool bricks_failed = false;
     std::string bricks_why;
@@ -183,6 +184,7 @@ int check_params(const omni3d_params *p, std::string *why)
     if (!(p->tol >= 0.0)) { *why = "tol must be >= 0"; return OMNI3D_ERR_ARG; }
     if (p->anchor_max_links < 0) { *why = "anchor_max_links must be >= 0"; return OMNI3D_ERR_ARG; }
     if (p->engine < OMNI3D_ENGINE_AUTO || p->engine > OMNI3D_ENGINE_BRICKS) { *why = "unknown engine"; return OMNI3D_ERR_ARG; }
+    if (p->sweep_fp64 != 0 && p->sweep_fp64 != 1) { *why = "sweep_fp64 must be 0 or 1"; return OMNI3D_ERR_ARG; }
     if (p->initial_guess != OMNI3D_INIT_ZERO && p->initial_guess != OMNI3D_INIT_CENTRE) {
         *why = "unknown initial_guess";
         return OMNI3D_ERR_ARG;
@@ -497,7 +499,7 @@ int omni3d_destroy(omni3d_ctx *ctx)
     ctx->adj_out.release();
     for (DeviceBuf *b : {&ctx->in_ax, &ctx->in_ay, &ctx->in_az, &ctx->in_aux, &ctx->in_pinit, &ctx->f32, &ctx->b16,
                          &ctx->curl, &ctx->pvol_a, &ctx->pvol_b, &ctx->pout, &ctx->cnt, &ctx->pncnt, &ctx->scratch,
-                         &ctx->flags, &ctx->centre})
+                         &ctx->flags, &ctx->centre, &ctx->pncnt64})
         b->release();
     for (auto &ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
@@ -698,7 +700,10 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
     if (ctx->geo.walk_rule == 3 && P.max_iter > 0)
         CK(ctx, run_walk(&ctx->geo, 3, F.curl, st));  // minimum-curl paths follow this field
     int engine = OMNI3D_ENGINE_LINES;
-    if (P.max_iter > 0) {
+    if (P.max_iter > 0 && P.sweep_fp64) {
+        if (P.engine == OMNI3D_ENGINE_BRICKS)
+            return fail(ctx, OMNI3D_ERR_STATE, "the brick engine accumulates in FP32 only (sweep_fp64)");
+    } else if (P.max_iter > 0) {
         engine = choose_engine(ctx, bf16, &rc);
         if (rc) return rc;
         if ((rc = engine_prepare(ctx, &engine, F, P.method))) return rc;
@@ -789,12 +794,25 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
                                 st));
         }
         cudaEventRecord(ctx->ev[1], st);
+        double2 *acc64 = nullptr;
+        if (P.sweep_fp64) {
+            CK(ctx, ctx->pncnt64.ensure(sizeof(double2) * (size_t)V));
+            acc64 = ctx->pncnt64.as<double2>();
+        }
         for (int it = 1; it <= K; it++) {
-            CK(ctx, init_accum(V, dpinit, seed && it == 1, acc, st));
-            cudaEventRecord(ctx->ev[5], st);
-            CK(ctx, engine_sweep(ctx, engine, F, P.method, bf16, pc, acc, st));
-            cudaEventRecord(ctx->ev[6], st);
-            CK(ctx, normalize(V, acc, pc, pn, dcnt, st));
+            if (acc64) {
+                CK(ctx, init_accum64(V, dpinit, seed && it == 1, acc64, st));
+                cudaEventRecord(ctx->ev[5], st);
+                CK(ctx, sweep_full64(ctx->geo, F, P.method, bf16, pc, acc64, st));
+                cudaEventRecord(ctx->ev[6], st);
+                CK(ctx, normalize64(V, acc64, pc, pn, dcnt, st));
+            } else {
+                CK(ctx, init_accum(V, dpinit, seed && it == 1, acc, st));
+                cudaEventRecord(ctx->ev[5], st);
+                CK(ctx, engine_sweep(ctx, engine, F, P.method, bf16, pc, acc, st));
+                cudaEventRecord(ctx->ev[6], st);
+                CK(ctx, normalize(V, acc, pc, pn, dcnt, st));
+            }
             done = it;
             if (P.tol > 0.0) {
                 CK(ctx, change_sums(V, pc, pn, P.gauge, P.gauge == OMNI3D_GAUGE_POINT ? ref : -1, rscratch, red2, st,
@@ -837,11 +855,21 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
         float *vol = ctx->pvol_a.as<float>();
         CK(ctx, cudaMemcpyAsync(vol, dpinit, sizeof(float) * (size_t)V, cudaMemcpyDeviceToDevice, st));
         CK(ctx, anchor_scatter(A, pc, vol, st));
-        CK(ctx, init_accum(V, dpinit, seed && its == 0, acc, st));
-        cudaEventRecord(ctx->ev[5], st);
-        CK(ctx, engine_sweep(ctx, engine, F, P.method, bf16, vol, acc, st));
-        cudaEventRecord(ctx->ev[6], st);
-        CK(ctx, normalize(V, acc, dpinit, dout, dcnt, st));
+        if (P.sweep_fp64) {  // the defect-correction sweep: FP64 sums and normalisation
+            CK(ctx, ctx->pncnt64.ensure(sizeof(double2) * (size_t)V));
+            double2 *acc64 = ctx->pncnt64.as<double2>();
+            CK(ctx, init_accum64(V, dpinit, seed && its == 0, acc64, st));
+            cudaEventRecord(ctx->ev[5], st);
+            CK(ctx, sweep_full64(ctx->geo, F, P.method, bf16, vol, acc64, st));
+            cudaEventRecord(ctx->ev[6], st);
+            CK(ctx, normalize64(V, acc64, dpinit, dout, dcnt, st));
+        } else {
+            CK(ctx, init_accum(V, dpinit, seed && its == 0, acc, st));
+            cudaEventRecord(ctx->ev[5], st);
+            CK(ctx, engine_sweep(ctx, engine, F, P.method, bf16, vol, acc, st));
+            cudaEventRecord(ctx->ev[6], st);
+            CK(ctx, normalize(V, acc, dpinit, dout, dcnt, st));
+        }
         done = its + 1;
     }
     CK(ctx, apply_gauge(V, P.gauge, ref, dcnt, dout, rscratch, st));

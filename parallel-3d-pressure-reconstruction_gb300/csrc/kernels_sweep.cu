@@ -72,6 +72,15 @@ struct LineWalk {
     }
 };
 
+// Contributions into the (pn, count) accumulators: one FP32 vector reduction, or (the FP64
+// defect-correction sweep) two FP64 reductions, each a native L2 atomic.
+__device__ __forceinline__ void acc_add(float2 *a, float x, float y) { atomicAdd(a, make_float2(x, y)); }
+__device__ __forceinline__ void acc_add(double2 *a, float x, float y)
+{
+    atomicAdd(&a->x, (double)x);
+    atomicAdd(&a->y, (double)y);
+}
+
 __device__ __forceinline__ void kahan_add(float &s, float &c, float x)
 {
     float y = x - c;
@@ -82,13 +91,13 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x)
 
 // Plain method: every voxel of the line, the entry included, receives p[entry] + I(v).
 // SELF = false leaves the entry out (the minimum-curl plain variant, K:2797-2936).
-template <bool BF16, bool SELF>
+template <bool BF16, bool SELF, typename ACC>
 __global__ void __launch_bounds__(256, 4) k_sweep_plain(Grid g, const LineRec *__restrict__ lines,
                                                      const uint32_t *__restrict__ gbase,
                                                      const uint32_t *__restrict__ desc, long long n_lines,
                                                      const float4 *__restrict__ f32,
                                                      const uint2 *__restrict__ b16,
-                                                     const float *__restrict__ p, float2 *pncnt)
+                                                     const float *__restrict__ p, ACC *pncnt)
 {
     long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (li >= n_lines) return;
@@ -96,14 +105,14 @@ __global__ void __launch_bounds__(256, 4) k_sweep_plain(Grid g, const LineRec *_
     LineWalk L;
     L.init(g, r, gbase, desc, li);
     const float pe = __ldg(p + r.e);
-    if (SELF) atomicAdd(pncnt + r.e, make_float2(pe, 1.0f));
+    if (SELF) acc_add(pncnt + r.e, pe, 1.0f);
     float4 gl = load_grad<BF16>(f32, b16, L.v);
     float I = 0.0f, comp = 0.0f;
     walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, false>(
         L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, nullptr, [&](int a, long long v, const float4 &gv, uint32_t) {
             float term = sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z));
             kahan_add(I, comp, term);
-            atomicAdd(pncnt + v, make_float2(pe + I, 1.0f));
+            acc_add(pncnt + v, pe + I, 1.0f);
             gl = gv;
         });
 }
@@ -112,14 +121,14 @@ __global__ void __launch_bounds__(256, 4) k_sweep_plain(Grid g, const LineRec *_
 // adds w_s (p[entry] + I_s) and w_s, w_s = s / sum_{t<=s} curl_t/1e4, once that sum is
 // nonzero.  Each curl/1e4 term is the reference's correctly rounded float division, so the
 // "sum != 0" decision (all curls so far zero) is the reference's.
-template <bool BF16>
+template <bool BF16, typename ACC>
 __global__ void __launch_bounds__(256, 4) k_sweep_weighted(Grid g, const LineRec *__restrict__ lines,
                                                         const uint32_t *__restrict__ gbase,
                                                         const uint32_t *__restrict__ desc, long long n_lines,
                                                         const float4 *__restrict__ f32,
                                                         const uint2 *__restrict__ b16,
                                                         const float *__restrict__ curl,
-                                                        const float *__restrict__ p, float2 *pncnt)
+                                                        const float *__restrict__ p, ACC *pncnt)
 {
     long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (li >= n_lines) return;
@@ -138,7 +147,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep_weighted(Grid g, const LineRec
             nseg += 1.0f;
             if (csum != 0.0f) {
                 float wc = __frcp_rn(csum) * nseg;
-                atomicAdd(pncnt + v, make_float2((pe + I) * wc, wc));
+                acc_add(pncnt + v, (pe + I) * wc, wc);
             }
             gl = gv;
         });
@@ -148,14 +157,14 @@ __global__ void __launch_bounds__(256, 4) k_sweep_weighted(Grid g, const LineRec
 // at the entry's curl and the entry receives (p[entry], 1) / C; step s adds its curl (not
 // divided by 1e4) and contributes w (p[entry] + I), w = (s + 1) / C, with no test for a zero
 // sum: a zero sum gives infinities, as in the reference.
-template <bool BF16>
+template <bool BF16, typename ACC>
 __global__ void __launch_bounds__(256, 4) k_sweep_weighted_raw(Grid g, const LineRec *__restrict__ lines,
                                                             const uint32_t *__restrict__ gbase,
                                                             const uint32_t *__restrict__ desc, long long n_lines,
                                                             const float4 *__restrict__ f32,
                                                             const uint2 *__restrict__ b16,
                                                             const float *__restrict__ curl,
-                                                            const float *__restrict__ p, float2 *pncnt)
+                                                            const float *__restrict__ p, ACC *pncnt)
 {
     long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (li >= n_lines) return;
@@ -167,7 +176,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep_weighted_raw(Grid g, const Lin
     float csum = BF16 ? __ldg(curl + L.v) : gl.w, nseg = 1.0f;
     {
         const float w0 = __frcp_rn(csum);
-        atomicAdd(pncnt + L.v, make_float2(pe * w0, w0));
+        acc_add(pncnt + L.v, pe * w0, w0);
     }
     float I = 0.0f, comp = 0.0f;
     walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, false>(
@@ -177,7 +186,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep_weighted_raw(Grid g, const Lin
             csum += cn;
             nseg += 1.0f;
             const float wc = __frcp_rn(csum) * nseg;
-            atomicAdd(pncnt + v, make_float2((pe + I) * wc, wc));
+            acc_add(pncnt + v, (pe + I) * wc, wc);
             gl = gv;
         });
 }
@@ -188,14 +197,14 @@ __global__ void __launch_bounds__(256, 4) k_sweep_weighted_raw(Grid g, const Lin
 // also pauses on curl == 0, a y/z step walks through it without adding that step's
 // increment); a good voxel after a pause restarts the segment at that voxel; the z
 // branch keeps the running curl/count sums on restart.
-template <bool BF16>
+template <bool BF16, typename ACC>
 __global__ void __launch_bounds__(256, 4) k_sweep_select(Grid g, const LineRec *__restrict__ lines,
                                                       const uint32_t *__restrict__ gbase,
                                                       const uint32_t *__restrict__ desc, long long n_lines,
                                                       const float4 *__restrict__ f32,
                                                       const uint2 *__restrict__ b16,
                                                       const float *__restrict__ curl,
-                                                      const float *__restrict__ p, float2 *pncnt)
+                                                      const float *__restrict__ p, ACC *pncnt)
 {
     long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (li >= n_lines) return;
@@ -229,7 +238,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep_select(Grid g, const LineRec *
                     csum += cn * 1.0e-4f;
                     nseg += 1.0f;
                     float wc = __frcp_rn(csum) * nseg;
-                    atomicAdd(pncnt + v, make_float2((p0 + I) * wc, wc));
+                    acc_add(pncnt + v, (p0 + I) * wc, wc);
                 }
                 bool enter_bad = (a == 0) ? ((!paused && cn >= thr) || cn == 0.0f) : (!paused && cn >= thr);
                 if (enter_bad) paused = true;
@@ -424,10 +433,9 @@ unsigned grid_for(long long n, int threads = 256)
     return (unsigned)b;
 }
 
-}  // namespace
-
-cudaError_t sweep_full(const Geometry &geo, const Field &f, int method, bool bf16, const float *p,
-                       float2 *pncnt, cudaStream_t st)
+template <typename ACC>
+cudaError_t sweep_full_t(const Geometry &geo, const Field &f, int method, bool bf16, const float *p, ACC *pncnt,
+                         cudaStream_t st)
 {
     if (geo.n_lines == 0) return cudaSuccess;
     // every pointer the kernels dereference must be set: refuse to launch otherwise
@@ -438,45 +446,97 @@ cudaError_t sweep_full(const Geometry &geo, const Field &f, int method, bool bf1
     const int acc = method_accum(method);
     if (acc == kAccWeighted) {
         if (bf16)
-            k_sweep_weighted<true><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
+            k_sweep_weighted<true, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
                                                            geo.n_lines, f.f32, f.bf16, f.curl, p, pncnt);
         else
-            k_sweep_weighted<false><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
+            k_sweep_weighted<false, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
                                                             geo.n_lines, f.f32, f.bf16, f.curl, p, pncnt);
         OM_COUNT_LAUNCH();
     } else if (acc == kAccWeightedRawCurl) {
         if (bf16)
-            k_sweep_weighted_raw<true><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
+            k_sweep_weighted_raw<true, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
                                                                geo.n_lines, f.f32, f.bf16, f.curl, p, pncnt);
         else
-            k_sweep_weighted_raw<false><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
+            k_sweep_weighted_raw<false, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
                                                                 geo.n_lines, f.f32, f.bf16, f.curl, p, pncnt);
         OM_COUNT_LAUNCH();
     } else if (acc == kAccSelect) {
         if (bf16)
-            k_sweep_select<true><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
+            k_sweep_select<true, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
                                                          f.f32, f.bf16, f.curl, p, pncnt);
         else
-            k_sweep_select<false><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
+            k_sweep_select<false, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
                                                           f.f32, f.bf16, f.curl, p, pncnt);
         OM_COUNT_LAUNCH();
     } else if (acc == kAccPlainNoEntry) {
         if (bf16)
-            k_sweep_plain<true, false><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
+            k_sweep_plain<true, false, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
                                                                geo.n_lines, f.f32, f.bf16, p, pncnt);
         else
-            k_sweep_plain<false, false><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
+            k_sweep_plain<false, false, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
                                                                 geo.n_lines, f.f32, f.bf16, p, pncnt);
         OM_COUNT_LAUNCH();
     } else {
         if (bf16)
-            k_sweep_plain<true, true><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
+            k_sweep_plain<true, true, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
                                                               geo.n_lines, f.f32, f.bf16, p, pncnt);
         else
-            k_sweep_plain<false, true><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
+            k_sweep_plain<false, true, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
                                                                geo.n_lines, f.f32, f.bf16, p, pncnt);
         OM_COUNT_LAUNCH();
     }
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t sweep_full(const Geometry &geo, const Field &f, int method, bool bf16, const float *p, float2 *pncnt,
+                       cudaStream_t st)
+{
+    return sweep_full_t(geo, f, method, bf16, p, pncnt, st);
+}
+
+cudaError_t sweep_full64(const Geometry &geo, const Field &f, int method, bool bf16, const float *p, double2 *pncnt,
+                         cudaStream_t st)
+{
+    return sweep_full_t(geo, f, method, bf16, p, pncnt, st);
+}
+
+namespace {
+
+__global__ void k_init_accum64(long long V, const float *__restrict__ p_init, int seed, double2 *pncnt)
+{
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < V;
+         v += (long long)gridDim.x * blockDim.x)
+        pncnt[v] = make_double2(seed && p_init ? (double)p_init[v] : 0.0, 0.0);
+}
+
+__global__ void k_normalize64(long long V, const double2 *__restrict__ pncnt, const float *__restrict__ p_keep,
+                              float *p_out, float *cnt_out)
+{
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < V;
+         v += (long long)gridDim.x * blockDim.x) {
+        const double2 a = pncnt[v];
+        const float pk = p_keep ? p_keep[v] : 0.0f;
+        if (p_out) p_out[v] = a.y > 0.0 ? (float)(a.x / a.y) : pk;
+        if (cnt_out) cnt_out[v] = (float)a.y;
+    }
+}
+
+}  // namespace
+
+cudaError_t init_accum64(long long V, const float *p_init, bool seed, double2 *pncnt, cudaStream_t st)
+{
+    k_init_accum64<<<grid_for(V), 256, 0, st>>>(V, p_init, seed ? 1 : 0, pncnt);
+    OM_COUNT_LAUNCH();
+    return cudaGetLastError();
+}
+
+cudaError_t normalize64(long long V, const double2 *pncnt, const float *p_keep, float *p_out, float *cnt_out,
+                        cudaStream_t st)
+{
+    k_normalize64<<<grid_for(V), 256, 0, st>>>(V, pncnt, p_keep, p_out, cnt_out);
+    OM_COUNT_LAUNCH();
     return cudaGetLastError();
 }
 

@@ -178,6 +178,13 @@ inline int method_accum(int method)
 // method: OMNI3D_METHOD_*; p is read at line entries / segment starts.
 cudaError_t sweep_full(const Geometry &geo, const Field &f, int method, bool bf16,
                        const float *p, float2 *pncnt, cudaStream_t st);
+// The same sweep accumulated in FP64 (two FP64 L2 reductions per contribution): the
+// defect-correction sweep of params.sweep_fp64.
+cudaError_t sweep_full64(const Geometry &geo, const Field &f, int method, bool bf16, const float *p,
+                         double2 *pncnt, cudaStream_t st);
+cudaError_t init_accum64(long long V, const float *p_init, bool seed, double2 *pncnt, cudaStream_t st);
+cudaError_t normalize64(long long V, const double2 *pncnt, const float *p_keep, float *p_out, float *cnt_out,
+                        cudaStream_t st);
 
 // p_out[v] = cnt > 0 ? pn / cnt : p_keep[v]; cnt_out[v] = cnt (either may be null).
 cudaError_t normalize(long long V, const float2 *pncnt, const float *p_keep, float *p_out,

@@ -49,7 +49,8 @@ class Omni3D:
 
     def __init__(self, dims, spacing, dirs, *, density=1.0, line_spacing=1.0, max_iter=4, threshold=0.0,
                  method="plain", solver="anchor", grad="f32", tol=0.0, gauge="none", ref=(0, 0, 0),
-                 seed_first_iteration=True, device=0, anchor_max_links=0, engine="auto", initial_guess="zero"):
+                 seed_first_iteration=True, device=0, anchor_max_links=0, engine="auto", initial_guess="zero",
+                 sweep_fp64=False):
         nx, ny, nz = (int(d) for d in dims)
         self.dims = (nx, ny, nz)
         self.V = nx * ny * nz
@@ -76,6 +77,7 @@ class Omni3D:
         P.anchor_max_links = int(anchor_max_links)
         P.engine = _ENGINES[engine]
         P.initial_guess = _INITS[initial_guess]
+        P.sweep_fp64 = int(bool(sweep_fp64))
         self.params = P
         self.method = method
         self.solve_count = 0

@@ -314,6 +314,35 @@ def test_solve_into_caller_buffers(omni):
             s.solve(f["ax"], f["ay"], f["az"], out=[np.empty(3, np.float32)] * 2)
 
 
+@pytest.mark.parametrize("method", ["plain", "select"])
+def test_fp64_defect_correction_sweep(omni, orc, method):
+    """sweep_fp64: the full sweep accumulates in FP64.  With one iteration the solve is that
+    sweep alone, so its distance to the FP64 oracle drops below the FP32-accumulated one's."""
+    dims = (26, 22, 19)
+    f = _field(dims, seed=15, sphere=4.0)
+    dirs = omni.icosphere(4)  # 642 directions: about a thousand contributions per voxel
+    p0 = _pinit(dims)
+    curl = orc.curl(dims, f["spacing"], f["ax"], f["ay"], f["az"], f["mask"])
+    thr = float(np.finfo(np.float32).max)
+    mode = 0 if method == "plain" else 1
+    ep, ecnt = orc.solve(dims, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p0, 1, mode=mode, thr=thr, curl=curl,
+                         precision="f64", nthreads=8)
+    err = {}
+    for fp64 in (False, True):
+        for solver in ("anchor", "sweep"):
+            with omni.Omni3D(dims, f["spacing"], dirs, max_iter=1, method=method, threshold=thr, solver=solver,
+                             sweep_fp64=fp64) as s:
+                r = s.solve(f["ax"], f["ay"], f["az"], curl=curl if method == "select" else None, p_init=p0)
+            err[(fp64, solver)] = synthetic.relative_l2(r.p, ep, gauge="none")
+            if method == "plain":
+                np.testing.assert_array_equal(r.count.reshape(-1), ecnt.astype(np.float32))
+    for solver in ("anchor", "sweep"):
+        assert err[(True, solver)] < err[(False, solver)] < TOL_PN, err
+    with omni.Omni3D(dims, f["spacing"], dirs, max_iter=1, sweep_fp64=True, engine="bricks") as s:
+        with pytest.raises(omni.Omni3DError):
+            s.solve(f["ax"], f["ay"], f["az"])
+
+
 def test_counts_deterministic(omni):
     dims = (20, 20, 20)
     f = _field(dims, seed=12)
