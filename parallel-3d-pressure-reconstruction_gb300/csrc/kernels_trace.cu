@@ -18,13 +18,20 @@ constexpr int kScanBlock = 1024;
 constexpr int kScanItems = 4;  // items per thread
 constexpr long long kScanTile = (long long)kScanBlock * kScanItems;
 
-// Candidate order: (group of `gsize` neighbouring directions, block of 32 lattice points,
-// direction within the group, point within the block).  A warp then holds 32 adjacent
-// lines of one direction and a block of warps holds the same lattice patch of several
-// nearly parallel directions, which walk through the same voxels at the same time.
+// Candidate order: (group of `gsize` neighbouring directions, 8 x 4 tile of lattice points,
+// direction within the group, point within the tile).  A warp then holds the 32 lines of
+// one direction through an 8 x 4 patch of its lattice plane, a compact bundle whose
+// staircases share voxels and 32-byte sectors along the whole walk (a 32 x 1 row of the
+// lattice spreads over 32 lines' worth of width and shares far fewer), and a block of
+// warps holds the same patch of several nearly parallel directions, which walk through the
+// same voxels at the same time.
+constexpr int kTileU = 8;  // lattice columns per tile
+constexpr int kTileV = 4;  // lattice rows per tile
+static_assert(kTileU * kTileV == 32 && (kTileU & (kTileU - 1)) == 0, "a tile is one warp of lines");
 struct CandOrder {
     long long ng2;    // lattice points per direction
-    long long nblk;   // 32-point lattice blocks per direction
+    long long tu;     // tiles across a lattice row
+    long long nblk;   // tiles per direction
     int gsize;        // directions per group
     int nv;
 };
@@ -40,9 +47,11 @@ __device__ __forceinline__ bool trace_candidate(const Grid &g, const DirEntry *d
     long long blk = r / per_block;
     r -= blk * per_block;
     int d = (int)(grp * co.gsize + r / 32);
-    long long pt = blk * 32 + (r & 31);
+    const long long u = (blk % co.tu) * kTileU + (r & (kTileU - 1));
+    const long long v = (blk / co.tu) * kTileV + ((r & 31) / kTileU);
     *dir = d;
-    if (d >= co.nv || pt >= co.ng2) return false;
+    if (d >= co.nv || u >= g.ng || v >= g.ng) return false;
+    const long long pt = u + v * g.ng;  // lattice point: column u, row v
     DirEntry D = dirs[d];
     om_line_offset(pt, g.ng, g.ls, D, o[0], o[1], o[2]);
     om_cross2point(g, o[0], o[1], o[2], D.k1, D.k2, D.k3, D.cas, in, out);
@@ -339,7 +348,8 @@ cudaError_t build_geometry(Geometry *g, cudaStream_t st, std::string *err)
     const Grid &G = g->grid;
     CandOrder co;
     co.ng2 = (long long)G.ng * G.ng;
-    co.nblk = (co.ng2 + 31) / 32;
+    co.tu = (G.ng + kTileU - 1) / kTileU;
+    co.nblk = co.tu * ((G.ng + kTileV - 1) / kTileV);
     co.gsize = std::max(1, std::min(g->dir_group, g->nv));
     co.nv = g->nv;
     long long ngroups = (g->nv + co.gsize - 1) / co.gsize;

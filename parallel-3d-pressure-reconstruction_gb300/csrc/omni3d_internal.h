@@ -51,7 +51,7 @@ struct LineRec {
 struct Geometry {
     Grid grid;
     int nv = 0;
-    int dir_group = 8;              // neighbouring directions interleaved per lattice block
+    int dir_group = 4;              // neighbouring directions interleaved per lattice tile
     DirEntry *d_dirs = nullptr;
     float4 *d_off = nullptr;        // per line: centred offset (x, y, z) of its lattice point
     LineRec *d_lines = nullptr;

@@ -38,3 +38,26 @@ def omni():
     omni3d.build()
     omni3d.lib()
     return omni3d
+
+
+def _match_lines(got, exp):
+    """Match the library's line table to the oracle's rows.  The library orders lines for
+    locality (direction groups, lattice tiles), the oracle by (direction, lattice point), so
+    the two tables must hold the same rows as multisets; each oracle row is then located in
+    the library's table by its (entry, exit, direction) key.  Returns, per oracle row, the
+    library rows with that key: one row, or several where lattice points of one direction
+    have lines that share entry and exit voxels (line spacing below a cell)."""
+    import numpy as np
+
+    assert got.shape == exp.shape
+    order = lambda t: t[np.lexsort(t.T[::-1])]
+    np.testing.assert_array_equal(order(got), order(exp))
+    where = {}
+    for i, r in enumerate(got[:, :3].tolist()):
+        where.setdefault(tuple(r), []).append(i)
+    return [where[tuple(r)] for r in exp[:, :3].tolist()]
+
+
+@pytest.fixture(scope="session")
+def match_lines():
+    return _match_lines

@@ -51,7 +51,7 @@ def _lines_oracle(orc, dims, ls, dirs):
 
 
 @pytest.mark.parametrize("dims,ls,level", [((20, 17, 13), 1.0, 3), ((16, 16, 16), 0.7, 3), ((12, 9, 15), 1.0, 2)])
-def test_line_table_bit_exact(omni, orc, dims, ls, level):
+def test_line_table_bit_exact(omni, orc, match_lines, dims, ls, level):
     dirs = omni.icosphere(level)
     with omni.Omni3D(dims, 1e-3, dirs, line_spacing=ls, max_iter=1) as s:
         info = s.geometry_info()
@@ -59,17 +59,14 @@ def test_line_table_bit_exact(omni, orc, dims, ls, level):
         got = s.line_table().astype(np.int64)
         got[:, 0] &= 0xFFFFFFFF
         got[:, 1] &= 0xFFFFFFFF
-        # the library stores directions in its own processing order, lattice order within
-        perm = np.argsort(got[:, 2], kind="stable")
         exp, geo = _lines_oracle(orc, dims, ls, dirs)
-        assert got.shape == exp.shape
-        np.testing.assert_array_equal(got[perm], exp)
+        at = match_lines(got, exp)  # the same rows, in the library's own order
         assert info["n_units"] == int((exp[:, 3] + 1).sum())
-        # staircases of a sample of lines
+        # staircases of a sample of lines (where lines share a key, one of them walks alike)
         for k in range(0, len(exp), max(1, len(exp) // 60)):
             io, xyz = geo[k]
             ax = orc.walk(dims, io, xyz, dirs[exp[k, 2]])
-            np.testing.assert_array_equal(s.line_steps(int(perm[k])), ax)
+            assert any(np.array_equal(s.line_steps(i), ax) for i in at[k]), k
 
 
 def test_curl_bit_exact(omni, orc):

@@ -33,7 +33,7 @@ def _pinit(dims, seed=1):
 
 
 @pytest.mark.parametrize("method,mode,rule", VARIANTS)
-def test_variant_staircases_bit_exact(omni, orc, method, mode, rule):
+def test_variant_staircases_bit_exact(omni, orc, match_lines, method, mode, rule):
     dims = (17, 14, 12)
     f = _field(dims, seed=50 + mode, sphere=3.0)
     dirs = omni.icosphere(3)
@@ -44,10 +44,8 @@ def test_variant_staircases_bit_exact(omni, orc, method, mode, rule):
         got = s.line_table().astype(np.int64)
         got[:, 0] &= 0xFFFFFFFF
         got[:, 1] &= 0xFFFFFFFF
-        perm = np.argsort(got[:, 2], kind="stable")
-        rows = got[perm]
         X, Y, Z = dims
-        k = 0
+        exp, walks = [], []
         stopped = 0
         for d in range(len(dirs)):
             valid, inout, nsteps, xyz = orc.trace_direction(dims, 1.0, dirs[d])
@@ -56,13 +54,13 @@ def test_variant_staircases_bit_exact(omni, orc, method, mode, rule):
                 e = io[0] + io[1] * X + io[2] * X * Y
                 x = io[3] + io[4] * X + io[5] * X * Y
                 ax = orc.walk(dims, io, xyz[pt], dirs[d], rule=rule, curl=curl, allow_early_stop=True)
-                assert (rows[k, 0], rows[k, 1], rows[k, 2]) == (e, x, d)
-                assert rows[k, 3] == len(ax)
+                exp.append((e, x, d, len(ax)))
+                walks.append(ax)
                 stopped += len(ax) < abs(io[3] - io[0]) + abs(io[4] - io[1]) + abs(io[5] - io[2])
-                if k % 7 == 0:
-                    np.testing.assert_array_equal(s.line_steps(int(perm[k])), ax)
-                k += 1
-        assert k == len(rows)
+        # the same (entry, exit, direction, steps) rows, in the library's own order
+        at = match_lines(got, np.array(exp, np.int64).reshape(-1, 4))
+        for k in range(0, len(exp), 7):
+            assert any(np.array_equal(s.line_steps(i), walks[k]) for i in at[k]), k
         if rule in (1, 2):
             assert stopped > 0  # lines that would enter the j = 0 face stop before it
 
