@@ -14,8 +14,13 @@
 // (up to the order of floating-point sums) at a fraction of the cost.
 //
 // The operator is built from the same line descriptors as the sweep: a marking pass finds
-// the anchors, a counting pass sizes each anchor's row, a filling pass writes
-// (column = start anchor, weight) pairs and accumulates b and c.
+// the anchors, the geometry's line counts size each anchor's row, a filling pass writes
+// (column = start anchor, weight) pairs and accumulates b and c.  The filling pass learns
+// whether a visited voxel is an anchor from the field gather itself: for the duration of
+// the pass the anchors' packed field entries carry a flag in a bit no value uses (the sign
+// of the curl in .w of the FP32 field, curl being non-negative; bit 31 of the BF16 entry's
+// second word), so a step costs one gather instead of a gather and a bitmap load.  A field
+// with a negative curl value keeps the bitmap.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -35,11 +40,23 @@ __device__ __forceinline__ float bf_hi(uint32_t u) { return __uint_as_float(u & 
 template <bool BF16>
 __device__ __forceinline__ float4 load_grad(const float4 *f32, const uint2 *b16, long long v)
 {
-    if (BF16) {
-        uint2 u = __ldg(b16 + v);
-        return make_float4(bf_lo(u.x), bf_hi(u.x), bf_lo(u.y), 0.0f);
-    }
+    if (BF16) return load_grad_b16(b16, v);
     return __ldg(f32 + v);
+}
+
+// Anchor flag of a gathered voxel: with FB the sign bit of its .w (the flag the filling
+// pass sets in the field), else its bit of the bitmap word gathered beside it.
+template <bool FB>
+__device__ __forceinline__ bool anchor_of(const float4 &gv, uint32_t word, long long v)
+{
+    return FB ? (__float_as_uint(gv.w) >> 31) != 0u : ((word >> (v & 31)) & 1u) != 0u;
+}
+
+// Curl from .w of the FP32 field: under FB its sign bit is the anchor flag.
+template <bool FB>
+__device__ __forceinline__ float curl_of(const float4 &gv)
+{
+    return FB ? fabsf(gv.w) : gv.w;
 }
 
 __device__ __forceinline__ float sel3(int a, float x, float y, float z)
@@ -75,14 +92,15 @@ struct Sink {
 };
 
 // Record one contribution of weight wt and integral I into voxel v from the segment that
-// started at voxel `start`.  `word` is the anchor bitmap's word of v when the caller has
-// loaded it (emit_w), else emit loads it.
+// started at voxel `start`.  emit_w is told whether v is an anchor (anchor_of); emit
+// looks it up in the bitmap.
 template <int PASS>
-__device__ __forceinline__ void emit_w(const Sink &S, long long v, long long start, float wt, float I, uint32_t word)
+__device__ __forceinline__ void emit_w(const Sink &S, long long v, long long start, float wt, float I, bool anchor)
 {
     if (PASS == kMark) return;
-    if (!((word >> (v & 31)) & 1u)) return;
+    if (!anchor) return;
     int row = __ldg(S.id + v);
+    if (row < 0) return;  // not an anchor after all: nothing to index
     if (PASS == kRhs) {  // plain method, operator cached: only b = sum I is field-dependent
         atomicAdd(S.b + row, I);
         return;
@@ -139,7 +157,7 @@ struct Walk {
 
 // Plain method: anchors are the entries; every voxel of a line takes (p[entry] + I, 1).
 // SELF = false leaves the entry's own term out (the minimum-curl plain variant).
-template <int PASS, bool BF16, bool SELF>
+template <int PASS, bool BF16, bool SELF, bool FB>
 __global__ void __launch_bounds__(256, 4) k_anchor_plain(Grid g, const LineRec *__restrict__ lines,
                                                       const uint32_t *__restrict__ gbase,
                                                       const uint32_t *__restrict__ desc, long long n_lines,
@@ -159,18 +177,18 @@ __global__ void __launch_bounds__(256, 4) k_anchor_plain(Grid g, const LineRec *
     if (SELF) emit<PASS>(S, e, e, 1.0f, 0.0f);
     float4 gl = load_grad<BF16>(f32, b16, e);
     float I = 0.0f, comp = 0.0f;
-    // the field and the anchor bitmap word of every voxel gathered in batches
-    walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, true>(
+    // the field (and without FB the anchor bitmap word) of every voxel gathered in batches
+    walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, !FB>(
         L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, long long v, const float4 &gv, uint32_t word) {
             kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
             gl = gv;
-            emit_w<PASS>(S, v, e, 1.0f, I, word);
+            emit_w<PASS>(S, v, e, 1.0f, I, anchor_of<FB>(gv, word, v));
         });
 }
 
 // Weighted method: the walk of k_sweep_weighted (K:1993-2135); anchors are the entries
 // (the marking pass is the plain method's), the entry itself receives nothing.
-template <int PASS, bool BF16>
+template <int PASS, bool BF16, bool FB>
 __global__ void __launch_bounds__(256, 4) k_anchor_weighted(Grid g, const LineRec *__restrict__ lines,
                                                          const uint32_t *__restrict__ gbase,
                                                          const uint32_t *__restrict__ desc, long long n_lines,
@@ -187,20 +205,20 @@ __global__ void __launch_bounds__(256, 4) k_anchor_weighted(Grid g, const LineRe
     const long long e = r.e;
     float4 gl = load_grad<BF16>(f32, b16, e);
     float I = 0.0f, comp = 0.0f, csum = 0.0f, nseg = 0.0f;
-    walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, true>(
+    walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, !FB>(
         L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, long long v, const float4 &gv, uint32_t word) {
-            float cn = BF16 ? __ldg(curl + v) : gv.w;
+            float cn = BF16 ? __ldg(curl + v) : curl_of<FB>(gv);
             kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
             csum += __fdiv_rn(cn, 1.0e4f);  // the weights as in k_sweep_weighted
             nseg += 1.0f;
-            if (csum != 0.0f) emit_w<PASS>(S, v, e, __frcp_rn(csum) * nseg, I, word);
+            if (csum != 0.0f) emit_w<PASS>(S, v, e, __frcp_rn(csum) * nseg, I, anchor_of<FB>(gv, word, v));
             gl = gv;
         });
 }
 
 // Weighted method with raw curl sums (the minimum-curl variant): the walk of
 // k_sweep_weighted_raw; anchors are the entries, the entry takes its own term.
-template <int PASS, bool BF16>
+template <int PASS, bool BF16, bool FB>
 __global__ void __launch_bounds__(256, 4) k_anchor_weighted_raw(Grid g, const LineRec *__restrict__ lines,
                                                              const uint32_t *__restrict__ gbase,
                                                              const uint32_t *__restrict__ desc, long long n_lines,
@@ -216,23 +234,23 @@ __global__ void __launch_bounds__(256, 4) k_anchor_weighted_raw(Grid g, const Li
     L.init(g, r, gbase, desc, li);
     const long long e = r.e;
     float4 gl = load_grad<BF16>(f32, b16, e);
-    float csum = BF16 ? __ldg(curl + e) : gl.w, nseg = 1.0f;
-    emit<PASS>(S, e, e, __frcp_rn(csum), 0.0f);
+    float csum = BF16 ? __ldg(curl + e) : curl_of<FB>(gl), nseg = 1.0f;
+    emit_w<PASS>(S, e, e, __frcp_rn(csum), 0.0f, FB ? anchor_of<FB>(gl, 0u, e) : is_anchor(S.bits, e));
     float I = 0.0f, comp = 0.0f;
-    walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, true>(
+    walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, !FB>(
         L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, long long v, const float4 &gv, uint32_t word) {
-            float cn = BF16 ? __ldg(curl + v) : gv.w;
+            float cn = BF16 ? __ldg(curl + v) : curl_of<FB>(gv);
             kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
             csum += cn;
             nseg += 1.0f;
-            emit_w<PASS>(S, v, e, __frcp_rn(csum) * nseg, I, word);
+            emit_w<PASS>(S, v, e, __frcp_rn(csum) * nseg, I, anchor_of<FB>(gv, word, v));
             gl = gv;
         });
 }
 
 // Selected method: the state machine of k_sweep_select (K:2280-2537); anchors are the
 // segment starts.
-template <int PASS, bool BF16>
+template <int PASS, bool BF16, bool FB>
 __global__ void __launch_bounds__(256, 4) k_anchor_select(Grid g, const LineRec *__restrict__ lines,
                                                        const uint32_t *__restrict__ gbase,
                                                        const uint32_t *__restrict__ desc, long long n_lines,
@@ -250,17 +268,18 @@ __global__ void __launch_bounds__(256, 4) k_anchor_select(Grid g, const LineRec 
     if (PASS == kFill) gl = load_grad<BF16>(f32, b16, L.v);
     // the FP32 field carries curl in .w: one gather per step in the filling pass
     constexpr bool kW = PASS == kFill && !BF16;
-    float ce = kW ? gl.w : __ldg(curl + L.v);
+    float ce = kW ? curl_of<FB>(gl) : __ldg(curl + L.v);
     bool started = !(ce == 0.0f || ce > thr);
     bool paused = false;
     long long start = L.v;
     if (PASS == kMark && started) S.flag[start] = 1;
     float I = 0.0f, comp = 0.0f, csum = 0.0f, nseg = 0.0f;
-    // the filling pass gathers the field and the anchor bitmap word of every voxel in batches
+    // the filling pass gathers the field (and without FB the anchor bitmap word) of every
+    // voxel in batches
     constexpr int kGrad = PASS == kFill ? (BF16 ? kGradBF16 : kGradF32) : kNoGrad;
-    walk_steps<kWalkBatch, kGrad, PASS == kFill>(
+    walk_steps<kWalkBatch, kGrad, PASS == kFill && !FB>(
         L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, long long v, const float4 &gv, uint32_t word) {
-            const float cn = kW ? gv.w : __ldg(curl + v);
+            const float cn = kW ? curl_of<FB>(gv) : __ldg(curl + v);
             if (!started) {
                 bool ok = (a == 0) ? (cn != 0.0f && cn < thr) : (cn != 0.0f);
                 if (ok) {
@@ -276,7 +295,7 @@ __global__ void __launch_bounds__(256, 4) k_anchor_select(Grid g, const LineRec 
                         kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
                     csum += cn * 1.0e-4f;  // the weights as in k_sweep_select
                     nseg += 1.0f;
-                    if (PASS == kFill) emit_w<PASS>(S, v, start, __frcp_rn(csum) * nseg, I, word);
+                    if (PASS == kFill) emit_w<PASS>(S, v, start, __frcp_rn(csum) * nseg, I, anchor_of<FB>(gv, word, v));
                     else emit<PASS>(S, v, start, __frcp_rn(csum) * nseg, I);
                 }
                 bool enter_bad = (a == 0) ? ((!paused && cn >= thr) || cn == 0.0f) : (!paused && cn >= thr);
@@ -497,8 +516,72 @@ unsigned grid_for(long long n, int threads = 256)
     return (unsigned)b;
 }
 
+// Set (set = 1) or clear the anchor flag in the field entries of the n anchors: bit 31 of
+// the BF16 entry's second word when b16 is given, else the sign bit of the FP32 entry's .w.
+__global__ void k_field_flags(long long n, const uint32_t *__restrict__ vox, float4 *f32, uint2 *b16, int set)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const uint32_t v = vox[i];
+        uint32_t *u = b16 ? &b16[v].y : reinterpret_cast<uint32_t *>(&f32[v].w);
+        *u = set ? (*u | 0x80000000u) : (*u & 0x7fffffffu);
+    }
+}
+
+// *any = 1 when some curl value has its sign bit set (negative, or -0).
+__global__ void k_sign_any(long long V, const float *__restrict__ curl, uint32_t *any)
+{
+    bool neg = false;
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x)
+        neg |= (__float_as_uint(curl[v]) >> 31) != 0u;
+    if (__any_sync(0xffffffffu, neg) && (threadIdx.x & 31) == 0) *any = 1u;
+}
+
+// Launch the pass for the method's accumulation kind.  BF16: the gradient gathers read the
+// BF16 storage; FB: the anchors are flagged in the field (bitmap otherwise).
+template <int PASS, bool BF16, bool FB>
+void launch_pass(int acc, const Geometry &geo, const Field &f, const Sink &S, cudaStream_t st)
+{
+    const unsigned blocks = (unsigned)((geo.n_lines + 255) / 256);
+    const Grid &g = geo.grid;
+    if constexpr (PASS == kFill) {
+        if (acc == kAccWeightedRawCurl) {
+            k_anchor_weighted_raw<kFill, BF16, FB><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
+                                                                           geo.n_lines, f.f32, f.bf16, f.curl, S);
+            OM_COUNT_LAUNCH();
+            return;
+        }
+        if (acc == kAccWeighted) {
+            k_anchor_weighted<kFill, BF16, FB><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
+                                                                       geo.n_lines, f.f32, f.bf16, f.curl, S);
+            OM_COUNT_LAUNCH();
+            return;
+        }
+        if (acc == kAccPlainNoEntry) {
+            k_anchor_plain<kFill, BF16, false, FB><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
+                                                                           geo.n_lines, f.f32, f.bf16, S);
+            OM_COUNT_LAUNCH();
+            return;
+        }
+    }
+    if constexpr (PASS != kRhs) {
+        if (acc == kAccSelect) {
+            k_anchor_select<PASS, BF16, FB><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
+                                                                    geo.n_lines, f.f32, f.bf16, f.curl, S);
+            OM_COUNT_LAUNCH();
+            return;
+        }
+    }
+    // plain method, and the marking pass of every method whose anchors are the entries
+    k_anchor_plain<PASS, BF16, true, FB><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
+                                                                 f.f32, f.bf16, S);
+    OM_COUNT_LAUNCH();
+}
+
+// fb: the anchors' field entries carry the anchor flag (k_field_flags); the BF16 storage
+// always can, the FP32 field when no curl value has its sign bit set.
 template <int PASS>
-cudaError_t run_pass(const Geometry &geo, const Field &f, int method, bool bf16, const Sink &S, cudaStream_t st)
+cudaError_t run_pass(const Geometry &geo, const Field &f, int method, bool bf16, bool fb, const Sink &S,
+                     cudaStream_t st)
 {
     if (geo.n_lines == 0) return cudaSuccess;
     // every pointer the pass dereferences must be set: refuse to launch otherwise
@@ -513,49 +596,10 @@ cudaError_t run_pass(const Geometry &geo, const Field &f, int method, bool bf16,
     if (acc == kAccSelect || (weighted && PASS == kFill)) ok = ok && f.curl && (bf16 || f.f32);
     if (PASS == kRhs && acc != kAccPlain) ok = false;  // only the plain operator is cached
     if (!ok) return cudaErrorInvalidValue;
-    unsigned blocks = (unsigned)((geo.n_lines + 255) / 256);
-    const Grid &g = geo.grid;
-    if (acc == kAccWeightedRawCurl && PASS == kFill) {
-        if (bf16)
-            k_anchor_weighted_raw<kFill, true><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
-                                                                       geo.n_lines, f.f32, f.bf16, f.curl, S);
-        else
-            k_anchor_weighted_raw<kFill, false><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
-                                                                        geo.n_lines, f.f32, f.bf16, f.curl, S);
-        OM_COUNT_LAUNCH();
-    } else if (acc == kAccWeighted && PASS == kFill) {
-        if (bf16)
-            k_anchor_weighted<kFill, true><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
-                                                                   geo.n_lines, f.f32, f.bf16, f.curl, S);
-        else
-            k_anchor_weighted<kFill, false><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
-                                                                    geo.n_lines, f.f32, f.bf16, f.curl, S);
-        OM_COUNT_LAUNCH();
-    } else if (acc == kAccSelect) {
-        if (bf16)
-            k_anchor_select<PASS, true><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
-                                                                f.f32, f.bf16, f.curl, S);
-        else
-            k_anchor_select<PASS, false><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
-                                                                 f.f32, f.bf16, f.curl, S);
-        OM_COUNT_LAUNCH();
-    } else if (acc == kAccPlainNoEntry && PASS == kFill) {
-        if (bf16)
-            k_anchor_plain<PASS, true, false><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
-                                                                      geo.n_lines, f.f32, f.bf16, S);
-        else
-            k_anchor_plain<PASS, false, false><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
-                                                                       geo.n_lines, f.f32, f.bf16, S);
-        OM_COUNT_LAUNCH();
-    } else {  // plain method, and the marking pass of every method whose anchors are the entries
-        if (bf16)
-            k_anchor_plain<PASS, true, true><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
-                                                                     geo.n_lines, f.f32, f.bf16, S);
-        else
-            k_anchor_plain<PASS, false, true><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
-                                                                      geo.n_lines, f.f32, f.bf16, S);
-        OM_COUNT_LAUNCH();
-    }
+    if (PASS == kMark) launch_pass<kMark, false, false>(acc, geo, f, S, st);  // reads no field
+    else if (bf16) launch_pass<PASS, true, true>(acc, geo, f, S, st);
+    else if (fb) launch_pass<PASS, false, true>(acc, geo, f, S, st);
+    else launch_pass<PASS, false, false>(acc, geo, f, S, st);
     return cudaGetLastError();
 }
 
@@ -591,6 +635,7 @@ void anchor_free(Anchor *A)
     cudaFree(A->flag); cudaFree(A->bits); cudaFree(A->id); cudaFree(A->vox); cudaFree(A->rowptr);
     cudaFree(A->col); cudaFree(A->w); cudaFree(A->b); cudaFree(A->c); cudaFree(A->pa); cudaFree(A->pb);
     cudaFree(A->red); cudaFree(A->rowlen); cudaFree(A->u); cudaFree(A->pos); cudaFree(A->tmp); cudaFree(A->cnt64); cudaFree(A->tmp64);
+    cudaFree(A->neg);
     *A = Anchor();
 }
 
@@ -624,18 +669,30 @@ cudaError_t anchor_build(Geometry &geo, const Field &f, int method, bool bf16, l
     }
     if (!marked) {
         AN_TRY(cudaMemsetAsync(A->flag, 0, (size_t)V, st));
-        AN_TRY(run_pass<kMark>(geo, f, method, bf16, S, st));
+        AN_TRY(run_pass<kMark>(geo, f, method, bf16, false, S, st));
     }
     if (ref_voxel >= 0 && ref_voxel < V) AN_TRY(cudaMemsetAsync(A->flag + ref_voxel, 1, 1, st));
+    // the FP32 field carries curl in .w: its sign bit can flag the anchors unless a curl
+    // value already has it set
+    const bool check_sign = !bf16 && f.curl != nullptr;
+    AN_TRY(grow(A->neg, cap[18], sizeof(uint32_t)));
+    AN_TRY(cudaMemsetAsync(A->neg, 0, sizeof(uint32_t), st));
+    if (check_sign) {
+        k_sign_any<<<grid_for(V), 256, 0, st>>>(V, f.curl, A->neg);
+        OM_COUNT_LAUNCH();
+        AN_TRY(cudaGetLastError());
+    }
 
     k_flag_to_u32<<<grid_for(V), 256, 0, st>>>(V, A->flag, A->u);
     OM_COUNT_LAUNCH();
     AN_TRY(cudaGetLastError());
     AN_TRY(exclusive_scan_u32(A->u, A->pos, V, A->tmp, st));
-    uint32_t n = 0;
+    uint32_t n = 0, neg = 0;
     AN_TRY(cudaMemcpyAsync(&n, A->pos + V, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    AN_TRY(cudaMemcpyAsync(&neg, A->neg, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     AN_TRY(cudaStreamSynchronize(st));
     A->n = n;
+    const bool fb = bf16 || neg == 0u;
     AN_TRY(grow(A->vox, cap[7], sizeof(uint32_t) * (size_t)n));
     k_assign_ids<<<grid_for(V), 256, 0, st>>>(V, A->flag, A->pos, A->id, A->vox, A->bits);
     OM_COUNT_LAUNCH();
@@ -679,7 +736,17 @@ cudaError_t anchor_build(Geometry &geo, const Field &f, int method, bool bf16, l
     S.w = A->w;
     S.b = A->b;
     S.c = A->c;
-    AN_TRY(run_pass<kFill>(geo, f, method, bf16, S, st));
+    if (fb && n) {
+        k_field_flags<<<grid_for(n), 256, 0, st>>>(n, A->vox, f.f32, bf16 ? f.bf16 : nullptr, 1);
+        OM_COUNT_LAUNCH();
+        AN_TRY(cudaGetLastError());
+    }
+    AN_TRY(run_pass<kFill>(geo, f, method, bf16, fb, S, st));
+    if (fb && n) {  // the sweeps read the field unflagged
+        k_field_flags<<<grid_for(n), 256, 0, st>>>(n, A->vox, f.f32, bf16 ? f.bf16 : nullptr, 0);
+        OM_COUNT_LAUNCH();
+        AN_TRY(cudaGetLastError());
+    }
     A->unit_weights = method_accum(method) == kAccPlain || method_accum(method) == kAccPlainNoEntry;
     return cudaGetLastError();
 }
@@ -725,7 +792,7 @@ cudaError_t anchor_mark(const Geometry &geo, const Field &f, int method, bool bf
         if (e != cudaSuccess) return e;
         Sink S{};
         S.flag = flag;
-        e = run_pass<kMark>(geo, f, method, bf16, S, st);
+        e = run_pass<kMark>(geo, f, method, bf16, false, S, st);
         if (e != cudaSuccess) return e;
     }
     if (ref_voxel >= 0 && ref_voxel < geo.grid.V) e = cudaMemsetAsync(flag + ref_voxel, 1, 1, st);
@@ -757,7 +824,17 @@ cudaError_t anchor_refresh_rhs(const Geometry &geo, const Field &f, bool bf16, A
     S.bits = A->bits;
     S.id = A->id;
     S.b = A->b;
-    return run_pass<kRhs>(geo, f, OMNI3D_METHOD_PLAIN, bf16, S, st);
+    // the plain method's field carries no curl (.w = +0), so the anchors can be flagged in it
+    const bool fb = bf16 || f.curl == nullptr;
+    if (fb) {
+        k_field_flags<<<grid_for(A->n), 256, 0, st>>>(A->n, A->vox, f.f32, bf16 ? f.bf16 : nullptr, 1);
+        OM_COUNT_LAUNCH();
+    }
+    e = run_pass<kRhs>(geo, f, OMNI3D_METHOD_PLAIN, bf16, fb, S, st);
+    if (e != cudaSuccess || !fb) return e;
+    k_field_flags<<<grid_for(A->n), 256, 0, st>>>(A->n, A->vox, f.f32, bf16 ? f.bf16 : nullptr, 0);
+    OM_COUNT_LAUNCH();
+    return cudaGetLastError();
 }
 
 cudaError_t anchor_scatter(const Anchor &A, const float *pa, float *vol, cudaStream_t st)

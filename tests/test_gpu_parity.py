@@ -129,6 +129,35 @@ def test_select_solve_matches_oracle(omni, orc, solver):
     assert synthetic.relative_l2(r.p, ep, gauge="none") < TOL_P_SELECT
 
 
+@pytest.mark.parametrize("method,mode", [("select", 1), ("weighted", 2)])
+def test_anchor_fill_with_signed_zero_curl(omni, orc, method, mode):
+    """The filling pass flags the anchors in the sign bit of the packed curl; a curl array
+    with a sign bit already set (here -0.0) makes it keep the bitmap instead.  Both forms
+    give the oracle's result, and the same field with +0.0 gives the same iterate."""
+    dims = (19, 16, 14)
+    f = _field(dims, seed=8, noise=0.1, sphere=3.5)
+    dirs = omni.icosphere(3)
+    p0 = _pinit(dims, seed=4)
+    curl = orc.curl(dims, f["spacing"], f["ax"], f["ay"], f["az"], f["mask"])
+    zero = np.nonzero(curl == 0)[0]
+    assert len(zero) > 10
+    signed = curl.copy()
+    signed[zero[::3]] = -0.0
+    assert (np.signbit(signed) & (signed == 0)).sum() > 0
+    thr = float(np.percentile(curl[curl > 0], 85)) if mode == 1 else 0.0
+    niter = 4
+    out = {}
+    for name, c in (("plus", curl), ("minus", signed)):
+        with omni.Omni3D(dims, f["spacing"], dirs, max_iter=niter, method=method, threshold=thr) as s:
+            out[name] = s.solve(f["ax"], f["ay"], f["az"], curl=c, p_init=p0)
+    ep, ecnt = orc.solve(dims, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p0, niter, mode=mode, thr=thr,
+                         curl=signed, precision="f64")
+    for r in out.values():
+        np.testing.assert_array_equal(r.count.reshape(-1) > 0, ecnt > 0)
+        assert synthetic.relative_l2(r.p, ep, gauge="none") < TOL_P_SELECT
+    assert synthetic.relative_l2(out["minus"].p, out["plus"].p, gauge="none") < 1e-6
+
+
 def test_weighted_sweep_matches_oracle(omni, orc):
     """One weighted sweep (K:1993-2135): the entry receives nothing, a step's weight is
     n / sum(curl/1e4) once that sum is nonzero; voxels inside the masked sphere have curl 0."""
