@@ -31,6 +31,11 @@
 namespace omni3d {
 
 constexpr int kWalkBatch = 4;  // steps whose gathers a walk issues together (walk.cuh)
+// Resident CTAs of 256 threads per SM for the operator passes: the filling pass waits on its
+// gathers (latency bound), and 5 CTAs (48 registers, a few bytes spilled to L1) beat 4 CTAs
+// (64 registers, no spill): 52.1 against 55.6 ms at 256^3 / 642 directions; 6 CTAs spill
+// more and took 60.8 ms.
+constexpr int kFillBlocks = 5;
 
 namespace {
 
@@ -130,7 +135,7 @@ __device__ __forceinline__ void emit(const Sink &S, long long v, long long start
 }
 
 struct Walk {
-    long long v;
+    uint32_t v;
     int d0, d1, d2;
     float h0, h1, h2;
     int m;
@@ -158,7 +163,7 @@ struct Walk {
 // Plain method: anchors are the entries; every voxel of a line takes (p[entry] + I, 1).
 // SELF = false leaves the entry's own term out (the minimum-curl plain variant).
 template <int PASS, bool BF16, bool SELF, bool FB>
-__global__ void __launch_bounds__(256, 4) k_anchor_plain(Grid g, const LineRec *__restrict__ lines,
+__global__ void __launch_bounds__(256, kFillBlocks) k_anchor_plain(Grid g, const LineRec *__restrict__ lines,
                                                       const uint32_t *__restrict__ gbase,
                                                       const uint32_t *__restrict__ desc, long long n_lines,
                                                       const float4 *__restrict__ f32,
@@ -179,7 +184,7 @@ __global__ void __launch_bounds__(256, 4) k_anchor_plain(Grid g, const LineRec *
     float I = 0.0f, comp = 0.0f;
     // the field (and without FB the anchor bitmap word) of every voxel gathered in batches
     walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, !FB>(
-        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, long long v, const float4 &gv, uint32_t word) {
+        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, uint32_t v, const float4 &gv, uint32_t word) {
             kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
             gl = gv;
             emit_w<PASS>(S, v, e, 1.0f, I, anchor_of<FB>(gv, word, v));
@@ -189,7 +194,7 @@ __global__ void __launch_bounds__(256, 4) k_anchor_plain(Grid g, const LineRec *
 // Weighted method: the walk of k_sweep_weighted (K:1993-2135); anchors are the entries
 // (the marking pass is the plain method's), the entry itself receives nothing.
 template <int PASS, bool BF16, bool FB>
-__global__ void __launch_bounds__(256, 4) k_anchor_weighted(Grid g, const LineRec *__restrict__ lines,
+__global__ void __launch_bounds__(256, kFillBlocks) k_anchor_weighted(Grid g, const LineRec *__restrict__ lines,
                                                          const uint32_t *__restrict__ gbase,
                                                          const uint32_t *__restrict__ desc, long long n_lines,
                                                          const float4 *__restrict__ f32,
@@ -206,7 +211,7 @@ __global__ void __launch_bounds__(256, 4) k_anchor_weighted(Grid g, const LineRe
     float4 gl = load_grad<BF16>(f32, b16, e);
     float I = 0.0f, comp = 0.0f, csum = 0.0f, nseg = 0.0f;
     walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, !FB>(
-        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, long long v, const float4 &gv, uint32_t word) {
+        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, uint32_t v, const float4 &gv, uint32_t word) {
             float cn = BF16 ? __ldg(curl + v) : curl_of<FB>(gv);
             kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
             csum += __fdiv_rn(cn, 1.0e4f);  // the weights as in k_sweep_weighted
@@ -219,7 +224,7 @@ __global__ void __launch_bounds__(256, 4) k_anchor_weighted(Grid g, const LineRe
 // Weighted method with raw curl sums (the minimum-curl variant): the walk of
 // k_sweep_weighted_raw; anchors are the entries, the entry takes its own term.
 template <int PASS, bool BF16, bool FB>
-__global__ void __launch_bounds__(256, 4) k_anchor_weighted_raw(Grid g, const LineRec *__restrict__ lines,
+__global__ void __launch_bounds__(256, kFillBlocks) k_anchor_weighted_raw(Grid g, const LineRec *__restrict__ lines,
                                                              const uint32_t *__restrict__ gbase,
                                                              const uint32_t *__restrict__ desc, long long n_lines,
                                                              const float4 *__restrict__ f32,
@@ -238,7 +243,7 @@ __global__ void __launch_bounds__(256, 4) k_anchor_weighted_raw(Grid g, const Li
     emit_w<PASS>(S, e, e, __frcp_rn(csum), 0.0f, FB ? anchor_of<FB>(gl, 0u, e) : is_anchor(S.bits, e));
     float I = 0.0f, comp = 0.0f;
     walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, !FB>(
-        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, long long v, const float4 &gv, uint32_t word) {
+        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, uint32_t v, const float4 &gv, uint32_t word) {
             float cn = BF16 ? __ldg(curl + v) : curl_of<FB>(gv);
             kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
             csum += cn;
@@ -251,7 +256,7 @@ __global__ void __launch_bounds__(256, 4) k_anchor_weighted_raw(Grid g, const Li
 // Selected method: the state machine of k_sweep_select (K:2280-2537); anchors are the
 // segment starts.
 template <int PASS, bool BF16, bool FB>
-__global__ void __launch_bounds__(256, 4) k_anchor_select(Grid g, const LineRec *__restrict__ lines,
+__global__ void __launch_bounds__(256, kFillBlocks) k_anchor_select(Grid g, const LineRec *__restrict__ lines,
                                                        const uint32_t *__restrict__ gbase,
                                                        const uint32_t *__restrict__ desc, long long n_lines,
                                                        const float4 *__restrict__ f32,
@@ -271,14 +276,14 @@ __global__ void __launch_bounds__(256, 4) k_anchor_select(Grid g, const LineRec 
     float ce = kW ? curl_of<FB>(gl) : __ldg(curl + L.v);
     bool started = !(ce == 0.0f || ce > thr);
     bool paused = false;
-    long long start = L.v;
+    uint32_t start = L.v;
     if (PASS == kMark && started) S.flag[start] = 1;
     float I = 0.0f, comp = 0.0f, csum = 0.0f, nseg = 0.0f;
     // the filling pass gathers the field (and without FB the anchor bitmap word) of every
     // voxel in batches
     constexpr int kGrad = PASS == kFill ? (BF16 ? kGradBF16 : kGradF32) : kNoGrad;
     walk_steps<kWalkBatch, kGrad, PASS == kFill && !FB>(
-        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, long long v, const float4 &gv, uint32_t word) {
+        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, uint32_t v, const float4 &gv, uint32_t word) {
             const float cn = kW ? curl_of<FB>(gv) : __ldg(curl + v);
             if (!started) {
                 bool ok = (a == 0) ? (cn != 0.0f && cn < thr) : (cn != 0.0f);

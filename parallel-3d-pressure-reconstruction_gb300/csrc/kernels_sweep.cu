@@ -45,7 +45,7 @@ __device__ __forceinline__ float sel3(int a, float x, float y, float z)
 
 // Per-line constants of the accumulation walk.
 struct LineWalk {
-    long long v;          // current voxel
+    uint32_t v;           // current voxel
     int d0, d1, d2;       // signed strides of a step along x, y, z
     float h0, h1, h2;     // -rho * sign * spacing / 2 per axis (K:1816, 1825, 1834)
     int m;
@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep_plain(Grid g, const LineRec *_
     float4 gl = load_grad<BF16>(f32, b16, L.v);
     float I = 0.0f, comp = 0.0f;
     walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, false>(
-        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, nullptr, [&](int a, long long v, const float4 &gv, uint32_t) {
+        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, nullptr, [&](int a, uint32_t v, const float4 &gv, uint32_t) {
             float term = sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z));
             kahan_add(I, comp, term);
             acc_add(pncnt + v, pe + I, 1.0f);
@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep_weighted(Grid g, const LineRec
     float4 gl = load_grad<BF16>(f32, b16, L.v);
     float I = 0.0f, comp = 0.0f, csum = 0.0f, nseg = 0.0f;
     walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, false>(
-        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, nullptr, [&](int a, long long v, const float4 &gv, uint32_t) {
+        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, nullptr, [&](int a, uint32_t v, const float4 &gv, uint32_t) {
             float cn = BF16 ? __ldg(curl + v) : gv.w;
             float term = sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z));
             kahan_add(I, comp, term);
@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep_weighted_raw(Grid g, const Lin
     }
     float I = 0.0f, comp = 0.0f;
     walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, false>(
-        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, nullptr, [&](int a, long long v, const float4 &gv, uint32_t) {
+        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, nullptr, [&](int a, uint32_t v, const float4 &gv, uint32_t) {
             float cn = BF16 ? __ldg(curl + v) : gv.w;
             kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
             csum += cn;
@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep_select(Grid g, const LineRec *
     float p0 = started ? __ldg(p + L.v) : 0.0f;
     float I = 0.0f, comp = 0.0f, csum = 0.0f, nseg = 0.0f;
     walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, false>(
-        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, nullptr, [&](int a, long long v, const float4 &gv, uint32_t) {
+        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, nullptr, [&](int a, uint32_t v, const float4 &gv, uint32_t) {
             const float cn = BF16 ? __ldg(curl + v) : gv.w;
             if (!started) {
                 bool ok = (a == 0) ? (cn != 0.0f && cn < thr) : (cn != 0.0f);

@@ -28,10 +28,11 @@ __device__ __forceinline__ float4 load_grad_b16(const uint2 *b16, long long v)
 // Which gradient a walk gathers per step.
 enum WalkGrad { kNoGrad = 0, kGradF32 = 1, kGradBF16 = 2 };
 
-// v: the line's current voxel (advanced to its last voxel); d0..d2: signed strides of a step
+// v: the line's current voxel (advanced to its last voxel; voxel indices are below 2^32,
+// and a negative stride wraps modulo 2^32 to the right index); d0..d2: signed strides of a step
 // along x, y, z; m: steps; dp: the lane's first step word (words 32 apart).
 template <int B, int GRAD, bool AUX, typename F>
-__device__ __forceinline__ void walk_steps(long long &v, int d0, int d1, int d2, int m, const uint32_t *dp,
+__device__ __forceinline__ void walk_steps(uint32_t &v, int d0, int d1, int d2, int m, const uint32_t *dp,
                                            const float4 *f32, const uint2 *b16, const uint32_t *aux, F &&f)
 {
     for (int s0 = 0; s0 < m; s0 += 16) {
@@ -39,7 +40,7 @@ __device__ __forceinline__ void walk_steps(long long &v, int d0, int d1, int d2,
         const int n = min(16, m - s0);
         for (int t0 = 0; t0 < n; t0 += B) {
             int ax[B];
-            uint32_t vv[B];  // voxel indices are below 2^32
+            uint32_t vv[B];
             float4 g[B];
             uint32_t xw[B];
 #pragma unroll
@@ -47,8 +48,8 @@ __device__ __forceinline__ void walk_steps(long long &v, int d0, int d1, int d2,
                 ax[q] = (int)(w & 3u);
                 w >>= 2;
                 if (t0 + q < n) {
-                    v += ax[q] == 0 ? d0 : (ax[q] == 1 ? d1 : d2);
-                    vv[q] = (uint32_t)v;
+                    v += (uint32_t)(ax[q] == 0 ? d0 : (ax[q] == 1 ? d1 : d2));
+                    vv[q] = v;
                     if (GRAD == kGradF32) g[q] = load_grad_f32(f32, v);
                     else if (GRAD == kGradBF16) g[q] = load_grad_b16(b16, v);
                     else g[q] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -57,7 +58,7 @@ __device__ __forceinline__ void walk_steps(long long &v, int d0, int d1, int d2,
             }
 #pragma unroll
             for (int q = 0; q < B; q++)
-                if (t0 + q < n) f(ax[q], (long long)vv[q], g[q], AUX ? xw[q] : 0u);
+                if (t0 + q < n) f(ax[q], vv[q], g[q], AUX ? xw[q] : 0u);
         }
     }
 }
