@@ -306,6 +306,27 @@ def test_bf16_gradient_storage(omni):
     assert 0 < err < 1e-2
 
 
+@pytest.mark.parametrize("method", ["plain", "weighted", "select"])
+def test_bf16_anchor_solver_matches_sweep_solver(omni, orc, method):
+    """With BF16 storage the filling pass finds the anchors from bit 31 of each gathered
+    entry; the anchor solver must then give the sweep solver's iterate (same BF16 field,
+    same arithmetic up to the order of sums)."""
+    dims = (22, 19, 17)
+    f = _field(dims, seed=12, noise=0.1, sphere=4.0)
+    dirs = omni.icosphere(3)
+    p0 = _pinit(dims, seed=5)
+    curl = orc.curl(dims, f["spacing"], f["ax"], f["ay"], f["az"], f["mask"])
+    thr = float(np.percentile(curl[curl > 0], 85)) if method == "select" else 0.0
+    out = {}
+    for solver in ("sweep", "anchor"):
+        with omni.Omni3D(dims, f["spacing"], dirs, max_iter=5, grad="bf16", method=method, threshold=thr,
+                         solver=solver) as s:
+            out[solver] = s.solve(f["ax"], f["ay"], f["az"], curl=None if method == "plain" else curl, p_init=p0)
+    np.testing.assert_array_equal(out["anchor"].count > 0, out["sweep"].count > 0)
+    assert synthetic.relative_l2(out["anchor"].count, out["sweep"].count, gauge="none") < 1e-6
+    assert synthetic.relative_l2(out["anchor"].p, out["sweep"].p, gauge="none") < 1e-5
+
+
 def test_device_pointers_match_host(omni):
     torch = pytest.importorskip("torch")
     dims = (16, 14, 12)
