@@ -153,16 +153,18 @@ __global__ void k_u32_to_u64(long long n, const uint32_t *in, unsigned long long
 }
 
 // acc += lambda / c (c > 0)
-__global__ void k_adj_accum(long long n, const float *lam, const float *c, float *acc)
+__global__ void k_adj_accum(long long n, const float *lam, const float2 *bc, float *acc)
 {
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        if (c[i] > 0.0f) acc[i] += __fdiv_rn(lam[i], c[i]);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float c = bc[i].y;
+        if (c > 0.0f) acc[i] += __fdiv_rn(lam[i], c);
+    }
 }
 
 // next = M^T D^-1 lambda (+ lambda where c = 0), a warp per column of M
 __global__ void __launch_bounds__(256) k_adj_spmvT(long long n, const unsigned long long *__restrict__ tptr,
                                                    const uint32_t *__restrict__ trow, const float *__restrict__ lam,
-                                                   const float *__restrict__ c, float *__restrict__ next)
+                                                   const float2 *__restrict__ bc, float *__restrict__ next)
 {
     long long a = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
@@ -171,11 +173,11 @@ __global__ void __launch_bounds__(256) k_adj_spmvT(long long n, const unsigned l
     float s = 0.0f;
     for (unsigned long long j = j0 + lane; j < j1; j += 32) {
         uint32_t r = __ldg(trow + j);
-        float cr = __ldg(c + r);
+        float cr = __ldg(&bc[r].y);
         if (cr > 0.0f) s += __fdiv_rn(__ldg(lam + r), cr);
     }
     for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) next[a] = s + (c[a] > 0.0f ? 0.0f : lam[a]);
+    if (lane == 0) next[a] = s + (bc[a].y > 0.0f ? 0.0f : lam[a]);
 }
 
 // dB[vox[a]] += acc[a]
@@ -320,10 +322,10 @@ cudaError_t adjoint_plain(const Geometry &geo, const Anchor &A, AdjointBuffers *
     // anchor iterations, backwards
     long long threads = n * 32;
     for (int k = K - 1; k >= 1; k--) {
-        k_adj_accum<<<grid_for(n), 256, 0, st>>>(n, B->lam, A.c, B->acc);
+        k_adj_accum<<<grid_for(n), 256, 0, st>>>(n, B->lam, A.bc, B->acc);
         OM_COUNT_LAUNCH();
         if (k > 1) {
-            k_adj_spmvT<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(n, B->tptr, B->trow, B->lam, A.c, B->nxt);
+            k_adj_spmvT<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(n, B->tptr, B->trow, B->lam, A.bc, B->nxt);
             OM_COUNT_LAUNCH();
             std::swap(B->lam, B->nxt);
         }

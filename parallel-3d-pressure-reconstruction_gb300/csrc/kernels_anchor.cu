@@ -90,48 +90,42 @@ struct Sink {
     uint8_t *flag;
     const unsigned long long *rowptr;
     uint32_t *cursor;
-    uint32_t *col;
-    float *w;
-    float *b;
-    float *c;
+    uint32_t *col;   // unit-weight operators: the start anchor of each link
+    uint2 *cw;       // weighted operators: (start anchor, weight bits) of each link
+    float2 *bc;      // per row: (b, c)
 };
 
-// Record one contribution of weight wt and integral I into voxel v from the segment that
-// started at voxel `start`.  emit_w is told whether v is an anchor (anchor_of); emit
-// looks it up in the bitmap.
-template <int PASS>
-__device__ __forceinline__ void emit_w(const Sink &S, long long v, long long start, float wt, float I, bool anchor)
+// Record one contribution of weight wt and integral I into voxel v from the segment whose
+// start anchor is scol (its id, loaded once per segment).  A link costs one row lookup, one
+// slot atomic, one store and one vector reduction of (b, c); UNIT operators (every weight
+// 1) store no weight.
+template <int PASS, bool UNIT>
+__device__ __forceinline__ void emit_w(const Sink &S, uint32_t v, uint32_t scol, float wt, float I, bool anchor)
 {
     if (PASS == kMark) return;
     if (!anchor) return;
     int row = __ldg(S.id + v);
     if (row < 0) return;  // not an anchor after all: nothing to index
+    if (PASS == kFill && (int)scol < 0) return;  // a start that is no anchor: no column to link
     if (PASS == kRhs) {  // plain method, operator cached: only b = sum I is field-dependent
-        atomicAdd(S.b + row, I);
+        atomicAdd(&S.bc[row].x, I);
         return;
     }
     unsigned long long slot = S.rowptr[row] + atomicAdd(S.cursor + row, 1u);
-    S.col[slot] = (uint32_t)__ldg(S.id + start);
-    S.w[slot] = wt;
-    atomicAdd(S.b + row, wt * I);
-    atomicAdd(S.c + row, wt);
+    if (UNIT) {
+        S.col[slot] = scol;
+        atomicAdd(S.bc + row, make_float2(I, 1.0f));
+    } else {
+        S.cw[slot] = make_uint2(scol, __float_as_uint(wt));
+        atomicAdd(S.bc + row, make_float2(wt * I, wt));
+    }
 }
 
+// The anchor id of a segment's start voxel, for the filling pass's links.
 template <int PASS>
-__device__ __forceinline__ void emit(const Sink &S, long long v, long long start, float wt, float I)
+__device__ __forceinline__ uint32_t start_col(const Sink &S, uint32_t start)
 {
-    if (PASS == kMark) return;
-    if (!is_anchor(S.bits, v)) return;
-    int row = __ldg(S.id + v);
-    if (PASS == kRhs) {  // plain method, operator cached: only b = sum I is field-dependent
-        atomicAdd(S.b + row, I);
-        return;
-    }
-    unsigned long long slot = S.rowptr[row] + atomicAdd(S.cursor + row, 1u);
-    S.col[slot] = (uint32_t)__ldg(S.id + start);
-    S.w[slot] = wt;
-    atomicAdd(S.b + row, wt * I);
-    atomicAdd(S.c + row, wt);
+    return PASS == kFill ? (uint32_t)__ldg(S.id + start) : 0u;
 }
 
 struct Walk {
@@ -178,8 +172,9 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_plain(Grid g, const
     }
     Walk L;
     L.init(g, r, gbase, desc, li);
-    const long long e = r.e;
-    if (SELF) emit<PASS>(S, e, e, 1.0f, 0.0f);
+    const uint32_t e = r.e;
+    const uint32_t ecol = start_col<PASS>(S, e);
+    if (SELF) emit_w<PASS, true>(S, e, ecol, 1.0f, 0.0f, is_anchor(S.bits, e));
     float4 gl = load_grad<BF16>(f32, b16, e);
     float I = 0.0f, comp = 0.0f;
     // the field (and without FB the anchor bitmap word) of every voxel gathered in batches
@@ -187,7 +182,7 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_plain(Grid g, const
         L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, uint32_t v, const float4 &gv, uint32_t word) {
             kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
             gl = gv;
-            emit_w<PASS>(S, v, e, 1.0f, I, anchor_of<FB>(gv, word, v));
+            emit_w<PASS, true>(S, v, ecol, 1.0f, I, anchor_of<FB>(gv, word, v));
         });
 }
 
@@ -207,7 +202,8 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_weighted(Grid g, co
     LineRec r = lines[li];
     Walk L;
     L.init(g, r, gbase, desc, li);
-    const long long e = r.e;
+    const uint32_t e = r.e;
+    const uint32_t ecol = start_col<PASS>(S, e);
     float4 gl = load_grad<BF16>(f32, b16, e);
     float I = 0.0f, comp = 0.0f, csum = 0.0f, nseg = 0.0f;
     walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, !FB>(
@@ -216,7 +212,7 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_weighted(Grid g, co
             kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
             csum += __fdiv_rn(cn, 1.0e4f);  // the weights as in k_sweep_weighted
             nseg += 1.0f;
-            if (csum != 0.0f) emit_w<PASS>(S, v, e, __frcp_rn(csum) * nseg, I, anchor_of<FB>(gv, word, v));
+            if (csum != 0.0f) emit_w<PASS, false>(S, v, ecol, __frcp_rn(csum) * nseg, I, anchor_of<FB>(gv, word, v));
             gl = gv;
         });
 }
@@ -237,10 +233,11 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_weighted_raw(Grid g
     LineRec r = lines[li];
     Walk L;
     L.init(g, r, gbase, desc, li);
-    const long long e = r.e;
+    const uint32_t e = r.e;
+    const uint32_t ecol = start_col<PASS>(S, e);
     float4 gl = load_grad<BF16>(f32, b16, e);
     float csum = BF16 ? __ldg(curl + e) : curl_of<FB>(gl), nseg = 1.0f;
-    emit_w<PASS>(S, e, e, __frcp_rn(csum), 0.0f, FB ? anchor_of<FB>(gl, 0u, e) : is_anchor(S.bits, e));
+    emit_w<PASS, false>(S, e, ecol, __frcp_rn(csum), 0.0f, FB ? anchor_of<FB>(gl, 0u, e) : is_anchor(S.bits, e));
     float I = 0.0f, comp = 0.0f;
     walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, !FB>(
         L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, uint32_t v, const float4 &gv, uint32_t word) {
@@ -248,7 +245,7 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_weighted_raw(Grid g
             kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
             csum += cn;
             nseg += 1.0f;
-            emit_w<PASS>(S, v, e, __frcp_rn(csum) * nseg, I, anchor_of<FB>(gv, word, v));
+            emit_w<PASS, false>(S, v, ecol, __frcp_rn(csum) * nseg, I, anchor_of<FB>(gv, word, v));
             gl = gv;
         });
 }
@@ -278,6 +275,7 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_select(Grid g, cons
     bool paused = false;
     uint32_t start = L.v;
     if (PASS == kMark && started) S.flag[start] = 1;
+    uint32_t scol = started ? start_col<PASS>(S, start) : 0u;
     float I = 0.0f, comp = 0.0f, csum = 0.0f, nseg = 0.0f;
     // the filling pass gathers the field (and without FB the anchor bitmap word) of every
     // voxel in batches
@@ -290,6 +288,7 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_select(Grid g, cons
                 if (ok) {
                     start = v;
                     if (PASS == kMark) S.flag[start] = 1;
+                    scol = start_col<PASS>(S, start);
                     started = true;
                     I = 0.0f; comp = 0.0f; nseg = 0.0f; csum = 0.0f;
                 }
@@ -300,14 +299,15 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_select(Grid g, cons
                         kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
                     csum += cn * 1.0e-4f;  // the weights as in k_sweep_select
                     nseg += 1.0f;
-                    if (PASS == kFill) emit_w<PASS>(S, v, start, __frcp_rn(csum) * nseg, I, anchor_of<FB>(gv, word, v));
-                    else emit<PASS>(S, v, start, __frcp_rn(csum) * nseg, I);
+                    if (PASS == kFill)
+                        emit_w<PASS, false>(S, v, scol, __frcp_rn(csum) * nseg, I, anchor_of<FB>(gv, word, v));
                 }
                 bool enter_bad = (a == 0) ? ((!paused && cn >= thr) || cn == 0.0f) : (!paused && cn >= thr);
                 if (enter_bad) paused = true;
                 if (paused && good) {
                     start = v;
                     if (PASS == kMark) S.flag[start] = 1;
+                    scol = start_col<PASS>(S, start);
                     I = 0.0f; comp = 0.0f;
                     paused = false;
                     if (a != 2) { nseg = 0.0f; csum = 0.0f; }
@@ -387,11 +387,12 @@ __device__ __forceinline__ double warp_sum_compensated(float s, float comp)
     return d;
 }
 
-__device__ __forceinline__ float anchor_update(double sum, long long row, const float *b, const float *c,
+__device__ __forceinline__ float anchor_update(double sum, long long row, const float2 *bc,
                                                const uint32_t *vox, const float *p_init, int seed, const float *pc)
 {
-    const float cc = c[row];
-    double numer = (double)b[row] + sum;
+    const float2 q = bc[row];
+    const float cc = q.y;
+    double numer = (double)q.x + sum;
     if (seed && p_init) numer += (double)p_init[vox[row]];
     return cc > 0.0f ? (float)(numer / (double)cc) : pc[row];
 }
@@ -399,8 +400,7 @@ __device__ __forceinline__ float anchor_update(double sum, long long row, const 
 // One anchor iteration, a warp per row.
 __global__ void __launch_bounds__(256) k_anchor_spmv(long long n, const unsigned long long *__restrict__ rowptr,
                                                      const uint32_t *__restrict__ rowlen,
-                                                     const uint32_t *__restrict__ col, const float *__restrict__ w,
-                                                     const float *__restrict__ b, const float *__restrict__ c,
+                                                     const uint2 *__restrict__ cw, const float2 *__restrict__ bc,
                                                      const uint32_t *__restrict__ vox, const float *__restrict__ p_init,
                                                      int seed, const float *__restrict__ pc, float *__restrict__ pn)
 {
@@ -409,16 +409,19 @@ __global__ void __launch_bounds__(256) k_anchor_spmv(long long n, const unsigned
     if (row >= n) return;  // whole warps
     unsigned long long j0 = rowptr[row], j1 = j0 + rowlen[row];
     float s = 0.0f, comp = 0.0f;
-    for (unsigned long long j = j0 + lane; j < j1; j += 32) kahan_add(s, comp, __ldg(w + j) * __ldg(pc + __ldg(col + j)));
+    for (unsigned long long j = j0 + lane; j < j1; j += 32) {
+        const uint2 q = __ldg(cw + j);
+        kahan_add(s, comp, __uint_as_float(q.y) * __ldg(pc + q.x));
+    }
     const double sum = warp_sum_compensated(s, comp);
-    if (lane == 0) pn[row] = anchor_update(sum, row, b, c, vox, p_init, seed, pc);
+    if (lane == 0) pn[row] = anchor_update(sum, row, bc, vox, p_init, seed, pc);
 }
 
 // Plain method: every weight is 1, so a row is a plain sum of gathered anchor values.
 __global__ void __launch_bounds__(256) k_anchor_spmv_unit(long long n, const unsigned long long *__restrict__ rowptr,
                                                           const uint32_t *__restrict__ rowlen,
-                                                          const uint32_t *__restrict__ col, const float *__restrict__ b,
-                                                          const float *__restrict__ c, const uint32_t *__restrict__ vox,
+                                                          const uint32_t *__restrict__ col, const float2 *__restrict__ bc,
+                                                          const uint32_t *__restrict__ vox,
                                                           const float *__restrict__ p_init, int seed,
                                                           const float *__restrict__ pc, float *__restrict__ pn)
 {
@@ -429,7 +432,7 @@ __global__ void __launch_bounds__(256) k_anchor_spmv_unit(long long n, const uns
     float s = 0.0f, comp = 0.0f;
     for (unsigned long long j = j0 + lane; j < j1; j += 32) kahan_add(s, comp, __ldg(pc + __ldg(col + j)));
     const double sum = warp_sum_compensated(s, comp);
-    if (lane == 0) pn[row] = anchor_update(sum, row, b, c, vox, p_init, seed, pc);
+    if (lane == 0) pn[row] = anchor_update(sum, row, bc, vox, p_init, seed, pc);
 }
 
 constexpr int kRedBlocks = 256, kRedThreads = 256;
@@ -521,6 +524,13 @@ unsigned grid_for(long long n, int threads = 256)
     return (unsigned)b;
 }
 
+// b = 0 on every row, c kept (the cached plain operator's refresh).
+__global__ void k_clear_b(long long n, float2 *bc)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        bc[i].x = 0.0f;
+}
+
 // Set (set = 1) or clear the anchor flag in the field entries of the n anchors: bit 31 of
 // the BF16 entry's second word when b16 is given, else the sign bit of the FP32 entry's .w.
 __global__ void k_field_flags(long long n, const uint32_t *__restrict__ vox, float4 *f32, uint2 *b16, int set)
@@ -593,8 +603,9 @@ cudaError_t run_pass(const Geometry &geo, const Field &f, int method, bool bf16,
     const bool need_field = PASS == kFill || PASS == kRhs;
     bool ok = geo.d_lines && geo.d_gbase && geo.d_desc;
     if (PASS == kMark) ok = ok && S.flag;
-    else ok = ok && S.bits && S.id && S.b;
-    if (PASS == kFill) ok = ok && S.rowptr && S.cursor && S.col && S.w && S.c;
+    else ok = ok && S.bits && S.id && S.bc;
+    const bool unit_links = method_accum(method) == kAccPlain || method_accum(method) == kAccPlainNoEntry;
+    if (PASS == kFill) ok = ok && S.rowptr && S.cursor && (unit_links ? S.col != nullptr : S.cw != nullptr);
     if (need_field) ok = ok && (bf16 ? f.bf16 != nullptr : f.f32 != nullptr);
     const int acc = method_accum(method);
     const bool weighted = acc == kAccWeighted || acc == kAccWeightedRawCurl;
@@ -638,7 +649,7 @@ cudaError_t grow(T *&p, size_t &cap, size_t bytes)
 void anchor_free(Anchor *A)
 {
     cudaFree(A->flag); cudaFree(A->bits); cudaFree(A->id); cudaFree(A->vox); cudaFree(A->rowptr);
-    cudaFree(A->col); cudaFree(A->w); cudaFree(A->b); cudaFree(A->c); cudaFree(A->pa); cudaFree(A->pb);
+    cudaFree(A->col); cudaFree(A->cw); cudaFree(A->bc); cudaFree(A->pa); cudaFree(A->pb);
     cudaFree(A->red); cudaFree(A->rowlen); cudaFree(A->u); cudaFree(A->pos); cudaFree(A->tmp); cudaFree(A->cnt64); cudaFree(A->tmp64);
     cudaFree(A->neg);
     *A = Anchor();
@@ -722,25 +733,23 @@ cudaError_t anchor_build(Geometry &geo, const Field &f, int method, bool bf16, l
         return cudaErrorNotSupported;
     }
 
-    AN_TRY(grow(A->col, cap[11], sizeof(uint32_t) * (size_t)nnz));
-    AN_TRY(grow(A->w, cap[12], sizeof(float) * (size_t)nnz));
-    AN_TRY(grow(A->b, cap[13], sizeof(float) * (size_t)n));
-    AN_TRY(grow(A->c, cap[14], sizeof(float) * (size_t)n));
+    const bool unit_links = method_accum(method) == kAccPlain || method_accum(method) == kAccPlainNoEntry;
+    if (unit_links) AN_TRY(grow(A->col, cap[11], sizeof(uint32_t) * (size_t)nnz));
+    else AN_TRY(grow(A->cw, cap[12], sizeof(uint2) * (size_t)nnz));
+    AN_TRY(grow(A->bc, cap[13], sizeof(float2) * (size_t)n));
     AN_TRY(grow(A->pa, cap[15], sizeof(float) * (size_t)n));
     AN_TRY(grow(A->pb, cap[16], sizeof(float) * (size_t)n));
     AN_TRY(grow(A->rowlen, cap[17], sizeof(uint32_t) * (size_t)n));
     uint32_t *cursor = A->rowlen;
     AN_TRY(cudaMemsetAsync(cursor, 0, sizeof(uint32_t) * (size_t)std::max<long long>(n, 1), st));
-    AN_TRY(cudaMemsetAsync(A->b, 0, sizeof(float) * (size_t)std::max<long long>(n, 1), st));
-    AN_TRY(cudaMemsetAsync(A->c, 0, sizeof(float) * (size_t)std::max<long long>(n, 1), st));
+    AN_TRY(cudaMemsetAsync(A->bc, 0, sizeof(float2) * (size_t)std::max<long long>(n, 1), st));
     S.bits = A->bits;
     S.id = A->id;
     S.rowptr = A->rowptr;
     S.cursor = cursor;
-    S.col = A->col;
-    S.w = A->w;
-    S.b = A->b;
-    S.c = A->c;
+    S.col = unit_links ? A->col : nullptr;
+    S.cw = unit_links ? nullptr : A->cw;
+    S.bc = A->bc;
     if (fb && n) {
         k_field_flags<<<grid_for(n), 256, 0, st>>>(n, A->vox, f.f32, bf16 ? f.bf16 : nullptr, 1);
         OM_COUNT_LAUNCH();
@@ -810,10 +819,10 @@ cudaError_t anchor_step(const Anchor &A, const float *p_init, bool seed, int gau
     if (A.n == 0) return cudaSuccess;
     long long threads = A.n * 32;
     if (A.unit_weights)
-        k_anchor_spmv_unit<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(A.n, A.rowptr, A.rowlen, A.col, A.b, A.c, A.vox,
+        k_anchor_spmv_unit<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(A.n, A.rowptr, A.rowlen, A.col, A.bc, A.vox,
                                                                                p_init, seed ? 1 : 0, p_cur, p_next);
     else
-        k_anchor_spmv<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(A.n, A.rowptr, A.rowlen, A.col, A.w, A.b, A.c,
+        k_anchor_spmv<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(A.n, A.rowptr, A.rowlen, A.cw, A.bc,
                                                                           A.vox, p_init, seed ? 1 : 0, p_cur, p_next);
     OM_COUNT_LAUNCH();
     if (red2) return change_sums(A.n, p_cur, p_next, gauge, ref_anchor, A.red, red2, st, nullptr);
@@ -823,12 +832,14 @@ cudaError_t anchor_step(const Anchor &A, const float *p_init, bool seed, int gau
 cudaError_t anchor_refresh_rhs(const Geometry &geo, const Field &f, bool bf16, Anchor *A, cudaStream_t st)
 {
     if (A->n == 0) return cudaSuccess;
-    cudaError_t e = cudaMemsetAsync(A->b, 0, sizeof(float) * (size_t)A->n, st);
+    k_clear_b<<<grid_for(A->n), 256, 0, st>>>(A->n, A->bc);
+    OM_COUNT_LAUNCH();
+    cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     Sink S{};
     S.bits = A->bits;
     S.id = A->id;
-    S.b = A->b;
+    S.bc = A->bc;
     // the plain method's field carries no curl (.w = +0), so the anchors can be flagged in it
     const bool fb = bf16 || f.curl == nullptr;
     if (fb) {

@@ -204,10 +204,9 @@ struct Anchor {
     uint32_t *vox = nullptr;        // n: voxel of anchor
     unsigned long long *rowptr = nullptr;  // n + 1: row capacities (lines through the voxel)
     uint32_t *rowlen = nullptr;     // n: entries in each row
-    uint32_t *col = nullptr;        // nnz
-    float *w = nullptr;             // nnz
-    float *b = nullptr;             // n: sum of w * I
-    float *c = nullptr;             // n: sum of w
+    uint32_t *col = nullptr;        // nnz, unit weights: the start anchor of each link
+    uint2 *cw = nullptr;            // nnz, other methods: (start anchor, weight bits) of each link
+    float2 *bc = nullptr;           // n: (b, c) = (sum of w * I, sum of w)
     float *pa = nullptr, *pb = nullptr;  // iterates
     double *red = nullptr;          // reduction scratch
     bool unit_weights = false;      // plain method: every w is 1 (the w array is unused)
