@@ -88,8 +88,7 @@ struct Sink {
     const uint32_t *bits;
     const int32_t *id;
     uint8_t *flag;
-    const unsigned long long *rowptr;
-    uint32_t *cursor;
+    unsigned long long *next;  // per row: the next free link slot (starts at the row's first slot)
     uint32_t *col;   // unit-weight operators: the start anchor of each link
     uint2 *cw;       // weighted operators: (start anchor, weight bits) of each link
     float2 *bc;      // per row: (b, c)
@@ -97,8 +96,8 @@ struct Sink {
 
 // Record one contribution of weight wt and integral I into voxel v from the segment whose
 // start anchor is scol (its id, loaded once per segment).  A link costs one row lookup, one
-// slot atomic, one store and one vector reduction of (b, c); UNIT operators (every weight
-// 1) store no weight.
+// 64-bit slot atomic, one store and one vector reduction of (b, c); UNIT operators (every
+// weight 1) store no weight.
 template <int PASS, bool UNIT>
 __device__ __forceinline__ void emit_w(const Sink &S, uint32_t v, uint32_t scol, float wt, float I, bool anchor)
 {
@@ -111,7 +110,7 @@ __device__ __forceinline__ void emit_w(const Sink &S, uint32_t v, uint32_t scol,
         atomicAdd(&S.bc[row].x, I);
         return;
     }
-    unsigned long long slot = S.rowptr[row] + atomicAdd(S.cursor + row, 1u);
+    const unsigned long long slot = atomicAdd(S.next + row, 1ull);
     if (UNIT) {
         S.col[slot] = scol;
         atomicAdd(S.bc + row, make_float2(I, 1.0f));
@@ -531,6 +530,22 @@ __global__ void k_clear_b(long long n, float2 *bc)
         bc[i].x = 0.0f;
 }
 
+// After the filling pass: each row's length from its next free slot, and (flags = 1) the
+// anchor flags cleared from the field entries.
+__global__ void k_fill_finish(long long n, const unsigned long long *__restrict__ rowptr,
+                              const unsigned long long *__restrict__ next, uint32_t *rowlen, int flags,
+                              const uint32_t *__restrict__ vox, float4 *f32, uint2 *b16)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        rowlen[i] = (uint32_t)(next[i] - rowptr[i]);
+        if (flags) {
+            const uint32_t v = vox[i];
+            uint32_t *u = b16 ? &b16[v].y : reinterpret_cast<uint32_t *>(&f32[v].w);
+            *u &= 0x7fffffffu;
+        }
+    }
+}
+
 // Set (set = 1) or clear the anchor flag in the field entries of the n anchors: bit 31 of
 // the BF16 entry's second word when b16 is given, else the sign bit of the FP32 entry's .w.
 __global__ void k_field_flags(long long n, const uint32_t *__restrict__ vox, float4 *f32, uint2 *b16, int set)
@@ -605,7 +620,7 @@ cudaError_t run_pass(const Geometry &geo, const Field &f, int method, bool bf16,
     if (PASS == kMark) ok = ok && S.flag;
     else ok = ok && S.bits && S.id && S.bc;
     const bool unit_links = method_accum(method) == kAccPlain || method_accum(method) == kAccPlainNoEntry;
-    if (PASS == kFill) ok = ok && S.rowptr && S.cursor && (unit_links ? S.col != nullptr : S.cw != nullptr);
+    if (PASS == kFill) ok = ok && S.next && (unit_links ? S.col != nullptr : S.cw != nullptr);
     if (need_field) ok = ok && (bf16 ? f.bf16 != nullptr : f.f32 != nullptr);
     const int acc = method_accum(method);
     const bool weighted = acc == kAccWeighted || acc == kAccWeightedRawCurl;
@@ -651,7 +666,7 @@ void anchor_free(Anchor *A)
     cudaFree(A->flag); cudaFree(A->bits); cudaFree(A->id); cudaFree(A->vox); cudaFree(A->rowptr);
     cudaFree(A->col); cudaFree(A->cw); cudaFree(A->bc); cudaFree(A->pa); cudaFree(A->pb);
     cudaFree(A->red); cudaFree(A->rowlen); cudaFree(A->u); cudaFree(A->pos); cudaFree(A->tmp); cudaFree(A->cnt64); cudaFree(A->tmp64);
-    cudaFree(A->neg);
+    cudaFree(A->neg); cudaFree(A->next);
     *A = Anchor();
 }
 
@@ -740,13 +755,12 @@ cudaError_t anchor_build(Geometry &geo, const Field &f, int method, bool bf16, l
     AN_TRY(grow(A->pa, cap[15], sizeof(float) * (size_t)n));
     AN_TRY(grow(A->pb, cap[16], sizeof(float) * (size_t)n));
     AN_TRY(grow(A->rowlen, cap[17], sizeof(uint32_t) * (size_t)n));
-    uint32_t *cursor = A->rowlen;
-    AN_TRY(cudaMemsetAsync(cursor, 0, sizeof(uint32_t) * (size_t)std::max<long long>(n, 1), st));
+    AN_TRY(grow(A->next, cap[19], sizeof(unsigned long long) * (size_t)std::max<long long>(n, 1)));
+    if (n) AN_TRY(cudaMemcpyAsync(A->next, A->rowptr, sizeof(unsigned long long) * (size_t)n, cudaMemcpyDeviceToDevice, st));
     AN_TRY(cudaMemsetAsync(A->bc, 0, sizeof(float2) * (size_t)std::max<long long>(n, 1), st));
     S.bits = A->bits;
     S.id = A->id;
-    S.rowptr = A->rowptr;
-    S.cursor = cursor;
+    S.next = A->next;
     S.col = unit_links ? A->col : nullptr;
     S.cw = unit_links ? nullptr : A->cw;
     S.bc = A->bc;
@@ -756,8 +770,9 @@ cudaError_t anchor_build(Geometry &geo, const Field &f, int method, bool bf16, l
         AN_TRY(cudaGetLastError());
     }
     AN_TRY(run_pass<kFill>(geo, f, method, bf16, fb, S, st));
-    if (fb && n) {  // the sweeps read the field unflagged
-        k_field_flags<<<grid_for(n), 256, 0, st>>>(n, A->vox, f.f32, bf16 ? f.bf16 : nullptr, 0);
+    if (n) {  // row lengths; the sweeps read the field unflagged
+        k_fill_finish<<<grid_for(n), 256, 0, st>>>(n, A->rowptr, A->next, A->rowlen, fb ? 1 : 0, A->vox, f.f32,
+                                                    bf16 ? f.bf16 : nullptr);
         OM_COUNT_LAUNCH();
         AN_TRY(cudaGetLastError());
     }

@@ -214,6 +214,7 @@ struct Anchor {
     uint32_t *u = nullptr, *pos = nullptr, *tmp = nullptr;
     unsigned long long *cnt64 = nullptr, *tmp64 = nullptr;
     uint32_t *neg = nullptr;        // 1 word: some curl value has its sign bit set
+    unsigned long long *next = nullptr;  // n: next free link slot of each row while filling
     // capacities in bytes, one per buffer above, so that rebuilding for a new field of the
     // same geometry allocates nothing
     size_t cap[20] = {};
