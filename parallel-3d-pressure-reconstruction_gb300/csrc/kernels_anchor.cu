@@ -319,8 +319,8 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_select(Grid g, cons
 // Selected method: a voxel can start a segment only if it is on the boundary (a line entry)
 // or if the voxel before it on some line is "bad" (curl == 0 or curl >= thr): a start
 // before the first good voxel follows a voxel that failed the start test, and a restart
-// follows a voxel that paused or kept the pause (K:2300-2506).  Flags that superset and
-// counts it into *count.
+// follows a voxel that paused or kept the pause (K:2300-2506); and every start voxel has
+// curl != 0.  Flags that superset and counts it into *count.
 __global__ void k_select_candidates(Grid g, const float *__restrict__ curl, uint8_t *flag,
                                     unsigned long long *count)
 {
@@ -338,6 +338,8 @@ __global__ void k_select_candidates(Grid g, const float *__restrict__ curl, uint
                 c |= (cu == 0.0f || cu >= g.thr);
             }
         }
+        // every start rule needs curl != 0 at the start voxel (the masked interior drops out)
+        c = c && __ldg(curl + v) != 0.0f;
         flag[v] = c ? 1 : 0;
         local += c ? 1 : 0;
     }
