@@ -116,6 +116,17 @@ typedef struct {
                                   FP64 -- for the anchor solver its one final sweep, a
                                   defect-correction step from the FP32 iteration; for the sweep
                                   solver every sweep.  Line integrals stay FP32 Kahan sums. */
+    int tile_width;            /* line order: a warp walks the lines of one direction through a
+                                  tile of 32 lattice points, tile_width (4, 8 or 16) wide;
+                                  0: 8 */
+    int dir_group;             /* line order: neighbouring directions interleaved per tile
+                                  (1-32); 0: 4 */
+    int autotune;              /* 1: omni3d_create picks tile_width and dir_group by timing one
+                                  sweep of each of a few candidate pairs on this grid and
+                                  direction set, and keeps the choice for the process, per
+                                  device and size class (largest grid dimension rounded up to
+                                  a multiple of 32, direction count, line spacing, walk rule);
+                                  tile_width and dir_group are then ignored */
 } omni3d_params;
 
 typedef struct {
@@ -136,6 +147,8 @@ typedef struct {
     int solver_used;           /* OMNI3D_SOLVER_*: the anchor solver falls back to the sweep
                                   solver when its operator would exceed anchor_max_links */
     int engine_used;           /* OMNI3D_ENGINE_LINES or OMNI3D_ENGINE_BRICKS */
+    int tile_width;            /* the line order in use (see omni3d_params) */
+    int dir_group;
 } omni3d_stats;
 
 /* Fill *p with the reference's defaults (K:8512-8535) and this implementation's. */
@@ -209,9 +222,9 @@ int omni3d_geometry_info(omni3d_ctx *ctx, long long *n_lines, long long *n_units
                          long long *walk_errors);
 
 /* Copy the line table to host memory: per line {entry voxel, exit voxel, direction, steps}
- * (4 x int32), n_max rows at most.  Lines are stored direction by direction in the
- * library's processing order (neighbouring directions adjacent) and, within a direction,
- * in lattice-point order; the direction column is the index in the caller's list. */
+ * (4 x int32), n_max rows at most.  Lines are stored in the library's processing order
+ * (groups of neighbouring directions, lattice tiles, direction, point: see tile_width and
+ * dir_group); the direction column is the index in the caller's list. */
 int omni3d_line_table(omni3d_ctx *ctx, int32_t *rows, long long n_max);
 
 /* Copy the staircase of line `line` (one axis code 0/1/2 per step) to host memory. */

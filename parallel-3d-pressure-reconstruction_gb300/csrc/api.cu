@@ -8,7 +8,10 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <utility>
 #include <vector>
 
@@ -189,6 +192,12 @@ int check_params(const omni3d_params *p, std::string *why)
         *why = "unknown initial_guess";
         return OMNI3D_ERR_ARG;
     }
+    if (p->tile_width != 0 && p->tile_width != 4 && p->tile_width != 8 && p->tile_width != 16) {
+        *why = "tile_width must be 0, 4, 8 or 16";
+        return OMNI3D_ERR_ARG;
+    }
+    if (p->dir_group < 0 || p->dir_group > 32) { *why = "dir_group must be 0..32"; return OMNI3D_ERR_ARG; }
+    if (p->autotune != 0 && p->autotune != 1) { *why = "autotune must be 0 or 1"; return OMNI3D_ERR_ARG; }
     double ng = std::max(std::max(p->nx, p->ny), p->nz) * 1.732 / (double)p->line_spacing;
     if (ng * ng * (double)p->n_dirs / 256.0 > 2.0e9) { *why = "too many lines (lattice x directions)"; return OMNI3D_ERR_RANGE; }
     return OMNI3D_OK;
@@ -410,6 +419,86 @@ void omni3d_default_params(omni3d_params *p)
 const char *omni3d_last_error(const omni3d_ctx *ctx) { return ctx ? ctx->err.c_str() : g_error.c_str(); }
 const char *omni3d_global_error(void) { return g_error.c_str(); }
 
+namespace {
+
+// Line-order tuning (params.autotune).  The line order decides which voxels the lanes of a
+// warp, and the warps of a block, touch at the same time, so the best tile width and
+// direction group depend on the grid and the direction set.  Each candidate pair is built
+// and timed with one plain sweep of a zero field (the sweep's cost depends on where its
+// gathers and reductions land, not on the values); the fastest pair is kept for the process,
+// per device and size class.
+struct TuneKey {
+    int device, size_class, nv, rule;
+    uint32_t ls_bits;
+    bool operator<(const TuneKey &o) const
+    {
+        return std::tie(device, size_class, nv, rule, ls_bits) <
+               std::tie(o.device, o.size_class, o.nv, o.rule, o.ls_bits);
+    }
+};
+std::mutex g_tune_mutex;
+std::map<TuneKey, std::pair<int, int>> g_tune_cache;
+
+cudaError_t tune_line_order(omni3d_ctx *ctx, std::string *err)
+{
+    Geometry &geo = ctx->geo;
+    const Grid &g = geo.grid;
+    uint32_t ls_bits;
+    std::memcpy(&ls_bits, &g.ls, sizeof(ls_bits));
+    const int mx = std::max(std::max(g.X, g.Y), g.Z);
+    const TuneKey key{ctx->prm.device, (mx + 31) / 32, geo.nv, geo.walk_rule, ls_bits};
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+        geo.tile_width = it->second.first;
+        geo.dir_group = it->second.second;
+        return cudaSuccess;
+    }
+    static const int kCand[][2] = {{8, 4}, {4, 4}, {16, 4}, {8, 2}, {8, 8}};
+    float4 *field = nullptr;
+    float *p = nullptr;
+    float2 *acc = nullptr;
+    const size_t V = (size_t)g.V;
+    cudaError_t e = cudaMalloc(&field, sizeof(float4) * V);
+    if (e == cudaSuccess) e = cudaMalloc(&p, sizeof(float) * V);
+    if (e == cudaSuccess) e = cudaMalloc(&acc, sizeof(float2) * V);
+    if (e == cudaSuccess) e = cudaMemsetAsync(field, 0, sizeof(float4) * V, ctx->st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(p, 0, sizeof(float) * V, ctx->st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(acc, 0, sizeof(float2) * V, ctx->st);
+    float best = 0.0f;
+    int bt = 8, bg = 4;
+    for (const auto &c : kCand) {
+        if (e != cudaSuccess) break;
+        geo.tile_width = c[0];
+        geo.dir_group = c[1];
+        if ((e = build_geometry(&geo, ctx->st, err)) != cudaSuccess) break;
+        Field F;
+        F.f32 = field;
+        e = sweep_full(geo, F, OMNI3D_METHOD_PLAIN, false, p, acc, ctx->st);  // warm-up
+        cudaEventRecord(ctx->ev[2], ctx->st);
+        if (e == cudaSuccess) e = sweep_full(geo, F, OMNI3D_METHOD_PLAIN, false, p, acc, ctx->st);
+        cudaEventRecord(ctx->ev[3], ctx->st);
+        if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev[3]);
+        const float ms = ms_between(ctx->ev[2], ctx->ev[3]);
+        free_geometry(&geo);
+        if (e == cudaSuccess && (best == 0.0f || ms < best)) {
+            best = ms;
+            bt = c[0];
+            bg = c[1];
+        }
+    }
+    cudaFree(field);
+    cudaFree(p);
+    cudaFree(acc);
+    if (e != cudaSuccess) return e;
+    geo.tile_width = bt;
+    geo.dir_group = bg;
+    g_tune_cache[key] = {bt, bg};
+    return cudaSuccess;
+}
+
+}  // namespace
+
 int omni3d_create(const omni3d_params *params, omni3d_ctx **out)
 {
     if (!out) return fail(nullptr, OMNI3D_ERR_ARG, "out is NULL");
@@ -468,8 +557,17 @@ int omni3d_create(const omni3d_params *params, omni3d_ctx **out)
     if ((e = cudaMemcpyAsync(ctx->geo.d_dirs, ctx->table.data(), sizeof(DirEntry) * ctx->table.size(),
                              cudaMemcpyHostToDevice, ctx->st)) != cudaSuccess)
         return bail(e, "upload dirs");
-    cudaEventRecord(ctx->ev[0], ctx->st);
+    ctx->geo.tile_width = params->tile_width ? params->tile_width : 8;
+    ctx->geo.dir_group = params->dir_group ? params->dir_group : 4;
     std::string gerr;
+    if (params->autotune && (e = tune_line_order(ctx, &gerr)) != cudaSuccess) {
+        ctx->err = "line-order tuning: " + (gerr.empty() ? std::string(cudaGetErrorString(e)) : gerr);
+        g_error = ctx->err;
+        int r = e == cudaErrorMemoryAllocation ? OMNI3D_ERR_NOMEM : OMNI3D_ERR_CUDA;
+        omni3d_destroy(ctx);
+        return r;
+    }
+    cudaEventRecord(ctx->ev[0], ctx->st);
     e = build_geometry(&ctx->geo, ctx->st, &gerr);
     if (e != cudaSuccess) {
         ctx->err = "line tracing: " + gerr;
@@ -904,6 +1002,8 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
         stats->kernel_launches = (long long)(__atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED) - launches0);
         stats->solver_used = solver;
         stats->engine_used = engine;
+        stats->tile_width = ctx->geo.tile_width;
+        stats->dir_group = ctx->geo.dir_group;
     }
     if (ctx->geo.walk_errors) return fail(ctx, OMNI3D_ERR_NUMERIC, "line walk hit the wrong-point branch");
     return OMNI3D_OK;
@@ -1143,6 +1243,8 @@ int omni3d_batch_solve(omni3d_batch *b, const float *const *ax, const float *con
         stats->kernel_launches = b->launches_per_graph;
         stats->solver_used = OMNI3D_SOLVER_ANCHOR;
         stats->engine_used = OMNI3D_ENGINE_LINES;
+        stats->tile_width = b->ctx.empty() ? 0 : b->ctx[0]->geo.tile_width;  // members may differ: the first's
+        stats->dir_group = b->ctx.empty() ? 0 : b->ctx[0]->geo.dir_group;
         for (omni3d_ctx *c : b->ctx) {
             stats->n_lines += c->geo.n_lines;
             stats->n_units += c->geo.n_units;

@@ -18,20 +18,19 @@ constexpr int kScanBlock = 1024;
 constexpr int kScanItems = 4;  // items per thread
 constexpr long long kScanTile = (long long)kScanBlock * kScanItems;
 
-// Candidate order: (group of `gsize` neighbouring directions, 8 x 4 tile of lattice points,
-// direction within the group, point within the tile).  A warp then holds the 32 lines of
-// one direction through an 8 x 4 patch of its lattice plane, a compact bundle whose
-// staircases share voxels and 32-byte sectors along the whole walk (a 32 x 1 row of the
-// lattice spreads over 32 lines' worth of width and shares far fewer), and a block of
-// warps holds the same patch of several nearly parallel directions, which walk through the
-// same voxels at the same time.
-constexpr int kTileU = 8;  // lattice columns per tile
-constexpr int kTileV = 4;  // lattice rows per tile
-static_assert(kTileU * kTileV == 32 && (kTileU & (kTileU - 1)) == 0, "a tile is one warp of lines");
+// Candidate order: (group of `gsize` neighbouring directions, tile of 32 lattice points,
+// direction within the group, point within the tile).  A tile is 2^tw_log2 lattice columns
+// wide and 32 / 2^tw_log2 rows high (8 x 4 by default).  A warp then holds the 32 lines of
+// one direction through a compact patch of its lattice plane, a bundle whose staircases
+// share voxels and 32-byte sectors along the whole walk (a 32 x 1 row of the lattice
+// spreads over 32 lines' worth of width and shares far fewer), and a block of warps holds
+// the same patch of several nearly parallel directions, which walk through the same voxels
+// at the same time.
 struct CandOrder {
     long long ng2;    // lattice points per direction
     long long tu;     // tiles across a lattice row
     long long nblk;   // tiles per direction
+    int tw_log2;      // log2 of the tile width (2, 3 or 4)
     int gsize;        // directions per group
     int nv;
 };
@@ -47,8 +46,8 @@ __device__ __forceinline__ bool trace_candidate(const Grid &g, const DirEntry *d
     long long blk = r / per_block;
     r -= blk * per_block;
     int d = (int)(grp * co.gsize + r / 32);
-    const long long u = (blk % co.tu) * kTileU + (r & (kTileU - 1));
-    const long long v = (blk / co.tu) * kTileV + ((r & 31) / kTileU);
+    const long long u = (blk % co.tu) * (1LL << co.tw_log2) + (r & ((1LL << co.tw_log2) - 1));
+    const long long v = (blk / co.tu) * (32LL >> co.tw_log2) + ((r & 31) >> co.tw_log2);
     *dir = d;
     if (d >= co.nv || u >= g.ng || v >= g.ng) return false;
     const long long pt = u + v * g.ng;  // lattice point: column u, row v
@@ -348,8 +347,10 @@ cudaError_t build_geometry(Geometry *g, cudaStream_t st, std::string *err)
     const Grid &G = g->grid;
     CandOrder co;
     co.ng2 = (long long)G.ng * G.ng;
-    co.tu = (G.ng + kTileU - 1) / kTileU;
-    co.nblk = co.tu * ((G.ng + kTileV - 1) / kTileV);
+    co.tw_log2 = g->tile_width == 4 ? 2 : (g->tile_width == 16 ? 4 : 3);
+    const long long tw = 1LL << co.tw_log2, th = 32LL >> co.tw_log2;
+    co.tu = (G.ng + tw - 1) / tw;
+    co.nblk = co.tu * ((G.ng + th - 1) / th);
     co.gsize = std::max(1, std::min(g->dir_group, g->nv));
     co.nv = g->nv;
     long long ngroups = (g->nv + co.gsize - 1) / co.gsize;

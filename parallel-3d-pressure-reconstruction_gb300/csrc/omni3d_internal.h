@@ -52,6 +52,7 @@ struct Geometry {
     Grid grid;
     int nv = 0;
     int dir_group = 4;              // neighbouring directions interleaved per lattice tile
+    int tile_width = 8;             // lattice tile width in points (4, 8 or 16; 32 points a tile)
     DirEntry *d_dirs = nullptr;
     float4 *d_off = nullptr;        // per line: centred offset (x, y, z) of its lattice point
     LineRec *d_lines = nullptr;

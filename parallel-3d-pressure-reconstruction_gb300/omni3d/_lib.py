@@ -39,14 +39,15 @@ class Params(C.Structure):
                 ("method", _i), ("solver", _i), ("grad_storage", _i), ("tol", _d), ("gauge", _i),
                 ("ref_i", _i), ("ref_j", _i), ("ref_k", _i), ("seed_first_iteration", _i), ("device", _i),
                 ("anchor_max_links", _ll), ("engine", _i), ("initial_guess", _i),
-                ("sweep_fp64", _i)]
+                ("sweep_fp64", _i), ("tile_width", _i), ("dir_group", _i), ("autotune", _i)]
 
 
 class Stats(C.Structure):
     _fields_ = [("iterations", _i), ("rel_change", _d), ("n_lines", _ll), ("n_units", _ll), ("walk_errors", _ll),
                 ("n_anchors", _ll), ("n_links", _ll), ("ms_geometry", _d), ("ms_setup", _d), ("ms_iterate", _d),
                 ("ms_final", _d), ("ms_total", _d), ("ms_sweep", _d),
-                ("kernel_launches", _ll), ("solver_used", _i), ("engine_used", _i)]
+                ("kernel_launches", _ll), ("solver_used", _i), ("engine_used", _i), ("tile_width", _i),
+                ("dir_group", _i)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -69,6 +69,55 @@ def test_line_table_bit_exact(omni, orc, match_lines, dims, ls, level):
             assert any(np.array_equal(s.line_steps(i), ax) for i in at[k]), k
 
 
+@pytest.mark.parametrize("tile_width,dir_group", [(4, 1), (16, 8), (8, 32)])
+def test_line_order_options(omni, orc, match_lines, tile_width, dir_group):
+    """Other line orders (tile width, directions per group) hold the same lines and
+    staircases and give the same solve up to the order of sums."""
+    dims = (21, 18, 15)
+    f = _field(dims, seed=14, sphere=3.5)
+    dirs = omni.icosphere(3)
+    curl = orc.curl(dims, f["spacing"], f["ax"], f["ay"], f["az"], f["mask"])
+    thr = float(np.percentile(curl[curl > 0], 85))
+    res = {}
+    for tw, dg in ((0, 0), (tile_width, dir_group)):
+        with omni.Omni3D(dims, f["spacing"], dirs, max_iter=4, method="select", threshold=thr, tile_width=tw,
+                         dir_group=dg) as s:
+            r = s.solve(f["ax"], f["ay"], f["az"], curl=curl)
+            assert (r.stats["tile_width"], r.stats["dir_group"]) == (tw or 8, dg or 4)
+            res[tw] = r
+            if tw:
+                got = s.line_table().astype(np.int64)
+                got[:, 0] &= 0xFFFFFFFF
+                got[:, 1] &= 0xFFFFFFFF
+                exp, geo = _lines_oracle(orc, dims, 1.0, dirs)
+                at = match_lines(got, exp)
+                for k in range(0, len(exp), max(1, len(exp) // 40)):
+                    io, xyz = geo[k]
+                    ax = orc.walk(dims, io, xyz, dirs[exp[k, 2]])
+                    assert any(np.array_equal(s.line_steps(i), ax) for i in at[k]), k
+    np.testing.assert_array_equal(res[0].count > 0, res[tile_width].count > 0)
+    assert synthetic.relative_l2(res[tile_width].count, res[0].count, gauge="none") < 1e-6
+    assert synthetic.relative_l2(res[tile_width].p, res[0].p, gauge="none") < 1e-6
+
+
+def test_autotune_picks_a_candidate_and_solves_alike(omni):
+    """params.autotune times a few line orders at creation and keeps the fastest per size
+    class; the result is the same solve."""
+    dims = (40, 36, 33)
+    f = _field(dims, seed=15, sphere=4.0)
+    dirs = omni.icosphere(3)
+    out = []
+    for tune in (True, True, False):
+        with omni.Omni3D(dims, f["spacing"], dirs, max_iter=4, autotune=tune) as s:
+            out.append(s.solve(f["ax"], f["ay"], f["az"]))
+    pairs = [(r.stats["tile_width"], r.stats["dir_group"]) for r in out]
+    assert pairs[0] in {(8, 4), (4, 4), (16, 4), (8, 2), (8, 8)}
+    assert pairs[1] == pairs[0]  # the same size class reuses the choice
+    assert pairs[2] == (8, 4)
+    np.testing.assert_array_equal(out[0].count, out[2].count)
+    assert synthetic.relative_l2(out[0].p, out[2].p, gauge="none") < 1e-6
+
+
 def test_curl_bit_exact(omni, orc):
     dims = (14, 11, 9)
     f = _field(dims, sphere=3.0)

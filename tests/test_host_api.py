@@ -272,6 +272,10 @@ def test_create_rejects_bad_params_without_gpu(omni):
     with pytest.raises(omni.Omni3DError) as e:
         omni.Omni3D((8, 8, 8), 1e-3, d, gauge="point", ref=(8, 0, 0))
     assert e.value.code == -1
+    for bad in ({"tile_width": 3}, {"tile_width": 32}, {"dir_group": 33}, {"dir_group": -1}):
+        with pytest.raises(omni.Omni3DError) as e:
+            omni.Omni3D((8, 8, 8), 1e-3, d, **bad)
+        assert e.value.code == -1
     # voxel indices are 32-bit on the device: 2^32 voxels and more are refused up front
     with pytest.raises(omni.Omni3DError) as e:
         omni.Omni3D((2048, 2048, 1024), 1e-3, d)
