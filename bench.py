@@ -283,8 +283,10 @@ def _event_time(fn, stream=None):
 def run_config4(args):
     """64 snapshots of uneven seeded sizes (each dimension ~ U[32, 160]), a vortex-ring core
     per snapshot, 5 % noise, 162 directions, plain method, K iterations: the whole batch in
-    one CUDA-graph launch (omni3d_batch_solve) against the same 64 solves issued one by one,
-    inputs resident on the device."""
+    one CUDA-graph launch (omni3d_batch_solve), inputs resident on the device.  The members
+    are created with the line-order autotuner (tile width and directions per group timed
+    per size class); the same batch with the default line order and the 64 solves issued one
+    by one are timed beside it."""
     import torch
 
     import omni3d
@@ -293,27 +295,42 @@ def run_config4(args):
     K = 20
     snaps = synthetic.batch_snapshots(count=64, lo=32, hi=160, seed=4)
     dirs = omni3d.icosphere(3)
-    solvers = [omni3d.Omni3D(s["dims"], s["spacing"], dirs, max_iter=K) for s in snaps]
     dev = [tuple(torch.from_numpy(s[k].reshape(-1)).cuda() for k in ("ax", "ay", "az")) for s in snaps]
-    out = [(torch.empty(s.V, device="cuda"), torch.empty(s.V, device="cuda")) for s in solvers]
-    units = sum(s.geometry_info()["n_units"] for s in solvers)
-    with omni3d.Batch(solvers) as b:
-        for _ in range(max(args.warmup, 1)):
-            b.solve(dev, out=out)
-        t_graph = [_event_time(lambda: b.solve(dev, out=out))[0] for _ in range(args.steps)]
-    for s, d in zip(solvers, dev):  # warm each context for the sequential form
-        s.solve(*d)
-    t_seq = [_event_time(lambda: [s.solve(*d) for s, d in zip(solvers, dev)])[0] for _ in range(args.steps)]
-    for s in solvers:
-        s.close()
-    tg, ts = float(np.mean(t_graph)), float(np.mean(t_seq))
+
+    def batch(autotune):
+        t0 = time.perf_counter()
+        solvers = [omni3d.Omni3D(s["dims"], s["spacing"], dirs, max_iter=K, autotune=autotune) for s in snaps]
+        t_create = time.perf_counter() - t0
+        out = [(torch.empty(s.V, device="cuda"), torch.empty(s.V, device="cuda")) for s in solvers]
+        choice = {}
+        for s, d in zip(solvers, dev):  # warm each context (and read its line order)
+            st = s.solve(*d).stats
+            choice.setdefault("max dim <= %d" % (32 * ((max(s.dims) + 31) // 32)), set()).add(
+                (st["tile_width"], st["dir_group"]))
+        with omni3d.Batch(solvers) as b:
+            for _ in range(max(args.warmup, 1)):
+                b.solve(dev, out=out)
+            t_graph = float(np.mean([_event_time(lambda: b.solve(dev, out=out))[0] for _ in range(args.steps)]))
+        t_seq = float(np.mean([_event_time(lambda: [s.solve(*d) for s, d in zip(solvers, dev)])[0]
+                               for _ in range(args.steps)]))
+        units = sum(s.geometry_info()["n_units"] for s in solvers)
+        for s in solvers:
+            s.close()
+        return t_graph, t_seq, t_create, {k: sorted(v) for k, v in sorted(choice.items())}, units
+
+    tg, ts, tc, choice, units = batch(True)
+    tg0, ts0, tc0, _, _ = batch(False)
     print(json.dumps({"metric": "batch time, 64 uneven snapshots (plain, %d iterations)" % K, "value": tg, "unit": "s",
                       "higher_is_better": False, "sequential_solves_s": ts, "speedup_vs_sequential": ts / tg,
+                      "default_line_order_s": tg0, "default_line_order_sequential_s": ts0,
+                      "line_order_by_size_class": {k: [list(p) for p in v] for k, v in choice.items()},
+                      "create_s_autotuned": tc, "create_s_default": tc0,
                       "snapshots_per_s": 64 / tg, "units_per_sweep_all": units,
                       "updates_per_s": K * units / tg, "steps": args.steps, "warmup": args.warmup,
                       "config": {"workload": "batch64_vortex_ring", "snapshots": 64, "sizes": "each dim U[32,160]",
                                  "direction_vertices": 162, "iterations": K, "method": "plain", "solver": "anchor",
-                                 "form": "one CUDA-graph launch (omni3d_batch_solve)"},
+                                 "form": "one CUDA-graph launch (omni3d_batch_solve)",
+                                 "line_order": "autotuned per size class (tile width, directions per group)"},
                       "data": "synthetic (seeded vortex rings, 5% noise)"}))
     return 0
 
