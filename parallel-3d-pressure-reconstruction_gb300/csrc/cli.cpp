@@ -11,6 +11,7 @@
 //                                   mini-curl|weighted-mini-curl
 //          --solver anchor|sweep  --tol T
 //          --gauge none|point|mean  --ref I,J,K  --grad f32|bf16  --device N
+//          --autotune (time a few line orders for this grid before the first snapshot)
 #include <dirent.h>
 #include <sys/stat.h>
 
@@ -65,7 +66,8 @@ int usage()
     std::fprintf(stderr,
                  "usage: omni3d [--params PATH] [--method select|plain|weighted|weighted-fixed-bc|select-fixed-bc|\n"
                  "              mini-curl|weighted-mini-curl] [--solver anchor|sweep] [--tol T]\n"
-                 "              [--gauge none|point|mean] [--ref I,J,K] [--grad f32|bf16] [--device N]\n");
+                 "              [--gauge none|point|mean] [--ref I,J,K] [--grad f32|bf16] [--device N]\n"
+                 "              [--autotune]\n");
     return 2;
 }
 
@@ -105,6 +107,7 @@ int main(int argc, char **argv)
             if (std::sscanf(v.c_str(), "%d,%d,%d", &prm.ref_i, &prm.ref_j, &prm.ref_k) != 3) return usage();
         } else if (k == "--grad") prm.grad_storage = val() == "bf16" ? OMNI3D_GRAD_BF16 : OMNI3D_GRAD_F32;
         else if (k == "--device") prm.device = std::atoi(val().c_str());
+        else if (k == "--autotune") prm.autotune = 1;
         else return usage();
     }
 

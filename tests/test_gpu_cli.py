@@ -24,7 +24,8 @@ def _write_input(path, f, u):
             fh.write(" ".join("%.9g" % c[r] for c in cols) + "\r\n")
 
 
-def test_cli_matches_library(omni, tmp_path):
+@pytest.mark.parametrize("extra", [[], ["--autotune"]])
+def test_cli_matches_library(omni, tmp_path, extra):
     from omni3d.build import CLI
 
     dims = (14, 12, 10)
@@ -44,7 +45,7 @@ def test_cli_matches_library(omni, tmp_path):
     params = [str(dims[0]), str(dims[1]), str(dims[2]), "0.001", "0.001", "0.001", "1", "1", "1", str(len(dirs)),
               "dirs.dat", ".\\acc\\", ".\\out\\", "3", repr(thr), "0.5", "", "", "", "", "", ""]
     (tmp_path / "Parameter_Omni3D.dat").write_text("\r\n".join(params) + "\r\n")
-    r = subprocess.run([CLI], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    r = subprocess.run([CLI] + extra, cwd=tmp_path, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert (tmp_path / "log.dat").read_text().startswith("Processing Starts")
     assert (tmp_path / "CurlofMaterialAcc_Sample.dat").exists()
