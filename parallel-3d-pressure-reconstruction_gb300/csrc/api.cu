@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -78,6 +79,11 @@ struct omni3d_ctx {
     int last_iterations = -1;  // iterations of the last solve (-1: no solve yet)
     int last_method = -1;
     cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    // tolerance-driven anchor iterations run as graph-captured chunks (see iterate_chunk)
+    cudaGraphExec_t iter_exec = nullptr;
+    std::vector<const void *> iter_key;  // what the captured chunk baked in
+    unsigned long long iter_launches = 0; // kernels per chunk
+    DeviceBuf iter_buf;                   // the chunk's stop word and per-step relative changes
 };
 
 namespace {
@@ -599,6 +605,8 @@ int omni3d_destroy(omni3d_ctx *ctx)
                          &ctx->curl, &ctx->pvol_a, &ctx->pvol_b, &ctx->pout, &ctx->cnt, &ctx->pncnt, &ctx->scratch,
                          &ctx->flags, &ctx->centre, &ctx->pncnt64})
         b->release();
+    if (ctx->iter_exec) cudaGraphExecDestroy(ctx->iter_exec);
+    ctx->iter_buf.release();
     for (auto &ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
     if (ctx->own_stream && ctx->st) cudaStreamDestroy(ctx->st);
@@ -776,6 +784,72 @@ int omni3d_sweep(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
     return engine_check(ctx, engine);
 }
 
+namespace {
+
+// Tolerance-driven anchor iterations in CUDA-graph chunks.  Checking the relative change on
+// the host after every step costs a stream synchronisation per iteration (about 70 us,
+// several times the step itself on small grids).  A chunk of kIterChunk steps is captured
+// once into a graph; each step is followed by a one-thread convergence test that sets a
+// device stop word, and every later kernel of the chunk sees the word and returns.  The host
+// synchronises once per chunk and learns from the word which step met the tolerance, so the
+// iterate and the iteration count are those of the step-by-step loop.
+constexpr int kIterChunk = 16;  // even: a chunk leaves the ping-pong buffers in place
+
+cudaError_t iterate_chunk(omni3d_ctx *ctx, const Anchor &A, int gauge, long long ref_anchor, double tol, float *pc,
+                          float *pn, double *red2, cudaStream_t st, int *j_out, double *rel_out)
+{
+    cudaError_t e = ctx->iter_buf.ensure(sizeof(double) * (kIterChunk + 1));
+    if (e != cudaSuccess) return e;
+    int *stop = ctx->iter_buf.as<int>();
+    double *rels = ctx->iter_buf.as<double>() + 1;
+    uint64_t tol_bits;
+    std::memcpy(&tol_bits, &tol, sizeof(tol_bits));
+    const std::vector<const void *> key = {
+        A.rowptr, A.rowlen, A.col, A.cw, A.bc, A.vox, A.red, reinterpret_cast<const void *>((uintptr_t)A.n),
+        reinterpret_cast<const void *>((uintptr_t)A.unit_weights), pc, pn, red2,
+        reinterpret_cast<const void *>((uintptr_t)gauge), reinterpret_cast<const void *>((intptr_t)ref_anchor),
+        reinterpret_cast<const void *>((uintptr_t)tol_bits), stop};
+    if (!ctx->iter_exec || ctx->iter_key != key) {
+        if (ctx->iter_exec) cudaGraphExecDestroy(ctx->iter_exec);
+        ctx->iter_exec = nullptr;
+        const unsigned long long l0 = __atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED);
+        if ((e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
+        cudaError_t ce = cudaMemsetAsync(stop, 0, sizeof(int), st);
+        for (int j = 0; j < kIterChunk && ce == cudaSuccess; j++) {
+            const float *from = (j % 2 == 0) ? pc : pn;
+            float *to = (j % 2 == 0) ? pn : pc;
+            ce = anchor_step(A, nullptr, false, gauge, ref_anchor, from, to, red2, st, stop);
+            if (ce == cudaSuccess) ce = converged_test_launch(red2, tol, j, stop, rels, st);
+        }
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamEndCapture(st, &graph);
+        const unsigned long long l1 = __atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED);
+        __atomic_fetch_sub(&g_kernel_launches, l1 - l0, __ATOMIC_RELAXED);  // captured, not launched
+        if (ce == cudaSuccess) ce = e;
+        if (ce == cudaSuccess) ce = cudaGraphInstantiate(&ctx->iter_exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (ce != cudaSuccess) {
+            ctx->iter_exec = nullptr;
+            return ce;
+        }
+        ctx->iter_key = key;
+        ctx->iter_launches = l1 - l0;
+    }
+    if ((e = cudaGraphLaunch(ctx->iter_exec, st)) != cudaSuccess) return e;
+    __atomic_fetch_add(&g_kernel_launches, ctx->iter_launches, __ATOMIC_RELAXED);
+    double h[kIterChunk + 1];
+    if ((e = cudaMemcpyAsync(h, ctx->iter_buf.p, sizeof(h), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess)
+        return e;
+    int stopv = 0;
+    std::memcpy(&stopv, &h[0], sizeof(stopv));
+    *j_out = stopv - 1;
+    *rel_out = h[1 + (stopv > 0 ? stopv - 1 : kIterChunk - 1)];
+    return cudaSuccess;
+}
+
+}  // namespace
+
 int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float *az, const float *curl,
                  const float *mask, const float *p_init, float *p_out, float *count_out, int device_ptrs,
                  omni3d_stats *stats)
@@ -938,7 +1012,19 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
         cudaEventRecord(ctx->ev[1], st);
         float *pc = A.pa, *pn = A.pb;
         int its = 0;
-        for (int it = 1; it <= K - 1; it++) {
+        for (int it = 1; it <= K - 1;) {
+            if (P.tol > 0.0 && it > 1 && A.n > 0 && st != nullptr && K - it >= kIterChunk) {
+                int j = -1;
+                CK(ctx, iterate_chunk(ctx, A, P.gauge, ref_anchor, P.tol, pc, pn, red2, st, &j, &rel));
+                if (j >= 0) {  // step it + j met the tolerance; step j wrote pn when j is even
+                    its = it + j;
+                    if (j % 2 == 0) std::swap(pc, pn);
+                    break;
+                }
+                its = it + kIterChunk - 1;
+                it += kIterChunk;
+                continue;
+            }
             CK(ctx, anchor_step(A, dpinit, seed && it == 1, P.gauge, ref_anchor, pc, pn, P.tol > 0.0 ? red2 : nullptr, st));
             its = it;
             std::swap(pc, pn);
@@ -948,6 +1034,7 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
                 rel = hred[1] > 0 ? std::sqrt(hred[0] / hred[1]) : 0.0;
                 if (rel < P.tol) break;
             }
+            it++;
         }
         cudaEventRecord(ctx->ev[2], st);
         float *vol = ctx->pvol_a.as<float>();

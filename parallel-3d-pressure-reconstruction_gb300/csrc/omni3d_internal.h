@@ -231,17 +231,23 @@ void anchor_free(Anchor *A);
 cudaError_t anchor_refresh_rhs(const Geometry &geo, const Field &f, bool bf16, Anchor *A,
                                cudaStream_t st);
 // One iteration p_next = (b + seed * p_init_a + M p_cur) / c; accumulates the gauged
-// change / norm sums into red[0..1] for the relative change.
+// change / norm sums into red[0..1] for the relative change.  With stop, every kernel of the
+// step returns at once while *stop != 0 (the gated steps of a graph-captured chunk).
 cudaError_t anchor_step(const Anchor &A, const float *p_init, bool seed, int gauge,
                         long long ref_anchor, const float *p_cur, float *p_next, double *red2,
-                        cudaStream_t st);
+                        cudaStream_t st, const int *stop = nullptr);
+// Launch the convergence test of step j of a chunk: rel_out[j] = sqrt(red2[0] / red2[1]),
+// *stop = j + 1 when it is below tol (no-op while *stop != 0).
+cudaError_t converged_test_launch(const double *red2, double tol, int j, int *stop, double *rel_out,
+                                  cudaStream_t st);
 // Gauged relative-change sums over the n values selected by mask (all when mask is null):
 // out2 = {sum (d - d_ref)^2, sum (p - p_ref)^2} with d = pn - pc; the shift is the value at
 // `ref` (point gauge), the mean (mean gauge) or zero.  Deterministic FP64 reduction;
 // scratch holds change_scratch_doubles().
 size_t change_scratch_doubles();
 cudaError_t change_sums(long long n, const float *pc, const float *pn, int gauge, long long ref,
-                        double *scratch, double *out2, cudaStream_t st, const uint8_t *mask);
+                        double *scratch, double *out2, cudaStream_t st, const uint8_t *mask,
+                        const int *stop = nullptr);
 // Flag the anchor voxels (line entries, or the segment starts of the selected method or a
 // small superset of them, plus ref_voxel when >= 0) into a V-byte array.  count1 is one
 // device word of scratch.

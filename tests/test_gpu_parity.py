@@ -342,6 +342,37 @@ def test_gauges_and_tolerance(omni, orc):
     assert abs(its[0] - its[1]) <= 1
 
 
+@pytest.mark.parametrize("gauge,method", [("mean", "plain"), ("point", "select"), ("mean", "weighted")])
+def test_tolerance_chunks_match_fixed_iterations(omni, orc, gauge, method):
+    """A tolerance stop runs the anchor iterations in graph-captured chunks with a device-side
+    stop word; the iterate and the count must be those of the same number of iterations run
+    one by one (up to the order of the FP32 atomic sums of the operator's right-hand side and
+    the final sweep, which differ between any two solves)."""
+    dims = (30, 26, 22)
+    f = _field(dims, seed=16, sphere=4.0)
+    dirs = omni.icosphere(3)
+    curl = orc.curl(dims, f["spacing"], f["ax"], f["ay"], f["az"], f["mask"]) if method != "plain" else None
+    thr = float(np.percentile(curl[curl > 0], 85)) if method == "select" else 0.0
+    kw = dict(method=method, threshold=thr, gauge=gauge, ref=(3, 0, 2))
+    with omni.Omni3D(dims, f["spacing"], dirs, max_iter=1000, tol=1e-6, **kw) as s:
+        r = s.solve(f["ax"], f["ay"], f["az"], curl=curl)
+        r2 = s.solve(f["ax"], f["ay"], f["az"], curl=curl)  # the captured chunk relaunched
+    K = r.stats["iterations"]
+    assert 20 < K < 1000 and r.stats["rel_change"] < 1e-6
+    # the plain operator is cached per context; the others are rebuilt per solve, their
+    # rows filled in atomic slot order
+    tol_p = 1e-6 if method == "plain" else 1e-5
+    assert abs(r2.stats["iterations"] - K) <= 1
+    assert synthetic.relative_l2(r2.p, r.p, gauge="none") < tol_p
+    with omni.Omni3D(dims, f["spacing"], dirs, max_iter=K, **kw) as s:
+        q = s.solve(f["ax"], f["ay"], f["az"], curl=curl)
+    if method == "plain":
+        np.testing.assert_array_equal(q.count, r.count)
+    else:
+        assert synthetic.relative_l2(q.count, r.count, gauge="none") < 1e-6
+    assert synthetic.relative_l2(q.p, r.p, gauge="none") < tol_p
+
+
 def test_bf16_gradient_storage(omni):
     dims = (24, 24, 24)
     f = _field(dims, seed=10)
