@@ -393,6 +393,8 @@ def main():
     ap.add_argument("--solver", default="anchor", choices=["anchor", "sweep"])
     ap.add_argument("--engine", default="auto", choices=["auto", "lines", "bricks"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--autotune", action="store_true", help="line order picked by the autotuner (default: 8 x 4 "
+                                                              "tiles, 4 directions per group)")
     ap.add_argument("--profile", action="store_true",
                     help="only the warm-up and timed solves (for ncu): no calibration, e2e, variants or CPU arm")
     ap.add_argument("--no-variants", action="store_true", help="skip timing the sweep-solver and BF16 forms")
@@ -437,7 +439,7 @@ def main():
     dev = torch.device("cuda", local)
 
     def make(iters, tol=0.0, **kw):
-        opts = dict(solver=args.solver, grad=args.grad, engine=args.engine)
+        opts = dict(solver=args.solver, grad=args.grad, engine=args.engine, autotune=args.autotune)
         opts.update(kw)
         return omni3d.Omni3D(dims, f["spacing"], dirs, max_iter=iters, method="select", threshold=FLT_MAX, tol=tol,
                              gauge="mean", device=local, **opts)
@@ -574,6 +576,8 @@ def main():
         "geometry_ms": stats["ms_geometry"], "n_anchors": stats["n_anchors"], "n_links": stats["n_links"],
     }
     line["config"]["engine"] = ["auto", "lines", "bricks"][engine_used]
+    line["config"]["line_order"] = {"tile_width": stats["tile_width"], "dir_group": stats["dir_group"],
+                                    "autotuned": bool(args.autotune)}
     line["clocks"] = clk.summary()
     if rank == 0 and world == 1 and not args.no_cpu and not args.profile:  # the CPU sample at N = 1 only
         try:
