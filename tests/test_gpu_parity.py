@@ -318,6 +318,21 @@ def test_minimal_grid_and_pole_directions(omni, orc):
         assert synthetic.relative_l2(r.p, ep, gauge="none") < TOL_P_PLAIN
 
 
+def test_large_direction_set_matches_oracle(omni, orc):
+    """2562 vertices (icosphere level 5): many direction groups and a long serpentine order
+    over the sphere; counts exact, p against the FP64 oracle."""
+    dims = (13, 11, 9)
+    f = _field(dims, seed=17)
+    dirs = omni.icosphere(5)
+    assert len(dirs) == 2562
+    p0 = _pinit(dims, seed=6)
+    with omni.Omni3D(dims, f["spacing"], dirs, max_iter=2) as s:
+        r = s.solve(f["ax"], f["ay"], f["az"], p_init=p0)
+    ep, ecnt = orc.solve(dims, f["spacing"], dirs, f["ax"], f["ay"], f["az"], p0, 2, precision="f64")
+    np.testing.assert_array_equal(r.count.reshape(-1), ecnt.astype(np.float32))
+    assert synthetic.relative_l2(r.p, ep, gauge="none") < TOL_P_PLAIN
+
+
 def test_gauges_and_tolerance(omni, orc):
     dims = (16, 16, 16)
     f = _field(dims, seed=9)
