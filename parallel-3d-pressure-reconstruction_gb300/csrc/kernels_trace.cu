@@ -25,15 +25,30 @@ constexpr long long kScanTile = (long long)kScanBlock * kScanItems;
 // share voxels and 32-byte sectors along the whole walk (a 32 x 1 row of the lattice
 // spreads over 32 lines' worth of width and shares far fewer), and a block of warps holds
 // the same patch of several nearly parallel directions, which walk through the same voxels
-// at the same time.
+// at the same time.  Tiles are visited in Z order within super-tiles of 32 x 32 tiles, the
+// super-tiles row by row, so the lines in flight at any moment (about a thousand tiles' worth)
+// cover a compact patch of the lattice plane rather than a long strip: at 512^3 their L2
+// footprints overlap more (final sweep 953 -> 854 ms; 256^3 unchanged).
+constexpr int kSuperLog2 = 5;  // super-tile side in tiles: 32
 struct CandOrder {
     long long ng2;    // lattice points per direction
-    long long tu;     // tiles across a lattice row
-    long long nblk;   // tiles per direction
+    long long su;     // super-tiles across the lattice plane
+    long long nblk;   // tile slots per direction (super-tiles x 1024; slots outside the lattice are empty)
     int tw_log2;      // log2 of the tile width (2, 3 or 4)
     int gsize;        // directions per group
     int nv;
 };
+
+// Even bits of x, packed (the column of a Z-order index).
+__device__ __forceinline__ uint32_t z_compact(uint32_t x)
+{
+    x &= 0x55555555u;
+    x = (x ^ (x >> 1)) & 0x33333333u;
+    x = (x ^ (x >> 2)) & 0x0f0f0f0fu;
+    x = (x ^ (x >> 4)) & 0x00ff00ffu;
+    x = (x ^ (x >> 8)) & 0x0000ffffu;
+    return x;
+}
 
 __device__ __forceinline__ bool trace_candidate(const Grid &g, const DirEntry *dirs, const CandOrder &co,
                                                 long long c, int in[3], int out[3], float o[3],
@@ -46,8 +61,12 @@ __device__ __forceinline__ bool trace_candidate(const Grid &g, const DirEntry *d
     long long blk = r / per_block;
     r -= blk * per_block;
     int d = (int)(grp * co.gsize + r / 32);
-    const long long u = (blk % co.tu) * (1LL << co.tw_log2) + (r & ((1LL << co.tw_log2) - 1));
-    const long long v = (blk / co.tu) * (32LL >> co.tw_log2) + ((r & 31) >> co.tw_log2);
+    const long long sup = blk >> (2 * kSuperLog2);
+    const uint32_t z = (uint32_t)(blk & ((1LL << (2 * kSuperLog2)) - 1));
+    const long long tx = (sup % co.su) * (1LL << kSuperLog2) + z_compact(z);
+    const long long ty = (sup / co.su) * (1LL << kSuperLog2) + z_compact(z >> 1);
+    const long long u = tx * (1LL << co.tw_log2) + (r & ((1LL << co.tw_log2) - 1));
+    const long long v = ty * (32LL >> co.tw_log2) + ((r & 31) >> co.tw_log2);
     *dir = d;
     if (d >= co.nv || u >= g.ng || v >= g.ng) return false;
     const long long pt = u + v * g.ng;  // lattice point: column u, row v
@@ -349,8 +368,9 @@ cudaError_t build_geometry(Geometry *g, cudaStream_t st, std::string *err)
     co.ng2 = (long long)G.ng * G.ng;
     co.tw_log2 = g->tile_width == 4 ? 2 : (g->tile_width == 16 ? 4 : 3);
     const long long tw = 1LL << co.tw_log2, th = 32LL >> co.tw_log2;
-    co.tu = (G.ng + tw - 1) / tw;
-    co.nblk = co.tu * ((G.ng + th - 1) / th);
+    const long long tu = (G.ng + tw - 1) / tw, tv = (G.ng + th - 1) / th, side = 1LL << kSuperLog2;
+    co.su = (tu + side - 1) / side;
+    co.nblk = co.su * ((tv + side - 1) / side) * side * side;
     co.gsize = std::max(1, std::min(g->dir_group, g->nv));
     co.nv = g->nv;
     long long ngroups = (g->nv + co.gsize - 1) / co.gsize;
