@@ -234,9 +234,10 @@ int omni3d_line_steps(omni3d_ctx *ctx, long long line, int8_t *axes, int cap);
 #define OMNI3D_NOALLOC_MAX_VOXELS (64LL * 64 * 64)
 
 /* omni3d_sweep without any device allocation, for callers that cannot call cudaMalloc at
- * that point: a solver step running inside a CUDA-graph capture, a framework whose own
- * memory pool owns the device, a real-time loop that cannot take cudaMalloc's implicit
- * synchronisation.  No counterpart in the reference.  Same arguments and result as
+ * that point: a framework whose own memory pool owns the device and forbids driver
+ * allocations inside its step, a plugin loaded into an application with a fixed device
+ * memory budget, a real-time loop that cannot take cudaMalloc's implicit synchronisation.
+ * No counterpart in the reference.  Same arguments and result as
  * omni3d_sweep with device pointers (pn and count are added to), FP32 gradient storage
  * only, at most OMNI3D_NOALLOC_MAX_VOXELS voxels (larger grids are rejected with
  * OMNI3D_ERR_RANGE).  The packed field and the (pn, count) accumulator live in static
@@ -244,8 +245,9 @@ int omni3d_line_steps(omni3d_ctx *ctx, long long line, int8_t *axes, int cap);
  * call only enqueues work on `stream` (NULL: the context's stream); the results are ready
  * when that stream reaches them.  All calls share the static arrays: calls that overlap on
  * the GPU (other streams, other contexts, other threads) race and must be serialised by
- * the caller.  The first call on a device looks up the arrays' device addresses, so make
- * it before any stream capture. */
+ * the caller.  The first call on a device looks up the arrays' device addresses (a
+ * one-time set-up on that device), so make it before any stream capture.  The caller's
+ * current device is left as it was. */
 int omni3d_sweep_noalloc(omni3d_ctx *ctx, const float *ax, const float *ay, const float *az,
                          const float *curl, const float *p, float *pn, float *count,
                          void *stream);

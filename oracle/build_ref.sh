@@ -2,10 +2,11 @@
 # Recipe for oracle/_ref: the reference's own CPU code for the omni path, compiled from
 # its sources, used only to pin the oracle and as the timed CPU baseline.
 #
-#   stage  (needs the reference tree, default /root/reference; REF_ROOT overrides):
+#   stage  (needs the reference tree, located by REF_ROOT, which has no default):
 #          copies the reference functions on the hot path, by line range, from
-#          Omni3D_8.0/Omni3D_8.0/kernel.cu, plus sor3D.cpp, calRHS.cpp and
-#          initialIntegration.cpp, into
+#          Omni3D_8.0/Omni3D_8.0/kernel.cu, plus sor3D.cpp, calRHS.cpp,
+#          initialIntegration.cpp and the direction files GridIcosahedronDivide{2,3,4}.dat
+#          of Omni3D_8.0/Executable, into
 #          oracle/_ref/src/ (git-ignored build intermediates, never committed).
 #   build  compiles oracle/_ref/src/* with oracle/ref_driver.cpp into
 #          oracle/_ref/libomni_ref.so.  Runs wherever oracle/_ref/src exists, so a
@@ -24,12 +25,13 @@ set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 OUT="$HERE/_ref"
 SRC="$OUT/src"
-REF_ROOT="${REF_ROOT:-/root/reference}"
+REF_ROOT="${REF_ROOT:-}"
 K="$REF_ROOT/Omni3D_8.0/Omni3D_8.0"
 CXX="${CXX:-g++}"
 what="${1:-all}"
 
 stage() {
+    [ -n "$REF_ROOT" ] || { echo "build_ref: set REF_ROOT to the reference checkout to stage its sources" >&2; return 1; }
     [ -f "$K/kernel.cu" ] || { echo "build_ref: reference not found at $K" >&2; return 1; }
     mkdir -p "$SRC/stub"
     {
@@ -55,6 +57,9 @@ stage() {
     tr -d '\r' < "$K/initialIntegration.cpp" > "$SRC/initialIntegration.cpp"
     tr -d '\r' < "$K/initialIntegration.h" > "$SRC/initialIntegration.h"
     printf '#include <cstring>\n#include <cstdlib>\n#include <cmath>\n' > "$SRC/stub/afx.h"
+    for lv in 2 3 4; do
+        cp "$REF_ROOT/Omni3D_8.0/Executable/GridIcosahedronDivide$lv.dat" "$SRC/"
+    done
     # the staged files must still hold the functions the driver binds
     grep -q 'bool cross2point' "$SRC/ref_kernel_extract.cpp"
     grep -q 'float bodyIntegralInner(' "$SRC/ref_kernel_extract.cpp"

@@ -719,6 +719,180 @@ DEFINE_SOLVE(f32, float)
 DEFINE_SOLVE(f64, double)
 
 /* ------------------------------------------------------------------------------------ */
+/* the same iteration with the line geometry traced and walked once                      */
+/* ------------------------------------------------------------------------------------ */
+
+/* orc_solve_f64 re-traces and re-walks every line in every sweep, as the reference does.
+ * For fixed points at the full grid sizes of the benchmark (hundreds of iterations of a
+ * direction subset) the lines are traced once here -- the same cross2point, validity test
+ * and walk per (direction, lattice point) -- and only the accumulation (the f64 line
+ * functions above, unchanged) runs per iteration.  Lines are processed in (direction,
+ * lattice point) order, split into nthreads contiguous blocks of about equal step count
+ * with private accumulators added in block order.  With tol > 0 the iteration stops after
+ * the first iteration whose mean-gauged relative change over the voxels with count > 0,
+ * sqrt(sum (d - mean d)^2 / sum (p - mean p)^2) with d = p_new - p_old, is below tol.
+ * The iterates after the iteration counts save_at[0..nsave) (ascending) are copied to
+ * saves + j * V.  Returns the number of lines that hit the reference's "Wrong Point" branch. */
+typedef struct {
+    int in[3], out[3];
+    int n;
+    long off;  /* first step in the step array */
+} orc_cline;
+
+typedef struct {
+    orc_cline *lines;
+    long nl, capl;
+    signed char *steps;
+    long ns, caps;
+    long errors;
+} orc_clist;
+
+static void clist_push(orc_clist *L, const int in[3], const int out[3], const signed char *ax, int n)
+{
+    if (L->nl == L->capl) {
+        L->capl = L->capl ? 2 * L->capl : 1024;
+        L->lines = (orc_cline *)realloc(L->lines, sizeof(orc_cline) * (size_t)L->capl);
+    }
+    if (L->ns + n > L->caps) {
+        while (L->ns + n > L->caps) L->caps = L->caps ? 2 * L->caps : 65536;
+        L->steps = (signed char *)realloc(L->steps, (size_t)L->caps);
+    }
+    orc_cline *c = &L->lines[L->nl++];
+    memcpy(c->in, in, sizeof(c->in));
+    memcpy(c->out, out, sizeof(c->out));
+    c->n = n;
+    c->off = L->ns;
+    memcpy(L->steps + L->ns, ax, (size_t)n);
+    L->ns += n;
+}
+
+long orc_solve_cached_f64(const orc_problem *P, const float *au, const float *av, const float *aw,
+                          const float *curl, const float *p_init, int niter, double tol, double *p,
+                          double *cnt, int nthreads, int *iters_out, double *rel_out, const int *save_at,
+                          int nsave, double *saves)
+{
+    const long V = P->X * P->Y * P->Z;
+    const int ng = orc_nogrid(P->X, P->Y, P->Z, P->ls, P->geom_cpu_twin);
+    const int rule = orc_mode_walk_rule(P->mode);
+    const long cap = max_path(P->X, P->Y, P->Z);
+    if (nthreads < 1) nthreads = 1;
+    orc_clist *per_dir = (orc_clist *)calloc((size_t)P->nv, sizeof(orc_clist));
+    /* trace and walk once, one direction per task */
+    _Pragma("omp parallel for num_threads(nthreads) schedule(dynamic, 1)")
+    for (int d = 0; d < P->nv; d++) {
+        signed char *ax = (signed char *)malloc((size_t)cap);
+        float c[4];
+        orc_dir_coeffs(P->k1[d], P->k2[d], P->k3[d], P->geom_cpu_twin, c);
+        for (int pt = 0; pt < ng * ng; pt++) {
+            float xyz[3];
+            int in[3], out[3];
+            orc_line_offset(pt, ng, P->ls, c, xyz);
+            orc_cross2point(P->X, P->Y, P->Z, xyz[0], xyz[1], xyz[2], P->k1[d], P->k2[d], P->k3[d], in, out);
+            if (!orc_line_valid(P->X, P->Y, P->Z, in, out)) continue;
+            int n = orc_walk_rule(P->X, P->Y, P->Z, in, out, xyz[0], xyz[1], xyz[2], P->k1[d], P->k2[d], P->k3[d],
+                                  rule, curl, ax, (int)cap);
+            if (n < 0) {
+                if (rule == 0) per_dir[d].errors++;
+                n = -n - 1;
+            }
+            clist_push(&per_dir[d], in, out, ax, n);
+        }
+        free(ax);
+    }
+    /* concatenate in direction order */
+    long nl = 0, ns = 0, errors = 0;
+    for (int d = 0; d < P->nv; d++) {
+        nl += per_dir[d].nl;
+        ns += per_dir[d].ns;
+        errors += per_dir[d].errors;
+    }
+    orc_cline *lines = (orc_cline *)malloc(sizeof(orc_cline) * (size_t)(nl > 0 ? nl : 1));
+    signed char *steps = (signed char *)malloc((size_t)(ns > 0 ? ns : 1));
+    for (long d = 0, l0 = 0, s0 = 0; d < P->nv; d++) {
+        for (long i = 0; i < per_dir[d].nl; i++) {
+            lines[l0 + i] = per_dir[d].lines[i];
+            lines[l0 + i].off += s0;
+        }
+        memcpy(steps + s0, per_dir[d].steps, (size_t)per_dir[d].ns);
+        l0 += per_dir[d].nl;
+        s0 += per_dir[d].ns;
+        free(per_dir[d].lines);
+        free(per_dir[d].steps);
+    }
+    free(per_dir);
+    /* thread blocks of about equal work (steps + 1 per line) */
+    long *bound = (long *)malloc(sizeof(long) * (size_t)(nthreads + 1));
+    {
+        long total = ns + nl, acc = 0, li = 0;
+        bound[0] = 0;
+        for (int t = 1; t < nthreads; t++) {
+            long target = total * t / nthreads;
+            while (li < nl && acc < target) acc += lines[li++].n + 1;
+            bound[t] = li;
+        }
+        bound[nthreads] = nl;
+    }
+    orc_grid g = {P->X, P->Y, P->Z, P->dx, P->dy, P->dz, P->rho, P->thr};
+    double *pn = (double *)malloc(sizeof(double) * (size_t)V);
+    double *pp = (double *)malloc(sizeof(double) * (size_t)V * 2 * (size_t)nthreads);
+    double *pold = (double *)malloc(sizeof(double) * (size_t)V);
+    for (long v = 0; v < V; v++) { p[v] = (double)p_init[v]; pn[v] = (double)p_init[v]; cnt[v] = 0; }
+    int it = 0;
+    double rel = 0.0;
+    for (it = 0; it < niter;) {
+        memcpy(pold, p, sizeof(double) * (size_t)V);
+        _Pragma("omp parallel for num_threads(nthreads) schedule(static, 1)")
+        for (int t = 0; t < nthreads; t++) {
+            double *mypn = pp + (size_t)V * 2 * t, *mycnt = mypn + V;
+            memset(mypn, 0, sizeof(double) * 2 * (size_t)V);
+            for (long i = bound[t]; i < bound[t + 1]; i++) {
+                const orc_cline *c = &lines[i];
+                const signed char *ax = steps + c->off;
+                if (P->mode == 0 || P->mode == 5)
+                    line_plain_f64(&g, c->in, c->out, ax, c->n, au, av, aw, p, mypn, mycnt, P->mode == 0);
+                else if (P->mode == 2 || P->mode == 3)
+                    line_weighted_f64(&g, c->in, c->out, ax, c->n, au, av, aw, curl, p, mypn, mycnt);
+                else if (P->mode == 6)
+                    line_weighted_mc_f64(&g, c->in, c->out, ax, c->n, au, av, aw, curl, p, mypn, mycnt);
+                else
+                    line_select_f64(&g, c->in, c->out, ax, c->n, au, av, aw, curl, p, mypn, mycnt);
+            }
+        }
+        memset(cnt, 0, sizeof(double) * (size_t)V);
+        for (int t = 0; t < nthreads; t++) {
+            const double *mypn = pp + (size_t)V * 2 * t, *mycnt = mypn + V;
+            for (long v = 0; v < V; v++) { pn[v] += mypn[v]; cnt[v] += mycnt[v]; }
+        }
+        orc_divide_f64(V, p, pn, cnt, 1);
+        it++;
+        for (int j = 0; j < nsave; j++)
+            if (save_at[j] == it) memcpy(saves + (size_t)j * V, p, sizeof(double) * (size_t)V);
+        /* mean-gauged relative change */
+        double sd = 0, sp = 0, m = 0;
+        for (long v = 0; v < V; v++)
+            if (cnt[v] > 0) { sd += p[v] - pold[v]; sp += p[v]; m += 1; }
+        double md = m > 0 ? sd / m : 0, mp = m > 0 ? sp / m : 0, a = 0, b = 0;
+        for (long v = 0; v < V; v++)
+            if (cnt[v] > 0) {
+                double dd = p[v] - pold[v] - md, q = p[v] - mp;
+                a += dd * dd;
+                b += q * q;
+            }
+        rel = b > 0 ? sqrt(a / b) : 0.0;
+        if (tol > 0 && rel < tol) break;
+    }
+    if (iters_out) *iters_out = it;
+    if (rel_out) *rel_out = rel;
+    free(lines);
+    free(steps);
+    free(bound);
+    free(pn);
+    free(pp);
+    free(pold);
+    return errors;
+}
+
+/* ------------------------------------------------------------------------------------ */
 /* helpers exposed for the tests                                                          */
 /* ------------------------------------------------------------------------------------ */
 
@@ -975,4 +1149,195 @@ void orc_centre_integration(long X, long Y, long Z, double dx, double dy, double
                     p[ind] = n == 1 ? v : (n == 2 ? v / 2.0 : v / 3.0);
                 }
     }
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* the reference's CPU Poisson baseline (sor3D.cpp) restated, for counting its iterations */
+/* ------------------------------------------------------------------------------------ */
+
+/* sor3D.cpp:9-1588 with its BCScheme all zero and its weights weight1 = weight2 = 0
+ * (sor3D.cpp:5-7) is a weighted Jacobi iteration with omega = 0.8 on the Neumann Laplacian:
+ * every voxel takes pn = (sum of its in-box axis neighbours + RHS) / (number of them) --
+ * 6 inside, 5 on a face, 4 on an edge, 3 at a corner, the neighbours added in the order
+ * i-1, i+1, j-1, j+1, k-1, k+1 -- then pn = p + 0.8 * (pn - p) (sor3D.cpp:739).  Each loop of
+ * sor3D runs two such steps (a forward and a backward pass, sor3D.cpp:790-1575), so it
+ * always takes an even number of steps.  This restatement runs the same steps with OpenMP;
+ * it exists to count how many steps the reference needs at sizes where running the
+ * reference itself to that point takes hours (the reference's own seconds per step are
+ * timed separately). */
+static void jacobi_step_f64(long X, long Y, long Z, const double *rhs, const double *p, double *pn,
+                            int nthreads)
+{
+    const long XY = X * Y;
+    _Pragma("omp parallel for num_threads(nthreads) schedule(static)")
+    for (long k = 0; k < Z; k++)
+        for (long j = 0; j < Y; j++)
+            for (long i = 0; i < X; i++) {
+                const long v = i + j * X + k * XY;
+                double s = 0.0;
+                int n = 0, first = 1;
+#define ORC_NB(cond, off)                         \
+    if (cond) {                                   \
+        s = first ? p[v + (off)] : s + p[v + (off)]; \
+        first = 0;                                \
+        n++;                                      \
+    }
+                ORC_NB(i > 0, -1)
+                ORC_NB(i < X - 1, 1)
+                ORC_NB(j > 0, -X)
+                ORC_NB(j < Y - 1, X)
+                ORC_NB(k > 0, -XY)
+                ORC_NB(k < Z - 1, XY)
+#undef ORC_NB
+                s += rhs[v];
+                s = s / (double)n;
+                pn[v] = p[v] + 0.8 * (s - p[v]);
+            }
+}
+
+/* Mean-gauged relative L2 distance of p from ref (ref already mean-free). */
+static double gauged_rel_f64(long V, const double *p, const double *ref, int nthreads)
+{
+    double sp = 0.0;
+    _Pragma("omp parallel for num_threads(nthreads) reduction(+ : sp)")
+    for (long v = 0; v < V; v++) sp += p[v];
+    const double mp = sp / (double)V;
+    double a = 0.0, b = 0.0;
+    _Pragma("omp parallel for num_threads(nthreads) reduction(+ : a, b)")
+    for (long v = 0; v < V; v++) {
+        const double d = p[v] - mp - ref[v];
+        a += d * d;
+        b += ref[v] * ref[v];
+    }
+    return b > 0 ? sqrt(a / b) : 0.0;
+}
+
+/* nsteps steps of the restated iteration from p (in place). */
+void orc_sor_steps_f64(long X, long Y, long Z, const double *rhs, double *p, long nsteps, int nthreads)
+{
+    const long V = X * Y * Z;
+    double *pn = (double *)malloc(sizeof(double) * (size_t)V);
+    for (long s = 0; s < nsteps; s++) {
+        jacobi_step_f64(X, Y, Z, rhs, p, pn, nthreads);
+        memcpy(p, pn, sizeof(double) * (size_t)V);
+    }
+    free(pn);
+}
+
+/* The converged (mean-free) solution of the restated iteration by conjugate gradients:
+ * its fixed point solves A p = rhs - c * d, where A is the Neumann Laplacian (A p)_v =
+ * d_v p_v - sum of in-box neighbours, d_v the neighbour count, and c = sum(rhs) / sum(d)
+ * (the part of rhs along the constant mode, which only shifts the iterate's mean).
+ * Stops when ||r|| <= tol * ||b||; returns the CG iterations. */
+long orc_sor_converged_f64(long X, long Y, long Z, const double *rhs, double tol, long max_iter, double *p,
+                           int nthreads)
+{
+    const long V = X * Y * Z, XY = X * Y;
+    double *b = (double *)malloc(sizeof(double) * (size_t)V);
+    double *r = (double *)malloc(sizeof(double) * (size_t)V);
+    double *d = (double *)malloc(sizeof(double) * (size_t)V);
+    double *q = (double *)malloc(sizeof(double) * (size_t)V);
+    double *nb = (double *)malloc(sizeof(double) * (size_t)V);
+    double srhs = 0.0, sd = 0.0;
+    for (long v = 0; v < V; v++) {
+        long i = v % X, j = (v / X) % Y, k = v / XY;
+        nb[v] = (double)((i > 0) + (i < X - 1) + (j > 0) + (j < Y - 1) + (k > 0) + (k < Z - 1));
+        srhs += rhs[v];
+        sd += nb[v];
+    }
+    const double c = srhs / sd;
+    double bb = 0.0;
+    for (long v = 0; v < V; v++) {
+        b[v] = rhs[v] - c * nb[v];
+        p[v] = 0.0;
+        r[v] = b[v];
+        d[v] = r[v];
+        bb += b[v] * b[v];
+    }
+    double rr = bb;
+    long it = 0;
+    while (it < max_iter && rr > tol * tol * bb) {
+        double dq = 0.0;
+        _Pragma("omp parallel for num_threads(nthreads) reduction(+ : dq) schedule(static)")
+        for (long k = 0; k < Z; k++)
+            for (long j = 0; j < Y; j++)
+                for (long i = 0; i < X; i++) {
+                    const long v = i + j * X + k * XY;
+                    double s = nb[v] * d[v];
+                    if (i > 0) s -= d[v - 1];
+                    if (i < X - 1) s -= d[v + 1];
+                    if (j > 0) s -= d[v - X];
+                    if (j < Y - 1) s -= d[v + X];
+                    if (k > 0) s -= d[v - XY];
+                    if (k < Z - 1) s -= d[v + XY];
+                    q[v] = s;
+                    dq += d[v] * s;
+                }
+        const double alpha = rr / dq;
+        double rr2 = 0.0;
+        _Pragma("omp parallel for num_threads(nthreads) reduction(+ : rr2)")
+        for (long v = 0; v < V; v++) {
+            p[v] += alpha * d[v];
+            r[v] -= alpha * q[v];
+            rr2 += r[v] * r[v];
+        }
+        const double beta = rr2 / rr;
+        rr = rr2;
+        _Pragma("omp parallel for num_threads(nthreads)")
+        for (long v = 0; v < V; v++) d[v] = r[v] + beta * d[v];
+        it++;
+    }
+    double sp = 0.0;
+    for (long v = 0; v < V; v++) sp += p[v];
+    for (long v = 0; v < V; v++) p[v] -= sp / (double)V;
+    free(b);
+    free(r);
+    free(d);
+    free(q);
+    free(nb);
+    return it;
+}
+
+/* Steps of the restated iteration from p = 0 until the mean-gauged relative L2 distance
+ * from ref (mean-free, e.g. orc_sor_converged_f64) is at most target, counted in sor3D's
+ * pairs (the result is even); the distance is checked every `check` pairs and the last
+ * interval is bisected by re-running from its start.  Returns -1 when max_steps pass. */
+long orc_sor_steps_to_f64(long X, long Y, long Z, const double *rhs, const double *ref, double target, long max_steps,
+                          long check, int nthreads, double *err_out)
+{
+    const long V = X * Y * Z;
+    double *a = (double *)calloc((size_t)V, sizeof(double));
+    double *b = (double *)malloc(sizeof(double) * (size_t)V);
+    double *keep = (double *)malloc(sizeof(double) * (size_t)V);
+    if (check < 1) check = 1;
+    long steps = 0, found = -1;
+    double err = gauged_rel_f64(V, a, ref, nthreads);
+    while (steps < max_steps && err > target) {
+        memcpy(keep, a, sizeof(double) * (size_t)V);
+        const long s0 = steps;
+        for (long c = 0; c < check; c++) {  /* one pair: a -> b -> a */
+            jacobi_step_f64(X, Y, Z, rhs, a, b, nthreads);
+            jacobi_step_f64(X, Y, Z, rhs, b, a, nthreads);
+        }
+        steps += 2 * check;
+        err = gauged_rel_f64(V, a, ref, nthreads);
+        if (err <= target) {  /* the first even step count in (s0, steps] that meets target */
+            memcpy(a, keep, sizeof(double) * (size_t)V);
+            long s = s0;
+            double e = 0.0;
+            do {
+                jacobi_step_f64(X, Y, Z, rhs, a, b, nthreads);
+                jacobi_step_f64(X, Y, Z, rhs, b, a, nthreads);
+                s += 2;
+                e = gauged_rel_f64(V, a, ref, nthreads);
+            } while (e > target && s < steps);
+            found = s;
+            err = e;
+        }
+    }
+    if (err_out) *err_out = err;
+    free(a);
+    free(b);
+    free(keep);
+    return found;
 }

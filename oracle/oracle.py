@@ -26,7 +26,9 @@ BUILD = os.path.join(HERE, "_build")
 ORC_SO = os.path.join(BUILD, "liborc.so")
 REF_SO = os.path.join(HERE, "_ref", "libomni_ref.so")
 REF_STAGED = os.path.join(HERE, "_ref", "src", "ref_kernel_extract.cpp")
-REFERENCE_ROOT = os.environ.get("OMNI3D_REFERENCE_ROOT", "/root/reference")
+# The reference checkout is located only through this variable; without it the staged copy
+# under oracle/_ref/src (made by an earlier `build_ref.sh stage`) is used, if present.
+REFERENCE_ROOT = os.environ.get("OMNI3D_REFERENCE_ROOT") or None
 
 _f = C.c_float
 _d = C.c_double
@@ -54,10 +56,12 @@ def build_oracle(force: bool = False) -> str:
 def build_ref(force: bool = False) -> str | None:
     """Stage the reference sources (when the reference tree is present) and compile them.
 
-    Returns the library path, or None when neither the reference tree nor a staged copy
-    exists on this machine."""
+    The reference tree is found through OMNI3D_REFERENCE_ROOT only.  Returns the library
+    path, or None when neither the tree (variable unset or pointing elsewhere) nor a staged
+    copy exists on this machine."""
     script = os.path.join(HERE, "build_ref.sh")
-    have_tree = os.path.exists(os.path.join(REFERENCE_ROOT, "Omni3D_8.0", "Omni3D_8.0", "kernel.cu"))
+    have_tree = REFERENCE_ROOT is not None and os.path.exists(
+        os.path.join(REFERENCE_ROOT, "Omni3D_8.0", "Omni3D_8.0", "kernel.cu"))
     if have_tree and (force or not os.path.exists(REF_STAGED)):
         subprocess.check_call(["bash", script, "stage"], env=dict(os.environ, REF_ROOT=REFERENCE_ROOT),
                               stdout=subprocess.DEVNULL)
@@ -109,6 +113,14 @@ class Oracle:
             fn.argtypes = [C.POINTER(OrcProblem), _fp, _fp, _fp, _fp, _fp, _i, ptr, ptr, _i]
             fn = getattr(L, "orc_divide_" + s)
             fn.argtypes = [_l, ptr, ptr, ptr, _i]
+        L.orc_solve_cached_f64.restype = _l
+        L.orc_solve_cached_f64.argtypes = [C.POINTER(OrcProblem), _fp, _fp, _fp, _fp, _fp, _i, _d, _dp, _dp, _i,
+                                           _ip, _dp, _ip, _i, _dp]
+        L.orc_sor_steps_f64.argtypes = [_l, _l, _l, _dp, _dp, _l, _i]
+        L.orc_sor_converged_f64.restype = _l
+        L.orc_sor_converged_f64.argtypes = [_l, _l, _l, _dp, _d, _l, _dp, _i]
+        L.orc_sor_steps_to_f64.restype = _l
+        L.orc_sor_steps_to_f64.argtypes = [_l, _l, _l, _dp, _dp, _d, _l, _l, _i, _dp]
         L.orc_adjoint_f64.argtypes = [C.POINTER(OrcProblem), _i, _dp, _dp, _dp, _dp]
         L.orc_calindex.argtypes = [_l, _l, _l, _lp]
         L.orc_curl.argtypes = [_l, _l, _l, _f, _f, _f, _fp, _fp, _fp, _fp, _fp]
@@ -191,6 +203,35 @@ class Oracle:
             raise RuntimeError("oracle: %d lines hit the wrong-point branch" % err)
         return p, cnt
 
+    def solve_cached(self, dims, spacing, k, au, av, aw, p_init, niter, *, rho=1.0, ls=1.0, mode=0, thr=0.0,
+                     curl=None, tol=0.0, nthreads=1, cpu_twin=False, save_at=()):
+        """The FP64 reference iteration of ``solve(precision="f64")`` with the lines traced
+        and walked once (orc_solve_cached_f64): up to niter iterations, stopping early once
+        the mean-gauged relative change is below tol (tol > 0).  Returns (p, count,
+        iterations, last relative change), plus a dict {k: p after k iterations} when
+        save_at lists iteration counts."""
+        P, keep = self._problem(dims, spacing, rho, ls, thr, k, mode, cpu_twin)
+        V = dims[0] * dims[1] * dims[2]
+        f = lambda a: np.ascontiguousarray(np.asarray(a, np.float32).reshape(-1))
+        au, av, aw, p_init = f(au), f(av), f(aw), f(p_init)
+        curl = f(curl) if curl is not None else np.zeros(V, np.float32)
+        p = np.zeros(V, np.float64)
+        cnt = np.zeros(V, np.float64)
+        its = C.c_int(0)
+        rel = C.c_double(0.0)
+        at = np.ascontiguousarray(sorted(int(x) for x in save_at), dtype=np.int32)
+        saves = np.zeros((max(len(at), 1), V), np.float64)
+        err = self.lib.orc_solve_cached_f64(C.byref(P), _ptr(au, C.c_float), _ptr(av, C.c_float),
+                                            _ptr(aw, C.c_float), _ptr(curl, C.c_float), _ptr(p_init, C.c_float),
+                                            int(niter), float(tol), _ptr(p, C.c_double), _ptr(cnt, C.c_double),
+                                            int(nthreads), C.byref(its), C.byref(rel),
+                                            _ptr(at, C.c_int) if len(at) else None, len(at), _ptr(saves, C.c_double))
+        if err:
+            raise RuntimeError("oracle: %d lines hit the wrong-point branch" % err)
+        if len(at):
+            return p, cnt, its.value, rel.value, {int(a): saves[j] for j, a in enumerate(at)}
+        return p, cnt, its.value, rel.value
+
     def sweep(self, dims, spacing, k, au, av, aw, p, *, rho=1.0, ls=1.0, mode=0, thr=0.0, curl=None,
               precision="f32", nthreads=1, cpu_twin=False):
         """One sweep from p: returns (pn, count) without normalisation."""
@@ -246,6 +287,35 @@ class Oracle:
                                         _ptr(au, C.c_double), _ptr(av, C.c_double), _ptr(aw, C.c_double),
                                         float(pref), _ptr(out, C.c_double))
         return out
+
+    # -- the reference's CPU Poisson baseline (sor3D), restated for counting its steps ------
+    def sor_steps(self, dims, rhs, p, nsteps, nthreads=1):
+        """nsteps steps of sor3D's weighted Jacobi iteration (orc_sor_steps_f64) from p."""
+        X, Y, Z = dims
+        rhs = np.ascontiguousarray(np.asarray(rhs, np.float64).reshape(-1))
+        p = np.array(np.asarray(p, np.float64).reshape(-1), copy=True)
+        self.lib.orc_sor_steps_f64(X, Y, Z, _ptr(rhs, C.c_double), _ptr(p, C.c_double), int(nsteps), int(nthreads))
+        return p
+
+    def sor_converged(self, dims, rhs, tol=1e-12, max_iter=1000000, nthreads=1):
+        """Mean-free fixed point of sor3D's iteration by conjugate gradients; (p, CG iterations)."""
+        X, Y, Z = dims
+        rhs = np.ascontiguousarray(np.asarray(rhs, np.float64).reshape(-1))
+        p = np.zeros(X * Y * Z, np.float64)
+        its = self.lib.orc_sor_converged_f64(X, Y, Z, _ptr(rhs, C.c_double), float(tol), int(max_iter),
+                                             _ptr(p, C.c_double), int(nthreads))
+        return p, int(its)
+
+    def sor_steps_to(self, dims, rhs, ref, target=1e-3, max_steps=10 ** 8, check=64, nthreads=1):
+        """Even number of sor3D steps from zero after which the mean-gauged relative L2
+        distance from ref (mean-free) is at most target; (steps or -1, distance)."""
+        X, Y, Z = dims
+        rhs = np.ascontiguousarray(np.asarray(rhs, np.float64).reshape(-1))
+        ref = np.ascontiguousarray(np.asarray(ref, np.float64).reshape(-1))
+        err = C.c_double(0.0)
+        n = self.lib.orc_sor_steps_to_f64(X, Y, Z, _ptr(rhs, C.c_double), _ptr(ref, C.c_double), float(target),
+                                          int(max_steps), int(check), int(nthreads), C.byref(err))
+        return int(n), err.value
 
     def num_threads(self) -> int:
         return self.lib.orc_num_threads()
@@ -364,11 +434,23 @@ class RefLib:
                           _ptr(aw, C.c_float), _ptr(mask, C.c_float), _ptr(out, C.c_float))
         return out
 
-    def sor(self, dims, spacing, au, av, aw, niter, eps, *, rho=1.0):
+    def calrhs(self, dims, spacing, au, av, aw, *, rho=1.0):
+        """calRHS (with its output-dropping line 10 left out of the staged copy)."""
         X, Y, Z = dims
         g = lambda a: np.ascontiguousarray(np.asarray(a, np.float64).reshape(-1))
         au, av, aw = g(au), g(av), g(aw)
-        p = np.zeros(X * Y * Z, np.float64)
+        rhs = np.zeros(X * Y * Z, np.float64)
+        self.lib.ref_calrhs(X, Y, Z, spacing[0], spacing[1], spacing[2], rho, _ptr(au, C.c_double),
+                            _ptr(av, C.c_double), _ptr(aw, C.c_double), _ptr(rhs, C.c_double))
+        return rhs
+
+    def sor(self, dims, spacing, au, av, aw, niter, eps, *, rho=1.0, p0=None):
+        """sor3D from p0 (zero by default) for niter steps (run in pairs) or until its mean
+        |residual| is below eps."""
+        X, Y, Z = dims
+        g = lambda a: np.ascontiguousarray(np.asarray(a, np.float64).reshape(-1))
+        au, av, aw = g(au), g(av), g(aw)
+        p = np.zeros(X * Y * Z, np.float64) if p0 is None else np.array(g(p0), copy=True)
         self.lib.ref_sor(X, Y, Z, spacing[0], spacing[1], spacing[2], rho, _ptr(au, C.c_double),
                          _ptr(av, C.c_double), _ptr(aw, C.c_double), int(niter), float(eps), _ptr(p, C.c_double))
         return p
@@ -388,9 +470,13 @@ class RefLib:
 
 
 def load_reference_directions(level_file: str) -> np.ndarray | None:
-    """Direction file of the reference tree (only where the tree is present)."""
-    path = os.path.join(REFERENCE_ROOT, "Omni3D_8.0", "Executable", level_file)
-    if not os.path.exists(path):
+    """Direction file of the reference tree (OMNI3D_REFERENCE_ROOT), or of the staged copy
+    that build_ref.sh keeps beside the staged sources; None when neither is present."""
+    cands = [os.path.join(HERE, "_ref", "src", level_file)]
+    if REFERENCE_ROOT is not None:
+        cands.insert(0, os.path.join(REFERENCE_ROOT, "Omni3D_8.0", "Executable", level_file))
+    path = next((c for c in cands if os.path.exists(c)), None)
+    if path is None:
         return None
     rows = open(path).read().replace("\r", "").strip().split("\n")
     return np.array([[float(x) for x in r.split()] for r in rows[:-1]], np.float32)

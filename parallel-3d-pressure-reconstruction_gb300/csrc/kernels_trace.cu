@@ -25,19 +25,31 @@ constexpr long long kScanTile = (long long)kScanBlock * kScanItems;
 // share voxels and 32-byte sectors along the whole walk (a 32 x 1 row of the lattice
 // spreads over 32 lines' worth of width and shares far fewer), and a block of warps holds
 // the same patch of several nearly parallel directions, which walk through the same voxels
-// at the same time.  Tiles are visited in Z order within super-tiles of 32 x 32 tiles, the
-// super-tiles row by row, so the lines in flight at any moment (about a thousand tiles' worth)
-// cover a compact patch of the lattice plane rather than a long strip: at 512^3 their L2
-// footprints overlap more (final sweep 953 -> 854 ms; 256^3 unchanged).
-constexpr int kSuperLog2 = 5;  // super-tile side in tiles: 32
+// at the same time.  Tiles are visited in Z order within super-tiles of up to 32 x 32 tiles,
+// the super-tiles row by row, so the lines in flight at any moment (about a thousand tiles'
+// worth) cover a compact patch of the lattice plane rather than a long strip: at 512^3 their
+// L2 footprints overlap more (final sweep 953 -> 868 ms; 256^3 unchanged).  On lattices of
+// fewer than 32 tiles a side the super-tile shrinks to the smallest power of two that covers
+// the tiles, so that few of its slots are empty.
+constexpr int kSuperLog2Max = 5;  // super-tile side in tiles: at most 32
 struct CandOrder {
     long long ng2;    // lattice points per direction
     long long su;     // super-tiles across the lattice plane
-    long long nblk;   // tile slots per direction (super-tiles x 1024; slots outside the lattice are empty)
+    long long nblk;   // tile slots per direction (super-tiles x side^2; slots outside the lattice are empty)
     int tw_log2;      // log2 of the tile width (2, 3 or 4)
+    int s_log2;       // log2 of the super-tile side in tiles (0..kSuperLog2Max)
     int gsize;        // directions per group
     int nv;
 };
+
+// Super-tile side (log2) for a lattice of tu x tv tiles: the smallest power of two that
+// covers both, at most 2^kSuperLog2Max.
+inline int super_log2(long long tu, long long tv)
+{
+    int s = 0;
+    while (s < kSuperLog2Max && (1LL << s) < std::max(tu, tv)) s++;
+    return s;
+}
 
 // Even bits of x, packed (the column of a Z-order index).
 __device__ __forceinline__ uint32_t z_compact(uint32_t x)
@@ -61,10 +73,10 @@ __device__ __forceinline__ bool trace_candidate(const Grid &g, const DirEntry *d
     long long blk = r / per_block;
     r -= blk * per_block;
     int d = (int)(grp * co.gsize + r / 32);
-    const long long sup = blk >> (2 * kSuperLog2);
-    const uint32_t z = (uint32_t)(blk & ((1LL << (2 * kSuperLog2)) - 1));
-    const long long tx = (sup % co.su) * (1LL << kSuperLog2) + z_compact(z);
-    const long long ty = (sup / co.su) * (1LL << kSuperLog2) + z_compact(z >> 1);
+    const long long sup = blk >> (2 * co.s_log2);
+    const uint32_t z = (uint32_t)(blk & ((1LL << (2 * co.s_log2)) - 1));
+    const long long tx = (sup % co.su) * (1LL << co.s_log2) + z_compact(z);
+    const long long ty = (sup / co.su) * (1LL << co.s_log2) + z_compact(z >> 1);
     const long long u = tx * (1LL << co.tw_log2) + (r & ((1LL << co.tw_log2) - 1));
     const long long v = ty * (32LL >> co.tw_log2) + ((r & 31) >> co.tw_log2);
     *dir = d;
@@ -331,6 +343,21 @@ cudaError_t exclusive_scan_u64(const unsigned long long *in, unsigned long long 
         }                                                                 \
     } while (0)
 
+namespace {
+// A device temporary freed when the guard goes out of scope (any return path).
+struct TmpBuf {
+    void *p = nullptr;
+    template <typename T>
+    cudaError_t alloc(T **out, size_t elems)
+    {
+        cudaError_t e = cudaMalloc(&p, sizeof(T) * std::max<size_t>(elems, 1));
+        *out = e == cudaSuccess ? static_cast<T *>(p) : nullptr;
+        return e;
+    }
+    ~TmpBuf() { cudaFree(p); }
+};
+}  // namespace
+
 cudaError_t ensure_lines_through(Geometry *g, cudaStream_t st)
 {
     if (g->d_lines_through) return cudaSuccess;
@@ -368,7 +395,9 @@ cudaError_t build_geometry(Geometry *g, cudaStream_t st, std::string *err)
     co.ng2 = (long long)G.ng * G.ng;
     co.tw_log2 = g->tile_width == 4 ? 2 : (g->tile_width == 16 ? 4 : 3);
     const long long tw = 1LL << co.tw_log2, th = 32LL >> co.tw_log2;
-    const long long tu = (G.ng + tw - 1) / tw, tv = (G.ng + th - 1) / th, side = 1LL << kSuperLog2;
+    const long long tu = (G.ng + tw - 1) / tw, tv = (G.ng + th - 1) / th;
+    co.s_log2 = super_log2(tu, tv);
+    const long long side = 1LL << co.s_log2;
     co.su = (tu + side - 1) / side;
     co.nblk = co.su * ((tv + side - 1) / side) * side * side;
     co.gsize = std::max(1, std::min(g->dir_group, g->nv));
@@ -380,9 +409,11 @@ cudaError_t build_geometry(Geometry *g, cudaStream_t st, std::string *err)
         if (err) *err = "too many lattice candidates";
         return cudaErrorInvalidValue;
     }
+    // temporaries of the build, freed on every exit
+    TmpBuf tb_blk, tb_tmp, tb_gw, tb_gtmp;
     uint32_t *blk = nullptr, *tmp = nullptr;
-    OM_TRY(cudaMalloc(&blk, sizeof(uint32_t) * (size_t)(2 * nblk + 1)));
-    OM_TRY(cudaMalloc(&tmp, sizeof(uint32_t) * scan_tmp_elems(nblk)));
+    OM_TRY(tb_blk.alloc(&blk, (size_t)(2 * nblk + 1)));
+    OM_TRY(tb_tmp.alloc(&tmp, scan_tmp_elems(nblk)));
     uint32_t *blk_off = blk + nblk;
     k_trace_count<<<(unsigned)nblk, kTraceBlock, 0, st>>>(G, g->d_dirs, ncand, co, blk);
     OM_COUNT_LAUNCH();
@@ -394,8 +425,6 @@ cudaError_t build_geometry(Geometry *g, cudaStream_t st, std::string *err)
     g->n_lines = total;
     g->n_groups = (total + 31) / 32;
     if (total == 0) {
-        cudaFree(blk);
-        cudaFree(tmp);
         g->n_words = 0;
         g->n_units = 0;
         return cudaSuccess;
@@ -406,14 +435,12 @@ cudaError_t build_geometry(Geometry *g, cudaStream_t st, std::string *err)
                                                          g->d_off);
     OM_COUNT_LAUNCH();
     OM_TRY(cudaGetLastError());
-    cudaFree(blk);
-    cudaFree(tmp);
 
     // words per group -> prefix offsets
     uint32_t *gw = nullptr, *gtmp = nullptr;
-    OM_TRY(cudaMalloc(&gw, sizeof(uint32_t) * (size_t)g->n_groups));
+    OM_TRY(tb_gw.alloc(&gw, (size_t)g->n_groups));
     OM_TRY(cudaMalloc(&g->d_gbase, sizeof(uint32_t) * (size_t)(g->n_groups + 1)));
-    OM_TRY(cudaMalloc(&gtmp, sizeof(uint32_t) * scan_tmp_elems(g->n_groups)));
+    OM_TRY(tb_gtmp.alloc(&gtmp, scan_tmp_elems(g->n_groups)));
     long long nthr = g->n_groups * 32;
     k_group_words<<<(unsigned)((nthr + 255) / 256), 256, 0, st>>>(g->d_lines, g->n_lines, g->n_groups, gw);
     OM_COUNT_LAUNCH();
@@ -423,8 +450,6 @@ cudaError_t build_geometry(Geometry *g, cudaStream_t st, std::string *err)
     OM_TRY(cudaMemcpyAsync(&words_per_lane_total, g->d_gbase + g->n_groups, sizeof(uint32_t),
                            cudaMemcpyDeviceToHost, st));
     OM_TRY(cudaStreamSynchronize(st));
-    cudaFree(gw);
-    cudaFree(gtmp);
     g->n_words = 32LL * words_per_lane_total;
     OM_TRY(cudaMalloc(&g->d_desc, sizeof(uint32_t) * (size_t)std::max(g->n_words, 1LL)));
 

@@ -2,18 +2,18 @@
 //
 // omni3d_sweep packs the gradient into a float4 field and accumulates (pn, count) in a
 // float2 volume, both in device buffers it allocates on first use.  Some callers cannot
-// allocate at that point: a program that runs its solver step inside a CUDA-graph capture
-// (cudaMalloc is not allowed while a stream is capturing), a host framework that owns all
-// device memory through its own pool and forbids driver allocations in its step, or a
-// real-time pipeline that cannot afford cudaMalloc's implicit device synchronisation.
-// For them this variant keeps both scratch volumes in file-scope device arrays sized for
-// at most OMNI3D_NOALLOC_MAX_VOXELS voxels (64^3: 4 MiB of field + 2 MiB of accumulator,
-// held by every GPU that loads the library until the process exits).
+// allocate at that point: a host framework that owns all device memory through its own
+// pool and forbids driver allocations inside its step, a plugin loaded into an application
+// whose memory budget is fixed up front, or a real-time pipeline that cannot afford
+// cudaMalloc's implicit device synchronisation in its loop.  For them this variant keeps
+// both scratch volumes in file-scope device arrays sized for at most
+// OMNI3D_NOALLOC_MAX_VOXELS voxels (64^3: 4 MiB of field + 2 MiB of accumulator, held by
+// every GPU that loads the library until the process exits).
 //
 // The host code below never passes the arrays' names to a kernel: in host code those
 // names are host-side stand-ins, not device addresses.  The first call on a device looks
 // up their device addresses with cudaGetSymbolAddress (with that device current) and keeps
-// them for later calls.
+// them for later calls; the caller's current device is restored before the call returns.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -52,6 +52,25 @@ cudaError_t scratch_addresses(int device, float4 **field, float2 **accum)
     return cudaSuccess;
 }
 
+// Makes `device` current for the guard's lifetime and restores the caller's device after.
+struct DeviceScope {
+    int prev = -1;
+    cudaError_t enter(int device)
+    {
+        cudaError_t e = cudaGetDevice(&prev);
+        if (e != cudaSuccess) {
+            prev = -1;
+            return e;
+        }
+        return prev == device ? cudaSuccess : cudaSetDevice(device);
+    }
+    ~DeviceScope()
+    {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
 }  // namespace
 
 namespace omni3d {
@@ -86,7 +105,8 @@ extern "C" int omni3d_sweep_noalloc(omni3d_ctx *ctx, const float *ax, const floa
                                           " voxels exceed its static scratch of OMNI3D_NOALLOC_MAX_VOXELS = " +
                                           std::to_string(kMaxVoxels));
     if (P->device < 0 || P->device >= kMaxDevices) return fail(OMNI3D_ERR_RANGE, "device ordinal too large");
-    cudaError_t e = cudaSetDevice(P->device);
+    DeviceScope scope;
+    cudaError_t e = scope.enter(P->device);
     float4 *field = nullptr;
     float2 *accum = nullptr;
     if (e == cudaSuccess) e = scratch_addresses(P->device, &field, &accum);

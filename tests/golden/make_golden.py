@@ -25,6 +25,9 @@ outputs of the reference functions:
   cputwin  10x10x10 grid, 42 directions, 2 iterations of the reference's own CPU loop
            omni3dparallellinesESInnerCPU + devidecountInnerCPU (no pole guard, count > 1)
   curl     the curl indicator calCurlofMaterialAccCPU of the select case
+  sor      13x11x9 grid: calRHS.cpp's right-hand side (FP64; its output-dropping line 10 left
+           out) and sor3D.cpp's iterate after 2 and 10 steps from zero (weighted Jacobi,
+           omega 0.8, the reference's CPU Poisson baseline)
 Directions are the 42-vertex icosphere (the vertex set of GridIcosahedronDivide2.dat).
 """
 import os
@@ -125,6 +128,15 @@ def main():
     out.update({"cputwin_dims": np.array(d), "cputwin_spacing": np.array(f["spacing"], np.float32),
                 "cputwin_ax": f["ax"].reshape(-1), "cputwin_ay": f["ay"].reshape(-1),
                 "cputwin_az": f["az"].reshape(-1), "cputwin_p": p, "cputwin_count": c})
+    # the CPU Poisson baseline
+    d = (13, 11, 9)
+    f = field(d, 12)
+    rhs = R.calrhs(d, f["spacing"], f["ax"], f["ay"], f["az"])
+    out.update({"sor_dims": np.array(d), "sor_spacing": np.array(f["spacing"], np.float64),
+                "sor_ax": f["ax"].reshape(-1), "sor_ay": f["ay"].reshape(-1), "sor_az": f["az"].reshape(-1),
+                "sor_rhs": rhs})
+    for k in (2, 10):
+        out["sor_p%d" % k] = R.sor(d, f["spacing"], f["ax"], f["ay"], f["az"], k, 0.0)
     np.savez_compressed(os.path.join(HERE, "reference_small.npz"), **out)
     print("wrote", os.path.join(HERE, "reference_small.npz"))
 

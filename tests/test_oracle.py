@@ -217,3 +217,66 @@ def test_oracle_converges_toward_analytic(orc):
                          precision="f64")
         errs.append(synthetic.relative_l2(p, f["p_true"]))
     assert errs[1] < errs[0] and errs[1] < 0.1
+
+
+@pytest.mark.parametrize("case,mode", [("plain", 0), ("select", 1), ("weighted", 2), ("variants", 4),
+                                       ("variants", 6)])
+def test_cached_fp64_solve_equals_fp64_solve(orc, gold, case, mode):
+    """The FP64 solve with the lines traced once (the fixed-point oracle of the full-size
+    parity tests) is the re-tracing FP64 solve up to the order of its sums, and it stops at
+    the first iteration whose gauged relative change is below tol."""
+    g = gold
+    d = _dims(g, case)
+    ax, ay, az = g[case + "_ax"], g[case + "_ay"], g[case + "_az"]
+    curl = g[case + "_curl"] if case + "_curl" in g else None
+    thr = float(g[case + "_thr"]) if case + "_thr" in g else 0.0
+    p0 = g[case + "_p0"]
+    a, ca = orc.solve(d, _sp(g, case), g["dirs"], ax, ay, az, p0, 3, mode=mode, thr=thr, curl=curl, precision="f64")
+    b, cb, its, rel, saved = orc.solve_cached(d, _sp(g, case), g["dirs"], ax, ay, az, p0, 3, mode=mode, thr=thr,
+                                              curl=curl, nthreads=3, save_at=(1, 3))
+    assert its == 3
+    assert np.abs(a - b).max() <= 1e-12 * np.abs(a).max()
+    assert np.abs(ca - cb).max() <= 1e-12 * np.abs(ca).max()
+    np.testing.assert_array_equal(saved[3], b)
+    a1, _ = orc.solve(d, _sp(g, case), g["dirs"], ax, ay, az, p0, 1, mode=mode, thr=thr, curl=curl, precision="f64")
+    assert np.abs(a1 - saved[1]).max() <= 1e-12 * np.abs(a1).max()
+    _, _, its_tol, rel_tol = orc.solve_cached(d, _sp(g, case), g["dirs"], ax, ay, az, p0, 200, mode=mode, thr=thr,
+                                              curl=curl, tol=1e-3)
+    assert rel_tol < 1e-3 and its_tol < 200
+
+
+def test_golden_sor_restatement_bit_exact(orc, gold):
+    """The restated sor3D iteration (used to count the reference baseline's steps at sizes
+    where the reference itself would run for hours) equals sor3D bit for bit, from the
+    golden right-hand side of calRHS."""
+    g = gold
+    d = _dims(g, "sor")
+    rhs = g["sor_rhs"]
+    assert np.count_nonzero(rhs) > 0.9 * rhs.size  # calRHS returns its output (line 10 left out)
+    for k in (2, 10):
+        p = orc.sor_steps(d, rhs, np.zeros(rhs.size), k, nthreads=2)
+        np.testing.assert_array_equal(p.view(np.uint64), np.ascontiguousarray(g["sor_p%d" % k]).view(np.uint64))
+
+
+def test_sor_reference_calrhs_and_residual(orc, reflib):
+    """The staged calRHS returns a nonzero right-hand side, and sor3D moves toward its fixed
+    point: the distance from the conjugate-gradient solution of the same discrete problem
+    falls with the step count, and the step count the restatement reports is where the
+    reference code itself first meets 1e-3."""
+    from omni3d import synthetic
+
+    f = synthetic.blobs(n=16, count=3, sigma_range=(1.0, 3.0), noise=0.05, seed=3, spacing=1e-3 * 16)
+    d = f["dims"]
+    rhs = reflib.calrhs(d, f["spacing"], f["ax"], f["ay"], f["az"])
+    assert np.count_nonzero(rhs) > 0.9 * rhs.size
+    conv, cg = orc.sor_converged(d, rhs, tol=1e-13)
+    assert cg > 10
+    errs = [synthetic.relative_l2(reflib.sor(d, f["spacing"], f["ax"], f["ay"], f["az"], k, 0.0), conv, gauge="mean")
+            for k in (10, 100, 400)]
+    assert errs[0] > errs[1] > errs[2]
+    n, err = orc.sor_steps_to(d, rhs, conv, 1e-3, check=8)
+    assert n > 0 and n % 2 == 0 and err <= 1e-3
+    at = synthetic.relative_l2(reflib.sor(d, f["spacing"], f["ax"], f["ay"], f["az"], n, 0.0), conv, gauge="mean")
+    short = synthetic.relative_l2(reflib.sor(d, f["spacing"], f["ax"], f["ay"], f["az"], n - 2, 0.0), conv,
+                                  gauge="mean")
+    assert at <= 1e-3 < short
