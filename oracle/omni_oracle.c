@@ -766,12 +766,19 @@ static void clist_push(orc_clist *L, const int in[3], const int out[3], const si
     L->ns += n;
 }
 
-long orc_solve_cached_f64(const orc_problem *P, const float *au, const float *av, const float *aw,
-                          const float *curl, const float *p_init, int niter, double tol, double *p,
-                          double *cnt, int nthreads, int *iters_out, double *rel_out, const int *save_at,
-                          int nsave, double *saves)
+/* The traced lines of one problem, kept between sweeps (orc_cache_*). */
+typedef struct {
+    orc_problem P;
+    orc_cline *lines;
+    signed char *steps;
+    long nl, ns, errors;
+    long *bound;     /* nthreads + 1 line offsets of about equal work */
+    int nthreads;
+    double *pp;      /* per-thread private accumulators, 2 V each */
+} orc_cache;
+
+void *orc_cache_build(const orc_problem *P, const float *curl, int nthreads)
 {
-    const long V = P->X * P->Y * P->Z;
     const int ng = orc_nogrid(P->X, P->Y, P->Z, P->ls, P->geom_cpu_twin);
     const int rule = orc_mode_walk_rule(P->mode);
     const long cap = max_path(P->X, P->Y, P->Z);
@@ -799,21 +806,23 @@ long orc_solve_cached_f64(const orc_problem *P, const float *au, const float *av
         }
         free(ax);
     }
+    orc_cache *h = (orc_cache *)calloc(1, sizeof(orc_cache));
+    h->P = *P;
+    h->nthreads = nthreads;
     /* concatenate in direction order */
-    long nl = 0, ns = 0, errors = 0;
     for (int d = 0; d < P->nv; d++) {
-        nl += per_dir[d].nl;
-        ns += per_dir[d].ns;
-        errors += per_dir[d].errors;
+        h->nl += per_dir[d].nl;
+        h->ns += per_dir[d].ns;
+        h->errors += per_dir[d].errors;
     }
-    orc_cline *lines = (orc_cline *)malloc(sizeof(orc_cline) * (size_t)(nl > 0 ? nl : 1));
-    signed char *steps = (signed char *)malloc((size_t)(ns > 0 ? ns : 1));
+    h->lines = (orc_cline *)malloc(sizeof(orc_cline) * (size_t)(h->nl > 0 ? h->nl : 1));
+    h->steps = (signed char *)malloc((size_t)(h->ns > 0 ? h->ns : 1));
     for (long d = 0, l0 = 0, s0 = 0; d < P->nv; d++) {
         for (long i = 0; i < per_dir[d].nl; i++) {
-            lines[l0 + i] = per_dir[d].lines[i];
-            lines[l0 + i].off += s0;
+            h->lines[l0 + i] = per_dir[d].lines[i];
+            h->lines[l0 + i].off += s0;
         }
-        memcpy(steps + s0, per_dir[d].steps, (size_t)per_dir[d].ns);
+        memcpy(h->steps + s0, per_dir[d].steps, (size_t)per_dir[d].ns);
         l0 += per_dir[d].nl;
         s0 += per_dir[d].ns;
         free(per_dir[d].lines);
@@ -821,48 +830,83 @@ long orc_solve_cached_f64(const orc_problem *P, const float *au, const float *av
     }
     free(per_dir);
     /* thread blocks of about equal work (steps + 1 per line) */
-    long *bound = (long *)malloc(sizeof(long) * (size_t)(nthreads + 1));
-    {
-        long total = ns + nl, acc = 0, li = 0;
-        bound[0] = 0;
-        for (int t = 1; t < nthreads; t++) {
-            long target = total * t / nthreads;
-            while (li < nl && acc < target) acc += lines[li++].n + 1;
-            bound[t] = li;
-        }
-        bound[nthreads] = nl;
+    h->bound = (long *)malloc(sizeof(long) * (size_t)(nthreads + 1));
+    long total = h->ns + h->nl, acc = 0, li = 0;
+    h->bound[0] = 0;
+    for (int t = 1; t < nthreads; t++) {
+        long target = total * t / nthreads;
+        while (li < h->nl && acc < target) acc += h->lines[li++].n + 1;
+        h->bound[t] = li;
     }
+    h->bound[nthreads] = h->nl;
+    const long V = P->X * P->Y * P->Z;
+    h->pp = (double *)malloc(sizeof(double) * (size_t)V * 2 * (size_t)nthreads);
+    return h;
+}
+
+long orc_cache_errors(const void *hv) { return ((const orc_cache *)hv)->errors; }
+
+void orc_cache_free(void *hv)
+{
+    orc_cache *h = (orc_cache *)hv;
+    if (!h) return;
+    free(h->lines);
+    free(h->steps);
+    free(h->bound);
+    free(h->pp);
+    free(h);
+}
+
+/* One FP64 sweep of the traced lines from p: pn += contributions, cnt += weights (the
+ * threads' private sums added in block order). */
+void orc_cache_sweep_f64(void *hv, const float *au, const float *av, const float *aw, const float *curl,
+                         const double *p, double *pn, double *cnt)
+{
+    orc_cache *h = (orc_cache *)hv;
+    const orc_problem *P = &h->P;
+    const long V = P->X * P->Y * P->Z;
+    const int nthreads = h->nthreads;
     orc_grid g = {P->X, P->Y, P->Z, P->dx, P->dy, P->dz, P->rho, P->thr};
+    _Pragma("omp parallel for num_threads(nthreads) schedule(static, 1)")
+    for (int t = 0; t < nthreads; t++) {
+        double *mypn = h->pp + (size_t)V * 2 * t, *mycnt = mypn + V;
+        memset(mypn, 0, sizeof(double) * 2 * (size_t)V);
+        for (long i = h->bound[t]; i < h->bound[t + 1]; i++) {
+            const orc_cline *c = &h->lines[i];
+            const signed char *ax = h->steps + c->off;
+            if (P->mode == 0 || P->mode == 5)
+                line_plain_f64(&g, c->in, c->out, ax, c->n, au, av, aw, p, mypn, mycnt, P->mode == 0);
+            else if (P->mode == 2 || P->mode == 3)
+                line_weighted_f64(&g, c->in, c->out, ax, c->n, au, av, aw, curl, p, mypn, mycnt);
+            else if (P->mode == 6)
+                line_weighted_mc_f64(&g, c->in, c->out, ax, c->n, au, av, aw, curl, p, mypn, mycnt);
+            else
+                line_select_f64(&g, c->in, c->out, ax, c->n, au, av, aw, curl, p, mypn, mycnt);
+        }
+    }
+    for (int t = 0; t < nthreads; t++) {
+        const double *mypn = h->pp + (size_t)V * 2 * t, *mycnt = mypn + V;
+        for (long v = 0; v < V; v++) { pn[v] += mypn[v]; cnt[v] += mycnt[v]; }
+    }
+}
+
+long orc_solve_cached_f64(const orc_problem *P, const float *au, const float *av, const float *aw,
+                          const float *curl, const float *p_init, int niter, double tol, double *p,
+                          double *cnt, int nthreads, int *iters_out, double *rel_out, const int *save_at,
+                          int nsave, double *saves)
+{
+    const long V = P->X * P->Y * P->Z;
+    void *h = orc_cache_build(P, curl, nthreads);
+    const long errors = orc_cache_errors(h);
     double *pn = (double *)malloc(sizeof(double) * (size_t)V);
-    double *pp = (double *)malloc(sizeof(double) * (size_t)V * 2 * (size_t)nthreads);
     double *pold = (double *)malloc(sizeof(double) * (size_t)V);
     for (long v = 0; v < V; v++) { p[v] = (double)p_init[v]; pn[v] = (double)p_init[v]; cnt[v] = 0; }
     int it = 0;
     double rel = 0.0;
     for (it = 0; it < niter;) {
         memcpy(pold, p, sizeof(double) * (size_t)V);
-        _Pragma("omp parallel for num_threads(nthreads) schedule(static, 1)")
-        for (int t = 0; t < nthreads; t++) {
-            double *mypn = pp + (size_t)V * 2 * t, *mycnt = mypn + V;
-            memset(mypn, 0, sizeof(double) * 2 * (size_t)V);
-            for (long i = bound[t]; i < bound[t + 1]; i++) {
-                const orc_cline *c = &lines[i];
-                const signed char *ax = steps + c->off;
-                if (P->mode == 0 || P->mode == 5)
-                    line_plain_f64(&g, c->in, c->out, ax, c->n, au, av, aw, p, mypn, mycnt, P->mode == 0);
-                else if (P->mode == 2 || P->mode == 3)
-                    line_weighted_f64(&g, c->in, c->out, ax, c->n, au, av, aw, curl, p, mypn, mycnt);
-                else if (P->mode == 6)
-                    line_weighted_mc_f64(&g, c->in, c->out, ax, c->n, au, av, aw, curl, p, mypn, mycnt);
-                else
-                    line_select_f64(&g, c->in, c->out, ax, c->n, au, av, aw, curl, p, mypn, mycnt);
-            }
-        }
         memset(cnt, 0, sizeof(double) * (size_t)V);
-        for (int t = 0; t < nthreads; t++) {
-            const double *mypn = pp + (size_t)V * 2 * t, *mycnt = mypn + V;
-            for (long v = 0; v < V; v++) { pn[v] += mypn[v]; cnt[v] += mycnt[v]; }
-        }
+        orc_cache_sweep_f64(h, au, av, aw, curl, p, pn, cnt);
         orc_divide_f64(V, p, pn, cnt, 1);
         it++;
         for (int j = 0; j < nsave; j++)
@@ -883,11 +927,8 @@ long orc_solve_cached_f64(const orc_problem *P, const float *au, const float *av
     }
     if (iters_out) *iters_out = it;
     if (rel_out) *rel_out = rel;
-    free(lines);
-    free(steps);
-    free(bound);
+    orc_cache_free(h);
     free(pn);
-    free(pp);
     free(pold);
     return errors;
 }

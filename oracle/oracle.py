@@ -121,6 +121,12 @@ class Oracle:
         L.orc_sor_converged_f64.argtypes = [_l, _l, _l, _dp, _d, _l, _dp, _i]
         L.orc_sor_steps_to_f64.restype = _l
         L.orc_sor_steps_to_f64.argtypes = [_l, _l, _l, _dp, _dp, _d, _l, _l, _i, _dp]
+        L.orc_cache_build.restype = C.c_void_p
+        L.orc_cache_build.argtypes = [C.POINTER(OrcProblem), _fp, _i]
+        L.orc_cache_errors.restype = _l
+        L.orc_cache_errors.argtypes = [C.c_void_p]
+        L.orc_cache_free.argtypes = [C.c_void_p]
+        L.orc_cache_sweep_f64.argtypes = [C.c_void_p, _fp, _fp, _fp, _fp, _dp, _dp, _dp]
         L.orc_adjoint_f64.argtypes = [C.POINTER(OrcProblem), _i, _dp, _dp, _dp, _dp]
         L.orc_calindex.argtypes = [_l, _l, _l, _lp]
         L.orc_curl.argtypes = [_l, _l, _l, _f, _f, _f, _fp, _fp, _fp, _fp, _fp]
@@ -231,6 +237,80 @@ class Oracle:
         if len(at):
             return p, cnt, its.value, rel.value, {int(a): saves[j] for j, a in enumerate(at)}
         return p, cnt, its.value, rel.value
+
+    def fixed_point(self, dims, spacing, k, au, av, aw, *, rho=1.0, ls=1.0, mode=0, thr=0.0, curl=None, tol=1e-10,
+                    max_iter=500, memory=6, nthreads=1, p_init=None):
+        """The fixed point of the FP64 reference iteration, mean-gauged over the voxels with
+        count > 0, found by Anderson acceleration (type II, `memory` differences) of the map
+        G(p) = (sweep of p) / count where count > 0, else p_init, with the mean over those
+        voxels removed.  G is one iteration of ``solve(precision="f64")`` (lines traced once,
+        orc_cache_*); the seeding of the reference's first sweep changes only the transient.
+        Stops when ||G(p) - p|| <= tol ||G(p)|| over those voxels.  Returns (p, count,
+        G evaluations, final residual).  The fixed point is unique (up to the removed
+        constant) when the iteration couples all receiving voxels, e.g. the selected method
+        with a threshold above every curl; where it splits them into islands, each island
+        keeps a free constant that the transient of the plain iteration sets, and
+        solve_cached is the reference."""
+        P, keep = self._problem(dims, spacing, rho, ls, thr, k, mode, False)
+        V = dims[0] * dims[1] * dims[2]
+        f = lambda a: np.ascontiguousarray(np.asarray(a, np.float32).reshape(-1))
+        au, av, aw = f(au), f(av), f(aw)
+        curl = f(curl) if curl is not None else np.zeros(V, np.float32)
+        p_init = np.zeros(V, np.float64) if p_init is None else np.asarray(p_init, np.float64).reshape(-1)
+        h = self.lib.orc_cache_build(C.byref(P), _ptr(curl, C.c_float), int(nthreads))
+        try:
+            if self.lib.orc_cache_errors(h):
+                raise RuntimeError("oracle: lines hit the wrong-point branch")
+            pn = np.zeros(V, np.float64)
+            cnt = np.zeros(V, np.float64)
+            full = p_init.copy()
+
+            def sweep_into(vol):
+                pn.fill(0.0)
+                cnt.fill(0.0)
+                self.lib.orc_cache_sweep_f64(h, _ptr(au, C.c_float), _ptr(av, C.c_float), _ptr(aw, C.c_float),
+                                             _ptr(curl, C.c_float), _ptr(vol, C.c_double), _ptr(pn, C.c_double),
+                                             _ptr(cnt, C.c_double))
+
+            def G(x):
+                full[sel] = x
+                sweep_into(full)
+                y = pn[sel]
+                y /= cnt[sel]
+                y -= y.mean()
+                return y
+
+            # the voxels that receive contributions depend on the field only: one sweep finds them
+            sweep_into(full)
+            sel = cnt > 0
+            x = np.zeros(int(sel.sum()), np.float64)
+            g = G(x)
+            fx = g - x
+            evals, dF, dG = 1, [], []
+            res = np.linalg.norm(fx) / max(np.linalg.norm(g), 1e-300)
+            while res > tol and evals < max_iter:
+                xn = g.copy()
+                if dF:  # least squares min ||fx - dF gamma|| by its normal equations (m x m)
+                    M = np.array([[np.dot(a, b) for b in dF] for a in dF])
+                    r = np.array([np.dot(a, fx) for a in dF])
+                    gamma = np.linalg.lstsq(M, r, rcond=None)[0]
+                    for gm, d in zip(gamma, dG):
+                        xn -= gm * d
+                gn = G(xn)
+                fn = gn - xn
+                evals += 1
+                dF.append(fn - fx)
+                dG.append(gn - g)
+                if len(dF) > memory:
+                    dF.pop(0)
+                    dG.pop(0)
+                x, g, fx = xn, gn, fn
+                res = np.linalg.norm(fx) / max(np.linalg.norm(g), 1e-300)
+            out = p_init.copy()
+            out[sel] = g
+            return out, cnt.copy(), evals, float(res)
+        finally:
+            self.lib.orc_cache_free(h)
 
     def sweep(self, dims, spacing, k, au, av, aw, p, *, rho=1.0, ls=1.0, mode=0, thr=0.0, curl=None,
               precision="f32", nthreads=1, cpu_twin=False):

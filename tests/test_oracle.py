@@ -280,3 +280,23 @@ def test_sor_reference_calrhs_and_residual(orc, reflib):
     short = synthetic.relative_l2(reflib.sor(d, f["spacing"], f["ax"], f["ay"], f["az"], n - 2, 0.0), conv,
                                   gauge="mean")
     assert at <= 1e-3 < short
+
+
+def test_anderson_fixed_point_is_the_iteration_limit(orc, gold):
+    """The accelerated FP64 fixed point (the bench's FP64 reference) is where the plain FP64
+    iteration goes: the same voxels, the same mean-gauged field.  As in the bench, the
+    threshold lies above every curl, so segments split only at the mask and the iteration
+    couples every receiving voxel (one free constant).  (A threshold that cuts the domain
+    into islands leaves one free constant per island, set by the transient, and the
+    accelerated limit need not equal the plain iteration's.)"""
+    from omni3d import synthetic
+
+    g = gold
+    d = _dims(g, "select")
+    args = (d, _sp(g, "select"), g["dirs"], g["select_ax"], g["select_ay"], g["select_az"])
+    kw = dict(mode=1, thr=float(np.finfo(np.float32).max), curl=g["select_curl"])
+    p, c, its, rel = orc.solve_cached(*args, np.zeros(int(np.prod(d)), np.float32), 2000, tol=1e-12, **kw)
+    q, cq, ev, res = orc.fixed_point(*args, tol=1e-12, **kw)
+    assert rel < 1e-12 and res < 1e-12 and ev < its
+    np.testing.assert_array_equal(c > 0, cq > 0)
+    assert synthetic.relative_l2(q, p, gauge="mean", weights=c > 0) < 1e-9
