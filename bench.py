@@ -50,8 +50,9 @@ for _p in (PKG, os.path.join(REPO, "oracle")):
 METRIC = "time-to-solution at 256³ to 1e-3 rel L2 vs FP64; voxel·dir updates/s; HBM GB/s"
 FLT_MAX = float(np.finfo(np.float32).max)
 # bytes per voxel-direction update of the full sweep (selected method): the gradient
-# component read (3 x 4 B), the curl read (4 B) and the accumulator read + write (8 B)
-ALG_BYTES_PER_UNIT = {"f32": 24.0, "bf16": 18.0}
+# component read (3 x 4 B), the curl read (4 B) and the accumulator read + write (8 B); with
+# BF16 storage one 8-byte record holds the three components and the curl
+ALG_BYTES_PER_UNIT = {"f32": 24.0, "bf16": 16.0}
 PROFILE_SUMMARY = os.path.join(REPO, "profiles", "k_sweep_select_k_anchor_select_blobs192.md")
 
 

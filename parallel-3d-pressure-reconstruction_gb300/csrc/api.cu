@@ -191,6 +191,11 @@ int check_params(const omni3d_params *p, std::string *why)
         return OMNI3D_ERR_ARG;
     }
     if (!(p->tol >= 0.0)) { *why = "tol must be >= 0"; return OMNI3D_ERR_ARG; }
+    if (p->grad_storage == OMNI3D_GRAD_BF16 && method_accum(p->method) == kAccSelect && p->threshold > 0.0f &&
+        p->threshold < 1.17549435e-38f) {
+        *why = "BF16 storage needs a threshold of 0 or at least 1.2e-38 (FP32's normal range)";
+        return OMNI3D_ERR_ARG;
+    }
     if (p->anchor_max_links < 0) { *why = "anchor_max_links must be >= 0"; return OMNI3D_ERR_ARG; }
     if (p->engine < OMNI3D_ENGINE_AUTO || p->engine > OMNI3D_ENGINE_BRICKS) { *why = "unknown engine"; return OMNI3D_ERR_ARG; }
     if (p->sweep_fp64 != 0 && p->sweep_fp64 != 1) { *why = "sweep_fp64 must be 0 or 1"; return OMNI3D_ERR_ARG; }
@@ -253,12 +258,17 @@ int prepare_field(omni3d_ctx *ctx, const float *ax, const float *ay, const float
     const bool bf16 = ctx->prm.grad_storage == OMNI3D_GRAD_BF16;
     CK(ctx, ctx->f32.ensure(sizeof(float4) * (size_t)V));
     F->f32 = ctx->f32.as<float4>();
+    float *rounded = nullptr;  // BF16 storage: every curl decision sees the rounded curl
     if (bf16) {
         CK(ctx, ctx->b16.ensure(sizeof(uint2) * (size_t)V));
         F->bf16 = ctx->b16.as<uint2>();
+        if (dcurl) {
+            CK(ctx, ctx->curl.ensure(sizeof(float) * (size_t)V));
+            rounded = ctx->curl.as<float>();
+        }
     }
-    F->curl = const_cast<float *>(dcurl);
-    CK(ctx, pack_field(g, dax, day, daz, dcurl, F, bf16, ctx->st));
+    F->curl = rounded ? rounded : const_cast<float *>(dcurl);
+    CK(ctx, pack_field(g, dax, day, daz, dcurl, F, bf16, ctx->st, rounded));
     return OMNI3D_OK;
 }
 
@@ -543,7 +553,17 @@ int omni3d_create(const omni3d_params *params, omni3d_ctx **out)
     g.dz = params->dz;
     g.rho = params->density;
     g.ls = params->line_spacing;
+    g.thr_src = params->threshold;
     g.thr = params->threshold;
+    if (params->grad_storage == OMNI3D_GRAD_BF16 && method_accum(params->method) == kAccSelect) {
+        // BF16 storage: the kernels compare the stored curl against the threshold's BF16
+        // truncation, and k_pack maps every curl to the same side of it (curl_bf16)
+        uint32_t b;
+        std::memcpy(&b, &params->threshold, sizeof(b));
+        b &= 0xffff0000u;
+        std::memcpy(&g.thr, &b, sizeof(b));
+        g.curl_map = 1;
+    }
     int mx = std::max(std::max(g.X, g.Y), g.Z);
     g.ng = (int)(mx * 1.732 / (double)params->line_spacing);  // K:6167
     ctx->geo.nv = params->n_dirs;

@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_weighted(Grid g, co
     float I = 0.0f, comp = 0.0f, csum = 0.0f, nseg = 0.0f;
     walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, !FB>(
         L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, uint32_t v, const float4 &gv, uint32_t word) {
-            float cn = BF16 ? __ldg(curl + v) : curl_of<FB>(gv);
+            float cn = curl_of<FB>(gv);
             kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
             csum += __fdiv_rn(cn, 1.0e4f);  // the weights as in k_sweep_weighted
             nseg += 1.0f;
@@ -235,12 +235,12 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_weighted_raw(Grid g
     const uint32_t e = r.e;
     const uint32_t ecol = start_col<PASS>(S, e);
     float4 gl = load_grad<BF16>(f32, b16, e);
-    float csum = BF16 ? __ldg(curl + e) : curl_of<FB>(gl), nseg = 1.0f;
+    float csum = curl_of<FB>(gl), nseg = 1.0f;
     emit_w<PASS, false>(S, e, ecol, __frcp_rn(csum), 0.0f, FB ? anchor_of<FB>(gl, 0u, e) : is_anchor(S.bits, e));
     float I = 0.0f, comp = 0.0f;
     walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, !FB>(
         L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, uint32_t v, const float4 &gv, uint32_t word) {
-            float cn = BF16 ? __ldg(curl + v) : curl_of<FB>(gv);
+            float cn = curl_of<FB>(gv);
             kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
             csum += cn;
             nseg += 1.0f;
@@ -267,8 +267,9 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_select(Grid g, cons
     const float thr = g.thr;
     float4 gl = make_float4(0.f, 0.f, 0.f, 0.f);
     if (PASS == kFill) gl = load_grad<BF16>(f32, b16, L.v);
-    // the FP32 field carries curl in .w: one gather per step in the filling pass
-    constexpr bool kW = PASS == kFill && !BF16;
+    // the field carries curl (.w of the FP32 entry, the high half of the BF16 record's second
+    // word): one gather per step in the filling pass
+    constexpr bool kW = PASS == kFill;
     float ce = kW ? curl_of<FB>(gl) : __ldg(curl + L.v);
     bool started = !(ce == 0.0f || ce > thr);
     bool paused = false;
@@ -697,7 +698,8 @@ cudaError_t run_pass(const Geometry &geo, const Field &f, int method, bool bf16,
     if (PASS == kRhs && acc != kAccPlain) ok = false;  // only the plain operator is cached
     if (!ok) return cudaErrorInvalidValue;
     if (PASS == kMark) launch_pass<kMark, false, false>(acc, geo, f, S, st);  // reads no field
-    else if (bf16) launch_pass<PASS, true, true>(acc, geo, f, S, st);
+    else if (bf16 && fb) launch_pass<PASS, true, true>(acc, geo, f, S, st);
+    else if (bf16) launch_pass<PASS, true, false>(acc, geo, f, S, st);
     else if (fb) launch_pass<PASS, false, true>(acc, geo, f, S, st);
     else launch_pass<PASS, false, false>(acc, geo, f, S, st);
     return cudaGetLastError();
@@ -772,9 +774,9 @@ cudaError_t anchor_build(Geometry &geo, const Field &f, int method, bool bf16, l
         AN_TRY(run_pass<kMark>(geo, f, method, bf16, false, S, st));
     }
     if (ref_voxel >= 0 && ref_voxel < V) AN_TRY(cudaMemsetAsync(A->flag + ref_voxel, 1, 1, st));
-    // the FP32 field carries curl in .w: its sign bit can flag the anchors unless a curl
-    // value already has it set
-    const bool check_sign = !bf16 && f.curl != nullptr;
+    // the field carries curl (FP32 .w, or the BF16 record's high half): its sign bit can flag
+    // the anchors unless a curl value already has it set
+    const bool check_sign = f.curl != nullptr;
     AN_TRY(grow(A->neg, cap[18], sizeof(uint32_t)));
     AN_TRY(cudaMemsetAsync(A->neg, 0, sizeof(uint32_t), st));
     if (check_sign) {
@@ -792,7 +794,7 @@ cudaError_t anchor_build(Geometry &geo, const Field &f, int method, bool bf16, l
     AN_TRY(cudaMemcpyAsync(&neg, A->neg, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     AN_TRY(cudaStreamSynchronize(st));
     A->n = n;
-    const bool fb = bf16 || neg == 0u;
+    const bool fb = neg == 0u;
     AN_TRY(grow(A->vox, cap[7], sizeof(uint32_t) * (size_t)n));
     k_assign_ids<<<grid_for(V), 256, 0, st>>>(V, A->flag, A->pos, A->id, A->vox, A->bits);
     OM_COUNT_LAUNCH();

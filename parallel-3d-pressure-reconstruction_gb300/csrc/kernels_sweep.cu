@@ -5,8 +5,8 @@
 //
 // One thread walks one line by decoding its 2-bit staircase; a warp holds 32 neighbouring
 // lines of one direction, whose step words are interleaved so that every word load is one
-// coalesced 128-byte transaction.  The gradient of each visited voxel is one 16-byte
-// (FP32) or 8-byte (BF16) gather; contributions go to an interleaved (pn, count) pair with
+// coalesced 128-byte transaction.  The gradient and curl of each visited voxel are one
+// 16-byte (FP32) or 8-byte (BF16) gather; contributions go to an interleaved (pn, count) pair with
 // one vector reduction (red.global.add.v2.f32) per visited voxel.  The trapezoid prefix
 // integral along the line is a compensated (Kahan) FP32 sum.
 #include <cuda_bf16.h>
@@ -27,12 +27,13 @@ namespace {
 __device__ __forceinline__ float bf_lo(uint32_t u) { return __uint_as_float(u << 16); }
 __device__ __forceinline__ float bf_hi(uint32_t u) { return __uint_as_float(u & 0xffff0000u); }
 
+// (ax, ay, az, curl) of voxel v from either storage.
 template <bool BF16>
 __device__ __forceinline__ float4 load_grad(const float4 *f32, const uint2 *b16, long long v)
 {
     if (BF16) {
         uint2 u = __ldg(b16 + v);
-        return make_float4(bf_lo(u.x), bf_hi(u.x), bf_lo(u.y), 0.0f);
+        return make_float4(bf_lo(u.x), bf_hi(u.x), bf_lo(u.y), bf_hi(u.y));
     } else {
         return __ldg(f32 + v);
     }
@@ -140,7 +141,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep_weighted(Grid g, const LineRec
     float I = 0.0f, comp = 0.0f, csum = 0.0f, nseg = 0.0f;
     walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, false>(
         L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, nullptr, [&](int a, uint32_t v, const float4 &gv, uint32_t) {
-            float cn = BF16 ? __ldg(curl + v) : gv.w;
+            float cn = gv.w;
             float term = sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z));
             kahan_add(I, comp, term);
             csum += __fdiv_rn(cn, 1.0e4f);
@@ -173,7 +174,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep_weighted_raw(Grid g, const Lin
     L.init(g, r, gbase, desc, li);
     const float pe = __ldg(p + r.e);
     float4 gl = load_grad<BF16>(f32, b16, L.v);
-    float csum = BF16 ? __ldg(curl + L.v) : gl.w, nseg = 1.0f;
+    float csum = gl.w, nseg = 1.0f;
     {
         const float w0 = __frcp_rn(csum);
         acc_add(pncnt + L.v, pe * w0, w0);
@@ -181,7 +182,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep_weighted_raw(Grid g, const Lin
     float I = 0.0f, comp = 0.0f;
     walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, false>(
         L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, nullptr, [&](int a, uint32_t v, const float4 &gv, uint32_t) {
-            float cn = BF16 ? __ldg(curl + v) : gv.w;
+            float cn = gv.w;
             kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
             csum += cn;
             nseg += 1.0f;
@@ -213,14 +214,14 @@ __global__ void __launch_bounds__(256, 4) k_sweep_select(Grid g, const LineRec *
     L.init(g, r, gbase, desc, li);
     const float thr = g.thr;
     float4 gl = load_grad<BF16>(f32, b16, L.v);
-    float ce = BF16 ? __ldg(curl + L.v) : gl.w;
+    float ce = gl.w;
     bool started = !(ce == 0.0f || ce > thr);
     bool paused = false;
     float p0 = started ? __ldg(p + L.v) : 0.0f;
     float I = 0.0f, comp = 0.0f, csum = 0.0f, nseg = 0.0f;
     walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, false>(
         L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, nullptr, [&](int a, uint32_t v, const float4 &gv, uint32_t) {
-            const float cn = BF16 ? __ldg(curl + v) : gv.w;
+            const float cn = gv.w;
             if (!started) {
                 bool ok = (a == 0) ? (cn != 0.0f && cn < thr) : (cn != 0.0f);
                 if (ok) {
@@ -287,15 +288,49 @@ __device__ __forceinline__ uint32_t to_bf16(float x)
     return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(x));
 }
 
-__global__ void k_pack(long long V, const float *__restrict__ ax, const float *__restrict__ ay,
-                       const float *__restrict__ az, const float *__restrict__ curl, float4 *f32,
-                       uint2 *b16)
+// BF16 pattern of a curl value.  Round to nearest even, except that a nonzero curl never
+// rounds to zero and, for a thresholded method (g.curl_map), every decision of the selected
+// method is kept: the kernels then compare against the BF16 stand-in g.thr of the threshold
+// g.thr_src (its truncation), and a positive curl below g.thr_src maps below g.thr, one equal
+// to it maps to g.thr, one above it maps above g.thr (positive BF16 patterns order like their
+// values).  The decisions (curl == 0, curl < thr, curl > thr) are then those of the FP32 curl.
+__device__ __forceinline__ uint32_t curl_bf16(float c, const Grid &g)
 {
+    if (c == 0.0f) return __float_as_uint(c) >> 16;  // +0 and -0 stay as they are
+    uint32_t v = to_bf16(c);
+    if ((v & 0x7fffu) == 0u) v |= 1u;  // no underflow to zero
+    if (g.curl_map && c > 0.0f && g.thr_src > 0.0f) {
+        const uint32_t t = __float_as_uint(g.thr) >> 16;
+        if (c < g.thr_src) {
+            if (v >= t) v = t - 1u;
+        } else if (c == g.thr_src) {
+            v = t;
+        } else if (v <= t) {
+            v = t + 1u;
+        }
+    }
+    return v;
+}
+
+// The packed field: float4 (ax, ay, az, curl) and, for BF16 storage, the 8-byte record
+// {ax | ay << 16, az | curl << 16} of round-to-nearest-even BF16 values (the curl by
+// curl_bf16).  With BF16 storage every curl decision must see the stored curl, so the FP32
+// entry's .w and curl_out (which may be the curl array itself) receive it as a float.
+__global__ void k_pack(Grid g, const float *__restrict__ ax, const float *__restrict__ ay,
+                       const float *__restrict__ az, const float *curl, float4 *f32, uint2 *b16, float *curl_out)
+{
+    const long long V = g.V;
     for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < V;
          v += (long long)gridDim.x * blockDim.x) {
         float x = ax[v], y = ay[v], z = az[v];
-        f32[v] = make_float4(x, y, z, curl ? curl[v] : 0.0f);
-        if (b16) b16[v] = make_uint2(to_bf16(x) | (to_bf16(y) << 16), to_bf16(z));
+        float c = curl ? curl[v] : 0.0f;
+        if (b16) {
+            const uint32_t cb = curl_bf16(c, g);
+            b16[v] = make_uint2(to_bf16(x) | (to_bf16(y) << 16), to_bf16(z) | (cb << 16));
+            c = __uint_as_float(cb << 16);
+            if (curl_out) curl_out[v] = c;
+        }
+        f32[v] = make_float4(x, y, z, c);
     }
 }
 
@@ -563,9 +598,10 @@ cudaError_t init_accum(long long V, const float *p_init, bool seed, float2 *pncn
 }
 
 cudaError_t pack_field(const Grid &g, const float *ax, const float *ay, const float *az, const float *curl,
-                       Field *f, bool make_bf16, cudaStream_t st)
+                       Field *f, bool make_bf16, cudaStream_t st, float *curl_rounded)
 {
-    k_pack<<<grid_for(g.V), 256, 0, st>>>(g.V, ax, ay, az, curl, f->f32, make_bf16 ? f->bf16 : nullptr);
+    k_pack<<<grid_for(g.V), 256, 0, st>>>(g, ax, ay, az, curl, f->f32, make_bf16 ? f->bf16 : nullptr,
+                                          make_bf16 ? curl_rounded : nullptr);
     OM_COUNT_LAUNCH();
     return cudaGetLastError();
 }

@@ -31,8 +31,12 @@ struct Grid {
     float cx, cy, cz;       // (N-1)/2 in float, K:665-667
     float dx, dy, dz, rho;  // spacing and density
     float ls;               // line spacing
-    float thr;              // select threshold
+    float thr;              // select threshold the kernels compare against (thr_src, or with
+                            // BF16 storage its BF16 stand-in, see k_pack)
     int ng;                 // lattice points per row, K:6159-6167
+    float thr_src;          // select threshold as given
+    int curl_map;           // 1: BF16 storage of a thresholded method (curl rounded so that
+                            // every threshold decision is kept)
 };
 
 // One traced line (16 bytes): entry voxel, exit voxel (linear indices), direction and
@@ -118,8 +122,9 @@ void free_bricks(Bricks *B);
 // Gradient field on the device: float4 (ax, ay, az, curl) per voxel, or its bf16 copy.
 struct Field {
     float4 *f32 = nullptr;          // always present
-    uint2 *bf16 = nullptr;          // (ax, ay, az, 0) as bf16 when grad_storage is BF16
-    float *curl = nullptr;          // curl (select method), also in f32[v].w
+    uint2 *bf16 = nullptr;          // {ax | ay << 16, az | curl << 16} as bf16 when grad_storage is BF16
+    float *curl = nullptr;          // curl (methods that read it), also in f32[v].w; BF16-rounded
+                                    // with BF16 storage
 };
 
 // Brick passes B1 + L for the field f (FP32) and the method: per-segment carry-in states.
@@ -137,9 +142,11 @@ cudaError_t brick_error(const Bricks &B, int *flag, cudaStream_t st);
 cudaError_t centre_integration(const Grid &g, const float *ax, const float *ay, const float *az, int stride,
                                double pref, double *scratch, float *out, cudaStream_t st);
 
-// Pack three component arrays (+ optional curl) into the interleaved field.
+// Pack three component arrays (+ optional curl) into the interleaved field.  With make_bf16
+// the BF16-rounded curl is also written to curl_rounded (when given; it may be curl).
 cudaError_t pack_field(const Grid &g, const float *ax, const float *ay, const float *az,
-                       const float *curl, Field *f, bool make_bf16, cudaStream_t st);
+                       const float *curl, Field *f, bool make_bf16, cudaStream_t st,
+                       float *curl_rounded = nullptr);
 // |curl a| x mask into out (and into field .w when f is given).
 cudaError_t curl_field(const Grid &g, const float *ax, const float *ay, const float *az,
                        const float *mask, float *out, cudaStream_t st);

@@ -16,13 +16,15 @@ namespace omni3d {
 
 __device__ __forceinline__ float4 load_grad_f32(const float4 *f32, long long v) { return __ldg(f32 + v); }
 
-// (ax, ay, az) from BF16 storage; .w is +0 or -0: bit 31 of the second word, which the
-// anchor filling pass sets on the anchor voxels (the bits above az are otherwise zero).
+// (ax, ay, az, curl) from the 8-byte BF16 record {ax | ay << 16, az | curl << 16}: one
+// 8-byte gather per voxel.  The curl's sign bit (bit 31 of the second word) is the anchor
+// flag that the filling pass sets on the anchor voxels (curl is a magnitude, so the bit is
+// otherwise clear).
 __device__ __forceinline__ float4 load_grad_b16(const uint2 *b16, long long v)
 {
     const uint2 u = __ldg(b16 + v);
     return make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xffff0000u), __uint_as_float(u.y << 16),
-                       __uint_as_float(u.y & 0x80000000u));
+                       __uint_as_float(u.y & 0xffff0000u));
 }
 
 // Which gradient a walk gathers per step.

@@ -20,6 +20,7 @@ relative L2 over those voxels (no gauge: both sides run the same iteration).
 """
 import os
 
+import bf16_ref
 import numpy as np
 import pytest
 
@@ -67,6 +68,31 @@ def test_config3_blobs256_select_vs_fp64_oracle_on_a_direction_subset(omni, orc)
             r = s.solve(f["ax"], f["ay"], f["az"], mask=f["mask"])
         assert r.stats["iterations"] == K
         _check(r, saved[K], ecnt, exact_counts=False)
+
+
+def test_config3_blobs256_select_bf16_storage_vs_fp64_oracle_on_the_stored_field(omni, orc):
+    """The same configuration with BF16 storage (one 8-byte record per voxel): K = 8 against the
+    FP64 oracle fed the field and curl as stored (tests/bf16_ref.py), and against the FP64
+    oracle on the FP32 field (the storage's own error at this size)."""
+    f = synthetic.blobs(n=256, count=8, sigma_range=(8.0, 24.0), noise=0.05, seed=0, spacing=1e-3,
+                        sphere_radius=40.0)
+    dims = f["dims"]
+    sub = _subset(omni.icosphere(4), 16)
+    curl = orc.curl(dims, f["spacing"], f["ax"], f["ay"], f["az"], f["mask"])
+    p0 = np.zeros(int(np.prod(dims)), np.float32)
+    K = 8
+    with omni.Omni3D(dims, f["spacing"], sub, max_iter=K, method="select", threshold=FLT_MAX, grad="bf16") as s:
+        r = s.solve(f["ax"], f["ay"], f["az"], mask=f["mask"])
+    rb = {k: bf16_ref.round_bf16(f[k]) for k in ("ax", "ay", "az")}
+    cb, thr_b = bf16_ref.curl_bf16(curl, FLT_MAX)
+    ep, ecnt, _, _ = orc.solve_cached(dims, f["spacing"], sub, rb["ax"], rb["ay"], rb["az"], p0, K, mode=1, thr=thr_b,
+                                      curl=cb, nthreads=os.cpu_count() or 1)
+    _check(r, ep, ecnt, exact_counts=False)
+    fp, fcnt, _, _ = orc.solve_cached(dims, f["spacing"], sub, f["ax"], f["ay"], f["az"], p0, K, mode=1, thr=FLT_MAX,
+                                      curl=curl, nthreads=os.cpu_count() or 1)
+    np.testing.assert_array_equal(fcnt > 0, ecnt > 0)
+    err = synthetic.relative_l2(r.p.reshape(-1), fp, gauge="mean", weights=fcnt > 0)
+    assert err < 2e-3, err
 
 
 def test_config2_taylor_green128_plain_vs_fp64_oracle_on_a_direction_subset(omni, orc):
