@@ -205,10 +205,12 @@ int omni3d_sweep(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
 int omni3d_gauge(omni3d_ctx *ctx, float *p, const float *count, long long n, int gauge,
                  long long ref, int device_ptrs);
 
-/* Adjoint of the last omni3d_solve on ctx (plain method): writes the gradient of
+/* Adjoint of the last omni3d_solve on ctx, for every method: writes the gradient of
  * <grad_p, p_out> with respect to ax, ay, az, i.e. the transpose of the solve's affine map
  * (scatter back along the lines and through the iterations, no stored iterates), including
- * the transpose of the output gauge.  No counterpart in the reference; it serves pressure
+ * the transpose of the output gauge.  The curl the solve used is held fixed: the weights and
+ * segment splits of the selected and weighted methods (K:1993-2537) depend on it, and no
+ * derivative is taken through it.  No counterpart in the reference; it serves pressure
  * sensitivities and torch.autograd (the omni3d Python package). */
 int omni3d_adjoint(omni3d_ctx *ctx, const float *grad_p, float *grad_ax, float *grad_ay,
                    float *grad_az, int device_ptrs);
@@ -254,21 +256,30 @@ int omni3d_sweep_noalloc(omni3d_ctx *ctx, const float *ax, const float *ay, cons
 
 /* ---------------------------------------------------------------- batches of snapshots */
 
-/* A batch solves several snapshots, each with its own context (grid sizes may differ), in
- * one CUDA-graph launch: every member's solve runs on its own stream, forked from and
- * joined to the batch stream, captured once and relaunched while the buffers stay the same.
- * This replaces the reference's sequential per-file loop (K:8701-8963).  Members need the
- * plain method, the anchor solver and tol = 0 (a fixed iteration count); the first
- * omni3d_batch_solve prepares each member with one regular solve. */
+/* A batch solves several snapshots, each with its own context (grid sizes, methods and
+ * tolerances may differ).  This replaces the reference's sequential per-file loop
+ * (K:8701-8963).  When every member has the plain method, the anchor solver and tol = 0 (a
+ * fixed iteration count), the batch is one CUDA-graph launch: every member's solve runs on
+ * its own stream, forked from and joined to the batch stream, captured once and relaunched
+ * while the buffers stay the same; the first omni3d_batch_solve prepares each member with
+ * one regular solve.  Otherwise (a member with another method -- the selected method that
+ * main runs rebuilds its operator per field --, the sweep solver, or its own tolerance) the
+ * members are solved concurrently, each by omni3d_solve on its own context stream, shared
+ * among a pool of host threads, so that one member's host synchronisations hold up only its
+ * own thread; stats->ms_total is then the host wall time of the batch and
+ * stats->iterations the most any member ran. */
 typedef struct omni3d_batch omni3d_batch;
 int omni3d_batch_create(omni3d_ctx *const *ctxs, int n, omni3d_batch **out);
 int omni3d_batch_destroy(omni3d_batch *batch);
 const char *omni3d_batch_last_error(const omni3d_batch *batch);
-/* Per-member arrays of n pointers; p_init and count_out (and their entries) may be NULL.
- * stats (optional) aggregates the members; ms_total is the device time of the graph. */
+/* Per-member arrays of n pointers; mask, p_init and count_out (and their entries) may be
+ * NULL.  mask is the members' mask column, from which the methods that read the curl
+ * compute it (|curl a| x mask, as omni3d_solve with curl = NULL); a batch with any mask
+ * runs in the concurrent form.  stats (optional) aggregates the members; ms_total is the
+ * device time of the graph (the host wall time in the concurrent form). */
 int omni3d_batch_solve(omni3d_batch *batch, const float *const *ax, const float *const *ay,
-                       const float *const *az, const float *const *p_init, float *const *p_out,
-                       float *const *count_out, int device_ptrs, omni3d_stats *stats);
+                       const float *const *az, const float *const *mask, const float *const *p_init,
+                       float *const *p_out, float *const *count_out, int device_ptrs, omni3d_stats *stats);
 
 /* ---------------------------------------------------------------- host-side helpers */
 

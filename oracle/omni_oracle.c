@@ -1382,3 +1382,178 @@ long orc_sor_steps_to_f64(long X, long Y, long Z, const double *rhs, const doubl
     free(keep);
     return found;
 }
+
+/* ------------------------------------------------------------------------------------ */
+/* FP64 adjoint of every accumulation mode, curl held fixed                               */
+/* ------------------------------------------------------------------------------------ */
+
+/* With the curl field held fixed, every mode's iteration is affine in the gradient field:
+ * a line's walk, its segments (the selected method's starts, pauses and restarts), its
+ * weights and the steps whose trapezoid increments enter its integral depend on the curl
+ * alone.  line_program_f64 records that structure for one line, in the FP64 line functions'
+ * arithmetic (line_plain / line_select / line_weighted / line_weighted_mc above), for the
+ * entry (index 0) and every step s = 1..n:
+ *   vox[s]   the voxel;  seg[s] the segment the step belongs to (-1: none yet);
+ *   term[s]  1 when the step's increment h * (a(v_s) + a(v_{s-1})) enters the integral;
+ *   w[s]     the weight of the contribution w * (p(start) + I) made to vox[s] (0: none);
+ * and start[j], the voxel whose value segment j reads.  Returns the number of segments. */
+static int line_program_f64(const orc_grid *g, int mode, const int in[3], const int out[3], const signed char *ax,
+                            int n, const float *curl, long *vox, int *seg, unsigned char *term, double *w,
+                            long *start)
+{
+    const long X = g->X, XY = g->X * g->Y;
+    int sg[3];
+    axis_signs(in, out, sg);
+    const long stride[3] = {1, X, XY};
+    vox[0] = in[0] + in[1] * X + in[2] * XY;
+    for (int s = 1; s <= n; s++) vox[s] = vox[s - 1] + sg[ax[s - 1]] * stride[ax[s - 1]];
+    memset(term, 0, (size_t)n + 1);
+    for (int s = 0; s <= n; s++) { w[s] = 0.0; seg[s] = -1; }
+    const long e = vox[0];
+    int nseg = 0;
+    if (mode == 0 || mode == 5) {  /* plain: one segment from the entry, unit weights */
+        start[nseg++] = e;
+        for (int s = 0; s <= n; s++) { seg[s] = 0; term[s] = s > 0; w[s] = (s > 0 || mode == 0) ? 1.0 : 0.0; }
+        return nseg;
+    }
+    if (mode == 2 || mode == 3 || mode == 6) {  /* weighted: one segment from the entry */
+        start[nseg++] = e;
+        double ctmp = mode == 6 ? (double)curl[e] : 0.0, ntmp = mode == 6 ? 1.0 : 0.0;
+        seg[0] = 0;
+        if (mode == 6) w[0] = 1 / ctmp * ntmp;
+        for (int s = 1; s <= n; s++) {
+            seg[s] = 0;
+            term[s] = 1;
+            ctmp += mode == 6 ? (double)curl[vox[s]] : (double)curl[vox[s]] / 10000.0;
+            ntmp += 1;
+            if (mode == 6 || ctmp != 0) w[s] = 1 / ctmp * ntmp;
+        }
+        return nseg;
+    }
+    /* selected (modes 1 and 4): the state machine of line_select */
+    const float thr = g->thr;
+    double ctmp = 0, ntmp = 0;
+    int started = 0, outz = 0, cur = -1;
+    if (!(curl[e] == 0 || curl[e] > thr)) { started = 1; cur = nseg; start[nseg++] = e; }
+    seg[0] = cur;
+    for (int s = 1; s <= n; s++) {
+        const int a = ax[s - 1];
+        const float cn = curl[vox[s]];
+        if (!started) {
+            int ok = (a == 0) ? (cn != 0 && cn < thr) : (cn != 0);
+            if (ok) { started = 1; cur = nseg; start[nseg++] = vox[s]; ntmp = 0; ctmp = 0; }
+        } else {
+            int good = (cn < thr && cn != 0);
+            if (outz == 0 && good) {
+                ctmp += (double)cn / 10000.0;
+                ntmp += 1;
+                term[s] = 1;
+                w[s] = 1 / ctmp * ntmp;
+            }
+            int enter_bad = (a == 0) ? ((outz == 0 && cn >= thr) || cn == 0) : (outz == 0 && cn >= thr);
+            if (enter_bad) outz = 1;
+            if (outz == 1 && good) {
+                cur = nseg;
+                start[nseg++] = vox[s];
+                outz = 0;
+                if (a != 2) { ntmp = 0; ctmp = 0; }
+            }
+        }
+        seg[s] = cur;
+    }
+    return nseg;
+}
+
+/* Gradient of <g, p_niter> with respect to (au, av, aw) for the iteration of orc_solve
+ * (p = pn = p_init, niter x {sweep, p = pn / count where count > 0}) of any mode, with curl
+ * held fixed, in FP64 on the full voxel set (no anchor operator):
+ *   p_k(v) = (sum over contributions c to v of w_c (p_{k-1}(start_c) + I_c) + seeding)
+ *            / C(v)  where C(v) = sum w_c > 0, else p_{k-1}(v);
+ * backwards: mu_k = lambda_k / C, dL/dI_c += w_c mu_k(v_c), lambda_{k-1}(start_c) +=
+ * w_c mu_k(v_c) (+ lambda_k where C = 0); then along each segment the suffix sums R_t of
+ * dL/dI over the contributions at or after step t multiply the step's trapezoid coefficient
+ * and go to both voxels of the step.  The seeding by p_init does not depend on the field. */
+void orc_adjoint_modes_f64(const orc_problem *P, const float *curl, int niter, const double *g, double *gau,
+                           double *gav, double *gaw)
+{
+    const long V = P->X * P->Y * P->Z;
+    orc_cache *h = (orc_cache *)orc_cache_build(P, curl, 1);
+    orc_grid gr = {P->X, P->Y, P->Z, P->dx, P->dy, P->dz, P->rho, P->thr};
+    const long cap = max_path(P->X, P->Y, P->Z) + 2;
+    long *vox = (long *)malloc(sizeof(long) * (size_t)cap), *start = (long *)malloc(sizeof(long) * (size_t)cap);
+    int *seg = (int *)malloc(sizeof(int) * (size_t)cap);
+    unsigned char *term = (unsigned char *)malloc((size_t)cap);
+    double *w = (double *)malloc(sizeof(double) * (size_t)cap);
+    /* pass 1: the contributions (voxel, start voxel, weight) in line order, and C */
+    long nc = 0, capc = 1 << 20;
+    long *cv = (long *)malloc(sizeof(long) * (size_t)capc), *cs = (long *)malloc(sizeof(long) * (size_t)capc);
+    double *cw = (double *)malloc(sizeof(double) * (size_t)capc);
+    double *C = (double *)calloc((size_t)V, sizeof(double));
+    for (long i = 0; i < h->nl; i++) {
+        const orc_cline *c = &h->lines[i];
+        line_program_f64(&gr, P->mode, c->in, c->out, h->steps + c->off, c->n, curl, vox, seg, term, w, start);
+        for (int s = 0; s <= c->n; s++) {
+            if (w[s] == 0.0) continue;
+            if (nc == capc) {
+                capc *= 2;
+                cv = (long *)realloc(cv, sizeof(long) * (size_t)capc);
+                cs = (long *)realloc(cs, sizeof(long) * (size_t)capc);
+                cw = (double *)realloc(cw, sizeof(double) * (size_t)capc);
+            }
+            cv[nc] = vox[s];
+            cs[nc] = start[seg[s]];
+            cw[nc] = w[s];
+            C[vox[s]] += w[s];
+            nc++;
+        }
+    }
+    /* the iterations backwards */
+    double *dI = (double *)calloc((size_t)(nc > 0 ? nc : 1), sizeof(double));
+    double *lam = (double *)malloc(sizeof(double) * (size_t)V), *nxt = (double *)malloc(sizeof(double) * (size_t)V);
+    double *mu = (double *)malloc(sizeof(double) * (size_t)V);
+    memcpy(lam, g, sizeof(double) * (size_t)V);
+    for (int k = niter; k >= 1; k--) {
+        for (long v = 0; v < V; v++) {
+            mu[v] = C[v] > 0 ? lam[v] / C[v] : 0.0;
+            nxt[v] = C[v] > 0 ? 0.0 : lam[v];
+        }
+        for (long j = 0; j < nc; j++) {
+            const double t = cw[j] * mu[cv[j]];
+            dI[j] += t;
+            nxt[cs[j]] += t;
+        }
+        memcpy(lam, nxt, sizeof(double) * (size_t)V);
+    }
+    /* pass 2: suffix sums along each segment, scattered to the two voxels of each step */
+    memset(gau, 0, sizeof(double) * (size_t)V);
+    memset(gav, 0, sizeof(double) * (size_t)V);
+    memset(gaw, 0, sizeof(double) * (size_t)V);
+    double *ga[3] = {gau, gav, gaw};
+    const float dl[3] = {P->dx, P->dy, P->dz};
+    long j0 = 0;
+    for (long i = 0; i < h->nl; i++) {
+        const orc_cline *c = &h->lines[i];
+        const signed char *ax = h->steps + c->off;
+        line_program_f64(&gr, P->mode, c->in, c->out, ax, c->n, curl, vox, seg, term, w, start);
+        int sgn[3];
+        axis_signs(c->in, c->out, sgn);
+        long nline = 0;
+        for (int s = 0; s <= c->n; s++) nline += w[s] != 0.0;
+        long j = j0 + nline;  /* contributions of this line: [j0, j0 + nline) in step order */
+        double R = 0.0;
+        for (int s = c->n; s >= 1; s--) {
+            if (s < c->n && seg[s] != seg[s + 1]) R = 0.0;
+            if (w[s] != 0.0) R += dI[--j];
+            if (term[s]) {
+                const int a = ax[s - 1];
+                const double hc = -(double)P->rho * (double)sgn[a] * (double)dl[a] * 0.5;
+                ga[a][vox[s]] += hc * R;
+                ga[a][vox[s - 1]] += hc * R;
+            }
+        }
+        j0 += nline;
+    }
+    orc_cache_free(h);
+    free(vox); free(start); free(seg); free(term); free(w);
+    free(cv); free(cs); free(cw); free(C); free(dI); free(lam); free(nxt); free(mu);
+}

@@ -127,6 +127,7 @@ class Oracle:
         L.orc_cache_errors.argtypes = [C.c_void_p]
         L.orc_cache_free.argtypes = [C.c_void_p]
         L.orc_cache_sweep_f64.argtypes = [C.c_void_p, _fp, _fp, _fp, _fp, _dp, _dp, _dp]
+        L.orc_adjoint_modes_f64.argtypes = [C.POINTER(OrcProblem), _fp, _i, _dp, _dp, _dp, _dp]
         L.orc_adjoint_f64.argtypes = [C.POINTER(OrcProblem), _i, _dp, _dp, _dp, _dp]
         L.orc_calindex.argtypes = [_l, _l, _l, _lp]
         L.orc_curl.argtypes = [_l, _l, _l, _f, _f, _f, _fp, _fp, _fp, _fp, _fp]
@@ -339,6 +340,19 @@ class Oracle:
         g = np.ascontiguousarray(np.asarray(g, np.float64).reshape(-1))
         out = [np.zeros(V, np.float64) for _ in range(3)]
         self.lib.orc_adjoint_f64(C.byref(P), int(niter), _ptr(g, C.c_double), *[_ptr(o, C.c_double) for o in out])
+        return out
+
+    def adjoint_modes(self, dims, spacing, k, niter, g, *, rho=1.0, ls=1.0, mode=0, thr=0.0, curl=None):
+        """FP64 gradient of <g, p_niter> with respect to (au, av, aw) for any mode, curl held
+        fixed (orc_adjoint_modes_f64: the full-voxel iteration, no anchor operator)."""
+        P, keep = self._problem(dims, spacing, rho, ls, thr, k, mode, False)
+        V = dims[0] * dims[1] * dims[2]
+        g = np.ascontiguousarray(np.asarray(g, np.float64).reshape(-1))
+        curl = np.ascontiguousarray(np.asarray(curl, np.float32).reshape(-1)) if curl is not None else np.zeros(
+            V, np.float32)
+        out = [np.zeros(V, np.float64) for _ in range(3)]
+        self.lib.orc_adjoint_modes_f64(C.byref(P), _ptr(curl, C.c_float), int(niter), _ptr(g, C.c_double),
+                                       *[_ptr(o, C.c_double) for o in out])
         return out
 
     def calindex(self, dims) -> np.ndarray:

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -12,6 +14,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <utility>
 #include <vector>
@@ -69,6 +72,7 @@ struct omni3d_ctx {
     DeviceBuf pvol_a, pvol_b, pout, cnt, pncnt, scratch, flags;
     Anchor anc;
     bool anc_cached = false;  // plain method: operator structure built for this geometry
+    bool anc_last = false;    // the operator in anc is that of the last solve's field and method
     DeviceBuf centre;         // FP64 scratch of the centre integration
     DeviceBuf pncnt64;        // FP64 accumulators of the sweep_fp64 sweeps
     Bricks bricks;            // brick segments of the geometry (built on first use)
@@ -937,6 +941,7 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
     int solver = P.solver;
     Anchor &A = ctx->anc;
     long long ref_anchor = -1;
+    ctx->anc_last = false;
     if (K > 0 && solver == OMNI3D_SOLVER_ANCHOR) {
         std::string aerr;
         cudaError_t e;
@@ -956,6 +961,7 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
             ctx->anc_cached = e == cudaSuccess && P.method == OMNI3D_METHOD_PLAIN;
             adjoint_free(&ctx->adj);
         }
+        ctx->anc_last = e == cudaSuccess;
         if (e == cudaErrorNotSupported) {
             cudaGetLastError();
             solver = OMNI3D_SOLVER_SWEEP;  // operator not profitable: one sweep per iteration
@@ -1121,9 +1127,6 @@ int omni3d_adjoint(omni3d_ctx *ctx, const float *grad_p, float *grad_ax, float *
 {
     if (!ctx || !grad_p || !grad_ax || !grad_ay || !grad_az) return fail(ctx, OMNI3D_ERR_ARG, "NULL argument");
     if (ctx->last_iterations < 0) return fail(ctx, OMNI3D_ERR_STATE, "no solve to differentiate on this context");
-    if (ctx->last_method != OMNI3D_METHOD_PLAIN)
-        return fail(ctx, OMNI3D_ERR_STATE, "the adjoint covers the plain method (the selected method's weights "
-                                           "depend on the field non-linearly)");
     cudaSetDevice(ctx->prm.device);
     const omni3d_params &P = ctx->prm;
     const Grid &g = ctx->geo.grid;
@@ -1131,15 +1134,24 @@ int omni3d_adjoint(omni3d_ctx *ctx, const float *grad_p, float *grad_ax, float *
     const bool dev = device_ptrs != 0;
     cudaStream_t st = ctx->st;
     const long long ref = (long long)P.ref_i + (long long)P.ref_j * g.X + (long long)P.ref_k * g.XY;
-    if (!ctx->anc_cached) {  // the last solve ran the sweep form: build the operator now
+    const bool plain = P.method == OMNI3D_METHOD_PLAIN;
+    // the plain operator's structure and anchor counts depend on the geometry alone; the other
+    // methods' weights depend on the curl, so their operator must be the last solve's
+    if (plain ? !ctx->anc_cached : !ctx->anc_last) {  // the last solve ran the sweep form: build it now
         Field F;
         F.f32 = ctx->f32.as<float4>();
         F.bf16 = P.grad_storage == OMNI3D_GRAD_BF16 ? ctx->b16.as<uint2>() : nullptr;
+        if (method_uses_curl(P.method)) {  // the curl the solve used, from the packed field
+            CK(ctx, ctx->curl.ensure(sizeof(float) * (size_t)V));
+            CK(ctx, field_curl(V, F.f32, ctx->curl.as<float>(), st));
+            F.curl = ctx->curl.as<float>();
+        }
         std::string aerr;
-        cudaError_t e = anchor_build(ctx->geo, F, OMNI3D_METHOD_PLAIN, F.bf16 != nullptr,
-                                     P.gauge == OMNI3D_GAUGE_POINT ? ref : -1, -1, &ctx->anc, st, &aerr);
+        cudaError_t e = anchor_build(ctx->geo, F, P.method, F.bf16 != nullptr, P.gauge == OMNI3D_GAUGE_POINT ? ref : -1,
+                                     -1, &ctx->anc, st, &aerr);
         if (e != cudaSuccess) return fail(ctx, OMNI3D_ERR_CUDA, "anchor operator: " + aerr);
-        ctx->anc_cached = true;
+        ctx->anc_cached = plain;
+        ctx->anc_last = true;
         adjoint_free(&ctx->adj);
     }
     const float *dg = grad_p;
@@ -1160,8 +1172,8 @@ int omni3d_adjoint(omni3d_ctx *ctx, const float *grad_p, float *grad_ax, float *
         gy = gx + V;
         gz = gy + V;
     }
-    CK(ctx, adjoint_plain(ctx->geo, ctx->anc, &ctx->adj, ctx->last_iterations, gg, ctx->cnt.as<float>(), gx, gy, gz,
-                          st));
+    CK(ctx, adjoint_solve(ctx->geo, ctx->anc, &ctx->adj, ctx->last_iterations, P.method, ctx->f32.as<float4>(), gg,
+                          ctx->cnt.as<float>(), gx, gy, gz, st));
     if (!dev) {
         CK(ctx, cudaMemcpyAsync(grad_ax, gx, sizeof(float) * (size_t)V, cudaMemcpyDeviceToHost, st));
         CK(ctx, cudaMemcpyAsync(grad_ay, gy, sizeof(float) * (size_t)V, cudaMemcpyDeviceToHost, st));
@@ -1232,8 +1244,79 @@ int omni3d_batch_destroy(omni3d_batch *b)
 
 const char *omni3d_batch_last_error(const omni3d_batch *b) { return b ? b->err.c_str() : g_error.c_str(); }
 
+namespace {
+
+// A member that the one-graph form can run: plain method, anchor solver, fixed iteration
+// count (its solve has no host synchronisation once the cached operator exists).
+bool graph_member(const omni3d_ctx *c)
+{
+    return c->prm.method == OMNI3D_METHOD_PLAIN && c->prm.solver == OMNI3D_SOLVER_ANCHOR && c->prm.tol == 0.0;
+}
+
+// The concurrent form: every member solved by omni3d_solve on its own context stream, the
+// members shared among a pool of host threads, so that one member's host synchronisations
+// (operator sizes of the selected method, tolerance checks) hold up only its own thread
+// while the others keep the GPU busy.  Returns the first failing member's status.
+int batch_solve_concurrent(omni3d_batch *b, const float *const *ax, const float *const *ay, const float *const *az,
+                           const float *const *mask, const float *const *p_init, float *const *p_out, float *const *count_out, int device_ptrs,
+                           omni3d_stats *stats)
+{
+    const int n = (int)b->ctx.size();
+    std::vector<omni3d_stats> st((size_t)n);
+    std::vector<int> rc((size_t)n, OMNI3D_OK);
+    std::atomic<int> next{0};
+    const auto t0 = std::chrono::steady_clock::now();
+    auto work = [&]() {
+        for (int i = next.fetch_add(1); i < n; i = next.fetch_add(1)) {
+            rc[i] = omni3d_solve(b->ctx[i], ax[i], ay[i], az[i], nullptr, mask ? mask[i] : nullptr,
+                                 p_init ? p_init[i] : nullptr, p_out[i],
+                                 count_out ? count_out[i] : nullptr, device_ptrs, &st[i]);
+        }
+    };
+    const int nthreads = std::max(1, std::min(n, 8));
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nthreads; t++) pool.emplace_back(work);
+    work();
+    for (auto &t : pool) t.join();
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    for (int i = 0; i < n; i++)
+        if (rc[i] != OMNI3D_OK) {
+            b->err = "batch member " + std::to_string(i) + ": " + b->ctx[i]->err;
+            g_error = b->err;
+            return rc[i];
+        }
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        stats->ms_total = ms;
+        stats->solver_used = OMNI3D_SOLVER_ANCHOR;
+        stats->engine_used = OMNI3D_ENGINE_LINES;
+        stats->tile_width = b->ctx[0]->geo.tile_width;  // members may differ: the first's
+        stats->dir_group = b->ctx[0]->geo.dir_group;
+        for (int i = 0; i < n; i++) {
+            const omni3d_stats &m = st[i];
+            stats->iterations = std::max(stats->iterations, m.iterations);
+            stats->rel_change = std::max(stats->rel_change, m.rel_change);
+            stats->n_lines += m.n_lines;
+            stats->n_units += m.n_units;
+            stats->walk_errors += m.walk_errors;
+            stats->n_anchors += m.n_anchors;
+            stats->n_links += m.n_links;
+            stats->ms_setup += m.ms_setup;
+            stats->ms_iterate += m.ms_iterate;
+            stats->ms_final += m.ms_final;
+            stats->ms_sweep += m.ms_sweep;
+            stats->kernel_launches += m.kernel_launches;
+            if (m.solver_used == OMNI3D_SOLVER_SWEEP) stats->solver_used = OMNI3D_SOLVER_SWEEP;
+            if (m.engine_used == OMNI3D_ENGINE_BRICKS) stats->engine_used = OMNI3D_ENGINE_BRICKS;
+        }
+    }
+    return OMNI3D_OK;
+}
+
+}  // namespace
+
 int omni3d_batch_solve(omni3d_batch *b, const float *const *ax, const float *const *ay, const float *const *az,
-                       const float *const *p_init, float *const *p_out, float *const *count_out, int device_ptrs,
+                       const float *const *mask, const float *const *p_init, float *const *p_out, float *const *count_out, int device_ptrs,
                        omni3d_stats *stats)
 {
     auto bfail = [&](int code, const std::string &m) {
@@ -1244,6 +1327,12 @@ int omni3d_batch_solve(omni3d_batch *b, const float *const *ax, const float *con
     if (!b || !ax || !ay || !az || !p_out) return bfail(OMNI3D_ERR_ARG, "NULL argument");
     cudaSetDevice(b->device);
     const int n = (int)b->ctx.size();
+    for (int i = 0; i < n; i++)
+        if (!ax[i] || !ay[i] || !az[i] || !p_out[i]) return bfail(OMNI3D_ERR_ARG, "NULL member argument");
+    bool any_mask = false;
+    for (int i = 0; mask && i < n; i++) any_mask = any_mask || mask[i] != nullptr;
+    if (any_mask || !std::all_of(b->ctx.begin(), b->ctx.end(), graph_member))
+        return batch_solve_concurrent(b, ax, ay, az, mask, p_init, p_out, count_out, device_ptrs, stats);
     const bool dev = device_ptrs != 0;
     // device-side inputs and outputs of every member
     std::vector<const float *> dax(n), day(n), daz(n), dp0(n);
@@ -1253,8 +1342,6 @@ int omni3d_batch_solve(omni3d_batch *b, const float *const *ax, const float *con
         if (!ax[i] || !ay[i] || !az[i] || !p_out[i]) return bfail(OMNI3D_ERR_ARG, "NULL member argument");
         // first use: a regular solve builds the context's cached operator and buffers
         if (!prepared_for_graph(c)) {
-            if (c->prm.method != OMNI3D_METHOD_PLAIN || c->prm.solver != OMNI3D_SOLVER_ANCHOR || c->prm.tol != 0.0)
-                return bfail(OMNI3D_ERR_STATE, "batch members need the plain method, the anchor solver and tol = 0");
             int rc = omni3d_solve(c, ax[i], ay[i], az[i], nullptr, nullptr, p_init ? p_init[i] : nullptr, p_out[i],
                                   count_out ? count_out[i] : nullptr, device_ptrs, nullptr);
             if (rc) return bfail(rc, std::string("preparing batch member: ") + c->err);

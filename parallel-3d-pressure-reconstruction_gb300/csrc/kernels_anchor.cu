@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_weighted(Grid g, co
             kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
             csum += __fdiv_rn(cn, 1.0e4f);  // the weights as in k_sweep_weighted
             nseg += 1.0f;
-            if (csum != 0.0f) emit_w<PASS, false>(S, v, ecol, __frcp_rn(csum) * nseg, I, anchor_of<FB>(gv, word, v));
+            if (csum != 0.0f) emit_w<PASS, false>(S, v, ecol, __fdividef(nseg, csum), I, anchor_of<FB>(gv, word, v));
             gl = gv;
         });
 }
@@ -244,7 +244,7 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_weighted_raw(Grid g
             kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
             csum += cn;
             nseg += 1.0f;
-            emit_w<PASS, false>(S, v, ecol, __frcp_rn(csum) * nseg, I, anchor_of<FB>(gv, word, v));
+            emit_w<PASS, false>(S, v, ecol, __fdividef(nseg, csum), I, anchor_of<FB>(gv, word, v));
             gl = gv;
         });
 }
@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_select(Grid g, cons
                     csum += cn * 1.0e-4f;  // the weights as in k_sweep_select
                     nseg += 1.0f;
                     if (PASS == kFill)
-                        emit_w<PASS, false>(S, v, scol, __frcp_rn(csum) * nseg, I, anchor_of<FB>(gv, word, v));
+                        emit_w<PASS, false>(S, v, scol, __fdividef(nseg, csum), I, anchor_of<FB>(gv, word, v));
                 }
                 bool enter_bad = (a == 0) ? ((!paused && cn >= thr) || cn == 0.0f) : (!paused && cn >= thr);
                 if (enter_bad) paused = true;

@@ -518,7 +518,7 @@ __device__ __forceinline__ void b2_segment(const BrickArgs &A, const float4 *F, 
                 csum += __fdiv_rn(gv.w, 1.0e4f);
                 nseg += 1.0f;
                 if (csum != 0.0f) {
-                    const float wc = __frcp_rn(csum) * nseg;
+                    const float wc = __fdividef(nseg, csum);
                     atomicAdd(&acc[acur].x, (pe + I) * wc);
                     atomicAdd(&acc[acur].y, wc);
                 }
@@ -566,7 +566,7 @@ __device__ __forceinline__ void b2_segment(const BrickArgs &A, const float4 *F, 
                                                (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
                         csum += cn * 1.0e-4f;
                         nseg += 1.0f;
-                        const float wc = __frcp_rn(csum) * nseg;
+                        const float wc = __fdividef(nseg, csum);
                         atomicAdd(&acc[acur].x, (p0 + I) * wc);
                         atomicAdd(&acc[acur].y, wc);
                     }

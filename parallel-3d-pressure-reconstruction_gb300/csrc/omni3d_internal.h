@@ -147,6 +147,8 @@ cudaError_t centre_integration(const Grid &g, const float *ax, const float *ay, 
 cudaError_t pack_field(const Grid &g, const float *ax, const float *ay, const float *az,
                        const float *curl, Field *f, bool make_bf16, cudaStream_t st,
                        float *curl_rounded = nullptr);
+// The curl a solve used (.w of its packed FP32 field) into out.
+cudaError_t field_curl(long long V, const float4 *f32, float *out, cudaStream_t st);
 // |curl a| x mask into out (and into field .w when f is given).
 cudaError_t curl_field(const Grid &g, const float *ax, const float *ay, const float *az,
                        const float *mask, float *out, cudaStream_t st);
@@ -270,15 +272,17 @@ cudaError_t anchor_gather(const Anchor &A, const float *vol, float *pa, cudaStre
 struct AdjointBuffers {
     unsigned long long *tptr = nullptr;  // transposed operator (built once per operator)
     uint32_t *trow = nullptr;
+    float *tw = nullptr;                 // weights of the transposed entries (weighted operators)
     unsigned long long *tmp = nullptr;
     float *mu = nullptr, *lam = nullptr, *nxt = nullptr, *acc = nullptr;
 };
 void adjoint_free(AdjointBuffers *B);
-// gx, gy, gz = d<g, p_K>/d(ax, ay, az) for the plain method after K iterations, given the
-// operator A of that solve and its per-voxel count cnt.
-cudaError_t adjoint_plain(const Geometry &geo, const Anchor &A, AdjointBuffers *B, int K,
-                          const float *g, const float *cnt, float *gx, float *gy, float *gz,
-                          cudaStream_t st);
+// gx, gy, gz = d<g, p_K>/d(ax, ay, az) for `method` after K iterations with the curl held
+// fixed, given the operator A of that solve, its per-voxel count cnt and its packed FP32
+// field f32 (whose .w holds the curl the solve used).
+cudaError_t adjoint_solve(const Geometry &geo, const Anchor &A, AdjointBuffers *B, int K, int method,
+                          const float4 *f32, const float *g, const float *cnt, float *gx, float *gy,
+                          float *gz, cudaStream_t st);
 // out = G^T g for the output gauge G (part: gauge_transpose_scratch_doubles()).
 cudaError_t gauge_transpose(long long V, int gauge, long long ref, const float *g,
                             const float *cnt, float *out, double *part, cudaStream_t st);

@@ -81,7 +81,7 @@ SIGNATURES = {
     "omni3d_batch_create": (_i, [_vp, _i, C.POINTER(_vp)]),
     "omni3d_batch_destroy": (_i, [_vp]),
     "omni3d_batch_last_error": (C.c_char_p, [_vp]),
-    "omni3d_batch_solve": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, C.POINTER(Stats)]),
+    "omni3d_batch_solve": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, C.POINTER(Stats)]),
     "omni3d_icosphere": (_i, [_i, _vp, _i]),
     "omni3d_read_directions": (_i, [C.c_char_p, _i, _vp]),
     "omni3d_read_params": (_i, [C.c_char_p, C.POINTER(FileParams)]),

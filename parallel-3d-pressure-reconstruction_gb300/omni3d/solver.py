@@ -205,7 +205,7 @@ class Omni3D:
 
     def adjoint(self, grad_p):
         """Gradient of <grad_p, p> with respect to (ax, ay, az) for the last solve on this
-        context (plain method): the transpose of the solve's affine map."""
+        context, with its curl held fixed: the transpose of the solve's affine map."""
         if _is_cuda_tensor(grad_p):
             import torch
 
@@ -324,9 +324,10 @@ def write_curl(path, dims, x, y, z, curl):
 
 
 class Batch:
-    """Several snapshots, one context each (grid sizes may differ), solved together in one
-    CUDA-graph launch (omni3d_batch_*).  Members need the plain method, the anchor solver
-    and tol = 0."""
+    """Several snapshots, one context each (grid sizes, methods and tolerances may differ),
+    solved together (omni3d_batch_*): in one CUDA-graph launch when every member has the
+    plain method, the anchor solver and tol = 0, else concurrently, each member on its own
+    stream from a pool of host threads."""
 
     def __init__(self, solvers):
         self.solvers = list(solvers)
@@ -353,10 +354,12 @@ class Batch:
     def __exit__(self, *exc):
         self.close()
 
-    def solve(self, fields, p_init=None, out=None):
+    def solve(self, fields, p_init=None, out=None, mask=None):
         """fields: list of (ax, ay, az) per member (all CUDA tensors, or all host arrays).
-        out: optional list of (p, count) output buffers (reused between calls so that the
-        captured graph is relaunched).  Returns ([p], [count], stats)."""
+        mask: optional list of per-member mask columns (the curl of the methods that read it
+        is computed from the field and the mask).  out: optional list of (p, count) output
+        buffers (reused between calls so that the captured graph is relaunched).  Returns
+        ([p], [count], stats)."""
         n = len(self.solvers)
         if len(fields) != n:
             raise ValueError("one field per member")
@@ -389,6 +392,9 @@ class Batch:
         arrs = []
         for k in range(3):
             arrs.append((C.c_void_p * n)(*[ptr(fields[i][k], s.V) for i, s in enumerate(self.solvers)]))
+        mk = None
+        if mask is not None:
+            mk = (C.c_void_p * n)(*[ptr(mask[i], s.V) for i, s in enumerate(self.solvers)])
         p0 = None
         if p_init is not None:
             p0 = (C.c_void_p * n)(*[ptr(p_init[i], s.V) for i, s in enumerate(self.solvers)])
@@ -399,7 +405,7 @@ class Batch:
 
             torch.cuda.current_stream().synchronize()
         st = L.Stats()
-        rc = lib().omni3d_batch_solve(self._h, arrs[0], arrs[1], arrs[2], p0, po, co, int(dev), C.byref(st))
+        rc = lib().omni3d_batch_solve(self._h, arrs[0], arrs[1], arrs[2], mk, p0, po, co, int(dev), C.byref(st))
         if rc < 0:
             msg = (lib().omni3d_batch_last_error(self._h) or b"").decode(errors="replace")
             raise L.Omni3DError(rc, msg)

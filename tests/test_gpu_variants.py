@@ -119,7 +119,8 @@ def test_variant_rejections(omni):
                      engine="bricks") as s:
         r = s.solve(f["ax"], f["ay"], f["az"], mask=f["mask"])
         assert r.stats["engine_used"] == 2
+    # the adjoint takes every method (curl held fixed; checked against the FP64 oracle in
+    # tests/test_gpu_adjoint.py)
     with omni.Omni3D(dims, f["spacing"], dirs, max_iter=2, method="weighted_fixed_bc") as s:
         s.solve(f["ax"], f["ay"], f["az"], mask=f["mask"])
-        with pytest.raises(omni.Omni3DError):
-            s.adjoint(np.ones(s.V, np.float32))
+        assert all(np.isfinite(g).all() for g in s.adjoint(np.ones(s.V, np.float32)))

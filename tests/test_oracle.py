@@ -300,3 +300,34 @@ def test_anderson_fixed_point_is_the_iteration_limit(orc, gold):
     assert rel < 1e-12 and res < 1e-12 and ev < its
     np.testing.assert_array_equal(c > 0, cq > 0)
     assert synthetic.relative_l2(q, p, gauge="mean", weights=c > 0) < 1e-9
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2, 4, 6])
+def test_fp64_adjoint_of_every_mode_is_the_transpose(orc, gold, mode):
+    """orc_adjoint_modes_f64 (curl held fixed) is the transpose of the FP64 iteration: the
+    plain mode equals the plain adjoint, and <g, J h> = <J^T g, h> with J h the FP64 solve's
+    response to h (the map is affine in the field for a fixed curl)."""
+    g_ = gold
+    d = _dims(g_, "select")
+    sp = _sp(g_, "select")
+    ax, ay, az = (g_["select_" + k] for k in ("ax", "ay", "az"))
+    curl = g_["select_curl"]
+    thr = float(g_["select_thr"]) if mode in (1, 4) else 0.0
+    V = int(np.prod(d))
+    rng = np.random.default_rng(11)
+    g = rng.normal(size=V)
+    K = 3
+    ga = orc.adjoint_modes(d, sp, g_["dirs"], K, g, mode=mode, thr=thr, curl=curl)
+    if mode == 0:
+        ref = orc.adjoint(d, sp, g_["dirs"], K, g)
+        for a, b in zip(ga, ref):
+            assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max()
+    p0 = np.zeros(V, np.float32)
+    h = [(rng.normal(size=V) * np.abs(c).max()).astype(np.float32) for c in (ax, ay, az)]
+    pp, _ = orc.solve(d, sp, g_["dirs"], ax + h[0], ay + h[1], az + h[2], p0, K, mode=mode, thr=thr, curl=curl,
+                      precision="f64")
+    pm, _ = orc.solve(d, sp, g_["dirs"], ax - h[0], ay - h[1], az - h[2], p0, K, mode=mode, thr=thr, curl=curl,
+                      precision="f64")
+    lhs = float(np.dot(g, (pp - pm) / 2))
+    rhs = float(sum(np.dot(a, b.astype(np.float64)) for a, b in zip(ga, h)))
+    assert abs(lhs - rhs) <= 1e-6 * abs(lhs)
