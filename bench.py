@@ -501,6 +501,7 @@ def config_dict(args):
             if args.level == 4 else None, "icosphere_level": args.level, "line_spacing": 1.0, "method": "select",
             "threshold": "above every curl (split at the mask only)", "sphere_radius_cells": 40.0 * args.n / 256,
             "noise": 0.05, "iterations": args.iters, "grad_storage": args.grad, "solver": args.solver,
+            "deterministic": bool(getattr(args, "deterministic", False)),
             "l2_between_steps": "inputs (%d MB: ax, ay, az, mask) rewritten each step%s" % (
                 16 * args.n ** 3 // 10 ** 6, ", larger than L2" if 16 * args.n ** 3 > 129 * 10 ** 6 else "")}
 
@@ -518,6 +519,7 @@ def main():
     ap.add_argument("--solver", default="anchor", choices=["anchor", "sweep"])
     ap.add_argument("--engine", default="auto", choices=["auto", "lines", "bricks"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--deterministic", action="store_true", help="bit-reproducible solves (fixed-point sums)")
     ap.add_argument("--autotune", action="store_true", help="line order picked by the autotuner (default: 8 x 4 "
                                                               "tiles, 4 directions per group)")
     ap.add_argument("--profile", action="store_true",
@@ -565,7 +567,8 @@ def main():
     dev = torch.device("cuda", local)
 
     def make(iters, tol=0.0, directions=None, **kw):
-        opts = dict(solver=args.solver, grad=args.grad, engine=args.engine, autotune=args.autotune)
+        opts = dict(solver=args.solver, grad=args.grad, engine=args.engine, autotune=args.autotune,
+                    deterministic=args.deterministic)
         opts.update(kw)
         return omni3d.Omni3D(dims, f["spacing"], dirs if directions is None else directions, max_iter=iters,
                              method="select", threshold=FLT_MAX, tol=tol, gauge="mean", device=local, **opts)

@@ -127,6 +127,16 @@ typedef struct {
                                   device and size class (largest grid dimension rounded up to
                                   a multiple of 32, direction count, line spacing, walk rule);
                                   tile_width and dir_group are then ignored */
+    int deterministic;         /* 1: bit-reproducible solves.  The sums whose order the GPU does
+                                  not fix -- the voxels' (pn, count) of every full sweep, the
+                                  anchor operator's rows (b, c) and the rows' sums in each
+                                  iteration -- are taken in 64-bit fixed point (exact and
+                                  order-independent) with power-of-two scales set on the device
+                                  from bounds of the field, and normalised in FP64, so the same
+                                  inputs give the same bits on every run.  Needs the line engine;
+                                  returns OMNI3D_ERR_RANGE if a bound is not finite (a nonzero
+                                  curl below about 1e-300 relative to the field).  The adjoint
+                                  and omni3d_sweep are not covered. */
 } omni3d_params;
 
 typedef struct {

@@ -19,6 +19,7 @@
 #include <utility>
 #include <vector>
 
+#include "fixed.cuh"
 #include "omni3d_internal.h"
 
 using namespace omni3d;
@@ -74,7 +75,9 @@ struct omni3d_ctx {
     bool anc_cached = false;  // plain method: operator structure built for this geometry
     bool anc_last = false;    // the operator in anc is that of the last solve's field and method
     DeviceBuf centre;         // FP64 scratch of the centre integration
-    DeviceBuf pncnt64;        // FP64 accumulators of the sweep_fp64 sweeps
+    DeviceBuf pncnt64;        // FP64 accumulators of the sweep_fp64 sweeps (or the fixed-point ones)
+    Fixed fix;                // bit-reproducible mode: scales and bounds (params.deterministic)
+    DeviceBuf fix_mem;        // its kFixSlots scales and kBitsSlots bits
     Bricks bricks;            // brick segments of the geometry (built on first use)
     bool bricks_failed = false;
     std::string bricks_why;
@@ -213,6 +216,11 @@ int check_params(const omni3d_params *p, std::string *why)
     }
     if (p->dir_group < 0 || p->dir_group > 32) { *why = "dir_group must be 0..32"; return OMNI3D_ERR_ARG; }
     if (p->autotune != 0 && p->autotune != 1) { *why = "autotune must be 0 or 1"; return OMNI3D_ERR_ARG; }
+    if (p->deterministic != 0 && p->deterministic != 1) { *why = "deterministic must be 0 or 1"; return OMNI3D_ERR_ARG; }
+    if (p->deterministic && p->engine == OMNI3D_ENGINE_BRICKS) {
+        *why = "the brick engine's shared-memory sums are not bit-reproducible (deterministic needs the line engine)";
+        return OMNI3D_ERR_ARG;
+    }
     double ng = std::max(std::max(p->nx, p->ny), p->nz) * 1.732 / (double)p->line_spacing;
     if (ng * ng * (double)p->n_dirs / 256.0 > 2.0e9) { *why = "too many lines (lattice x directions)"; return OMNI3D_ERR_RANGE; }
     return OMNI3D_OK;
@@ -621,6 +629,8 @@ int omni3d_destroy(omni3d_ctx *ctx)
     free_geometry(&ctx->geo);
     cudaFree(ctx->geo.d_dirs);
     anchor_free(&ctx->anc);
+    cudaFree(ctx->fix.bc64);
+    ctx->fix_mem.release();
     free_bricks(&ctx->bricks);
     adjoint_free(&ctx->adj);
     ctx->adj_g.release();
@@ -820,7 +830,7 @@ namespace {
 constexpr int kIterChunk = 16;  // even: a chunk leaves the ping-pong buffers in place
 
 cudaError_t iterate_chunk(omni3d_ctx *ctx, const Anchor &A, int gauge, long long ref_anchor, double tol, float *pc,
-                          float *pn, double *red2, cudaStream_t st, int *j_out, double *rel_out)
+                          float *pn, double *red2, cudaStream_t st, int *j_out, double *rel_out, const Fixed *fx)
 {
     cudaError_t e = ctx->iter_buf.ensure(sizeof(double) * (kIterChunk + 1));
     if (e != cudaSuccess) return e;
@@ -832,7 +842,8 @@ cudaError_t iterate_chunk(omni3d_ctx *ctx, const Anchor &A, int gauge, long long
         A.rowptr, A.rowlen, A.col, A.cw, A.bc, A.vox, A.red, reinterpret_cast<const void *>((uintptr_t)A.n),
         reinterpret_cast<const void *>((uintptr_t)A.unit_weights), pc, pn, red2,
         reinterpret_cast<const void *>((uintptr_t)gauge), reinterpret_cast<const void *>((intptr_t)ref_anchor),
-        reinterpret_cast<const void *>((uintptr_t)tol_bits), stop};
+        reinterpret_cast<const void *>((uintptr_t)tol_bits), stop, fx ? fx->scale : nullptr,
+        fx ? fx->bits : nullptr};
     if (!ctx->iter_exec || ctx->iter_key != key) {
         if (ctx->iter_exec) cudaGraphExecDestroy(ctx->iter_exec);
         ctx->iter_exec = nullptr;
@@ -842,7 +853,7 @@ cudaError_t iterate_chunk(omni3d_ctx *ctx, const Anchor &A, int gauge, long long
         for (int j = 0; j < kIterChunk && ce == cudaSuccess; j++) {
             const float *from = (j % 2 == 0) ? pc : pn;
             float *to = (j % 2 == 0) ? pn : pc;
-            ce = anchor_step(A, nullptr, false, gauge, ref_anchor, from, to, red2, st, stop);
+            ce = anchor_step(A, nullptr, false, gauge, ref_anchor, from, to, red2, st, stop, fx);
             if (ce == cudaSuccess) ce = converged_test_launch(red2, tol, j, stop, rels, st);
         }
         cudaGraph_t graph = nullptr;
@@ -896,7 +907,8 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
     if (ctx->geo.walk_rule == 3 && P.max_iter > 0)
         CK(ctx, run_walk(&ctx->geo, 3, F.curl, st));  // minimum-curl paths follow this field
     int engine = OMNI3D_ENGINE_LINES;
-    if (P.max_iter > 0 && P.sweep_fp64) {
+    const bool det = P.deterministic != 0;  // bit-reproducible: fixed-point sums, line engine
+    if (P.max_iter > 0 && (P.sweep_fp64 || det)) {
         if (P.engine == OMNI3D_ENGINE_BRICKS)
             return fail(ctx, OMNI3D_ERR_STATE, "the brick engine accumulates in FP32 only (sweep_fp64)");
     } else if (P.max_iter > 0) {
@@ -942,11 +954,28 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
     Anchor &A = ctx->anc;
     long long ref_anchor = -1;
     ctx->anc_last = false;
+    Fixed *fx = nullptr;
+    if (det && K > 0) {  // the bounds of every fixed-point sum of this solve (kernels_fixed.cu)
+        fx = &ctx->fix;
+        CK(ctx, ctx->fix_mem.ensure(sizeof(double) * kFixSlots + sizeof(unsigned) * kBitsSlots));
+        fx->scale = ctx->fix_mem.as<double>();
+        fx->bits = reinterpret_cast<unsigned *>(fx->scale + kFixSlots);
+        static const double ones[kFixSlots] = {1.0, 1.0, 1.0, 1.0, 1.0};  // scales this solve leaves unused
+        CK(ctx, cudaMemcpyAsync(fx->scale, ones, sizeof(ones), cudaMemcpyHostToDevice, st));
+        fx->acc = method_accum(P.method);
+        fx->hmax = 0.5 * (double)P.density * (double)std::max(std::max(std::fabs(P.dx), std::fabs(P.dy)), std::fabs(P.dz));
+        fx->path = (double)g.X + (double)g.Y + (double)g.Z;
+        unsigned lmax = 0;
+        CK(ctx, max_lines_through(&ctx->geo, st, &lmax));
+        fx->lmax = (double)lmax;
+        CK(ctx, fix_field_bounds(V, F.f32, *fx, st));
+        CK(ctx, fix_fill_scales(*fx, st));
+    }
     if (K > 0 && solver == OMNI3D_SOLVER_ANCHOR) {
         std::string aerr;
         cudaError_t e;
         if (P.method == OMNI3D_METHOD_PLAIN && ctx->anc_cached) {
-            e = anchor_refresh_rhs(ctx->geo, F, bf16, &ctx->anc, st);
+            e = anchor_refresh_rhs(ctx->geo, F, bf16, &ctx->anc, st, fx);
             aerr = cudaGetErrorString(e);
         } else {
             ctx->anc_cached = false;
@@ -957,7 +986,7 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
                 max_links = (long long)(0.8 * (double)fr / 8.0);
             }
             e = anchor_build(ctx->geo, F, P.method, bf16, P.gauge == OMNI3D_GAUGE_POINT ? ref : -1, max_links,
-                             &ctx->anc, st, &aerr);
+                             &ctx->anc, st, &aerr, fx);
             ctx->anc_cached = e == cudaSuccess && P.method == OMNI3D_METHOD_PLAIN;
             adjoint_free(&ctx->adj);
         }
@@ -993,12 +1022,20 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
         }
         cudaEventRecord(ctx->ev[1], st);
         double2 *acc64 = nullptr;
-        if (P.sweep_fp64) {
+        if (P.sweep_fp64 || det) {
             CK(ctx, ctx->pncnt64.ensure(sizeof(double2) * (size_t)V));
             acc64 = ctx->pncnt64.as<double2>();
         }
         for (int it = 1; it <= K; it++) {
-            if (acc64) {
+            if (det) {  // exact fixed-point sums, normalised in FP64
+                Fix2 *accf = reinterpret_cast<Fix2 *>(acc64);
+                CK(ctx, fix_sweep_scales(V, pc, *fx, st));
+                CK(ctx, init_accum_fix(V, dpinit, seed && it == 1, *fx, accf, st));
+                cudaEventRecord(ctx->ev[5], st);
+                CK(ctx, sweep_full_fix(ctx->geo, F, P.method, bf16, pc, accf, fx->scale, st));
+                cudaEventRecord(ctx->ev[6], st);
+                CK(ctx, normalize_fix(V, accf, *fx, pc, pn, dcnt, st));
+            } else if (acc64) {
                 CK(ctx, init_accum64(V, dpinit, seed && it == 1, acc64, st));
                 cudaEventRecord(ctx->ev[5], st);
                 CK(ctx, sweep_full64(ctx->geo, F, P.method, bf16, pc, acc64, st));
@@ -1041,7 +1078,7 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
         for (int it = 1; it <= K - 1;) {
             if (P.tol > 0.0 && it > 1 && A.n > 0 && st != nullptr && K - it >= kIterChunk) {
                 int j = -1;
-                CK(ctx, iterate_chunk(ctx, A, P.gauge, ref_anchor, P.tol, pc, pn, red2, st, &j, &rel));
+                CK(ctx, iterate_chunk(ctx, A, P.gauge, ref_anchor, P.tol, pc, pn, red2, st, &j, &rel, fx));
                 if (j >= 0) {  // step it + j met the tolerance; step j wrote pn when j is even
                     its = it + j;
                     if (j % 2 == 0) std::swap(pc, pn);
@@ -1051,7 +1088,8 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
                 it += kIterChunk;
                 continue;
             }
-            CK(ctx, anchor_step(A, dpinit, seed && it == 1, P.gauge, ref_anchor, pc, pn, P.tol > 0.0 ? red2 : nullptr, st));
+            CK(ctx, anchor_step(A, dpinit, seed && it == 1, P.gauge, ref_anchor, pc, pn, P.tol > 0.0 ? red2 : nullptr, st,
+                                nullptr, fx));
             its = it;
             std::swap(pc, pn);
             if (P.tol > 0.0) {
@@ -1066,7 +1104,16 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
         float *vol = ctx->pvol_a.as<float>();
         CK(ctx, cudaMemcpyAsync(vol, dpinit, sizeof(float) * (size_t)V, cudaMemcpyDeviceToDevice, st));
         CK(ctx, anchor_scatter(A, pc, vol, st));
-        if (P.sweep_fp64) {  // the defect-correction sweep: FP64 sums and normalisation
+        if (det) {  // bit-reproducible: exact fixed-point sums, normalised in FP64
+            CK(ctx, ctx->pncnt64.ensure(sizeof(double2) * (size_t)V));
+            Fix2 *accf = reinterpret_cast<Fix2 *>(ctx->pncnt64.p);
+            CK(ctx, fix_sweep_scales(V, vol, *fx, st));
+            CK(ctx, init_accum_fix(V, dpinit, seed && its == 0, *fx, accf, st));
+            cudaEventRecord(ctx->ev[5], st);
+            CK(ctx, sweep_full_fix(ctx->geo, F, P.method, bf16, vol, accf, fx->scale, st));
+            cudaEventRecord(ctx->ev[6], st);
+            CK(ctx, normalize_fix(V, accf, *fx, dpinit, dout, dcnt, st));
+        } else if (P.sweep_fp64) {  // the defect-correction sweep: FP64 sums and normalisation
             CK(ctx, ctx->pncnt64.ensure(sizeof(double2) * (size_t)V));
             double2 *acc64 = ctx->pncnt64.as<double2>();
             CK(ctx, init_accum64(V, dpinit, seed && its == 0, acc64, st));
@@ -1096,6 +1143,14 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
     CK(ctx, cudaStreamSynchronize(st));
     CK(ctx, cudaGetLastError());
     if ((rc = engine_check(ctx, engine))) return rc;
+    if (fx) {  // a bound without a finite scale (a curl too close to zero): the sums were not held
+        double sc[kFixSlots];
+        CK(ctx, cudaMemcpy(sc, fx->scale, sizeof(sc), cudaMemcpyDeviceToHost));
+        for (double x : sc)
+            if (x == 0.0)
+                return fail(ctx, OMNI3D_ERR_RANGE, "deterministic: a fixed-point bound is not finite (the least "
+                                                   "nonzero curl is too small for the weights' bound)");
+    }
     ctx->last_iterations = done;
     ctx->last_method = P.method;
     if (stats) {
@@ -1250,7 +1305,8 @@ namespace {
 // count (its solve has no host synchronisation once the cached operator exists).
 bool graph_member(const omni3d_ctx *c)
 {
-    return c->prm.method == OMNI3D_METHOD_PLAIN && c->prm.solver == OMNI3D_SOLVER_ANCHOR && c->prm.tol == 0.0;
+    return c->prm.method == OMNI3D_METHOD_PLAIN && c->prm.solver == OMNI3D_SOLVER_ANCHOR && c->prm.tol == 0.0 &&
+           !c->prm.deterministic;
 }
 
 // The concurrent form: every member solved by omni3d_solve on its own context stream, the

@@ -25,6 +25,7 @@
 
 #include <algorithm>
 
+#include "fixed.cuh"
 #include "omni3d_internal.h"
 #include "walk.cuh"
 
@@ -92,6 +93,8 @@ struct Sink {
     uint32_t *col;   // unit-weight operators: the start anchor of each link
     uint2 *cw;       // weighted operators: (start anchor, weight bits) of each link
     float2 *bc;      // per row: (b, c)
+    long long *bc64; // bit-reproducible mode: per row the fixed-point (b, c) instead of bc
+    const double *fix;  // its scales (fixed.cuh)
 };
 
 // Record one contribution of weight wt and integral I into voxel v from the segment whose
@@ -107,16 +110,19 @@ __device__ __forceinline__ void emit_w(const Sink &S, uint32_t v, uint32_t scol,
     if (row < 0) return;  // not an anchor after all: nothing to index
     if (PASS == kFill && (int)scol < 0) return;  // a start that is no anchor: no column to link
     if (PASS == kRhs) {  // plain method, operator cached: only b = sum I is field-dependent
-        atomicAdd(&S.bc[row].x, I);
+        if (S.bc64) fix_add(S.bc64 + 2 * row, I, S.fix[kFixB]);
+        else atomicAdd(&S.bc[row].x, I);
         return;
     }
     const unsigned long long slot = atomicAdd(S.next + row, 1ull);
-    if (UNIT) {
-        S.col[slot] = scol;
-        atomicAdd(S.bc + row, make_float2(I, 1.0f));
+    const float bt = UNIT ? I : wt * I, ct = UNIT ? 1.0f : wt;
+    if (UNIT) S.col[slot] = scol;
+    else S.cw[slot] = make_uint2(scol, __float_as_uint(wt));
+    if (S.bc64) {  // bit-reproducible: exact, order-independent fixed-point row sums
+        fix_add(S.bc64 + 2 * row, bt, S.fix[kFixB]);
+        fix_add(S.bc64 + 2 * row + 1, ct, S.fix[kFixC]);
     } else {
-        S.cw[slot] = make_uint2(scol, __float_as_uint(wt));
-        atomicAdd(S.bc + row, make_float2(wt * I, wt));
+        atomicAdd(S.bc + row, make_float2(bt, ct));
     }
 }
 
@@ -389,6 +395,13 @@ __device__ __forceinline__ double warp_sum_compensated(float s, float comp)
     return d;
 }
 
+// The warp's exact sum of fixed-point lane sums (integer additions: order-independent).
+__device__ __forceinline__ long long warp_sum_fixed(long long t)
+{
+    for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    return t;
+}
+
 __device__ __forceinline__ float anchor_update(double sum, long long row, const float2 *bc,
                                                const uint32_t *vox, const float *p_init, int seed, const float *pc)
 {
@@ -405,19 +418,30 @@ __global__ void __launch_bounds__(256) k_anchor_spmv(long long n, const unsigned
                                                      const uint2 *__restrict__ cw, const float2 *__restrict__ bc,
                                                      const uint32_t *__restrict__ vox, const float *__restrict__ p_init,
                                                      int seed, const float *__restrict__ pc, float *__restrict__ pn,
-                                                     const int *stop)
+                                                     const int *stop, const double *__restrict__ fix)
 {
     if (stop && *stop) return;  // a graph-captured chunk that has met its tolerance
     long long row = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     if (row >= n) return;  // whole warps
     unsigned long long j0 = rowptr[row], j1 = j0 + rowlen[row];
-    float s = 0.0f, comp = 0.0f;
-    for (unsigned long long j = j0 + lane; j < j1; j += 32) {
-        const uint2 q = __ldg(cw + j);
-        kahan_add(s, comp, __uint_as_float(q.y) * __ldg(pc + q.x));
+    double sum;
+    if (fix) {  // bit-reproducible: exact fixed-point sum, whatever the entries' order
+        const double sr = fix[kFixRow];
+        long long t = 0;
+        for (unsigned long long j = j0 + lane; j < j1; j += 32) {
+            const uint2 q = __ldg(cw + j);
+            t += (long long)fix_term(__uint_as_float(q.y) * __ldg(pc + q.x), sr);
+        }
+        sum = (double)warp_sum_fixed(t) / sr;
+    } else {
+        float s = 0.0f, comp = 0.0f;
+        for (unsigned long long j = j0 + lane; j < j1; j += 32) {
+            const uint2 q = __ldg(cw + j);
+            kahan_add(s, comp, __uint_as_float(q.y) * __ldg(pc + q.x));
+        }
+        sum = warp_sum_compensated(s, comp);
     }
-    const double sum = warp_sum_compensated(s, comp);
     if (lane == 0) pn[row] = anchor_update(sum, row, bc, vox, p_init, seed, pc);
 }
 
@@ -428,16 +452,24 @@ __global__ void __launch_bounds__(256) k_anchor_spmv_unit(long long n, const uns
                                                           const uint32_t *__restrict__ vox,
                                                           const float *__restrict__ p_init, int seed,
                                                           const float *__restrict__ pc, float *__restrict__ pn,
-                                                          const int *stop)
+                                                          const int *stop, const double *__restrict__ fix)
 {
     if (stop && *stop) return;
     long long row = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     if (row >= n) return;  // whole warps
     unsigned long long j0 = rowptr[row], j1 = j0 + rowlen[row];
-    float s = 0.0f, comp = 0.0f;
-    for (unsigned long long j = j0 + lane; j < j1; j += 32) kahan_add(s, comp, __ldg(pc + __ldg(col + j)));
-    const double sum = warp_sum_compensated(s, comp);
+    double sum;
+    if (fix) {  // bit-reproducible: exact fixed-point sum, whatever the entries' order
+        const double sr = fix[kFixRow];
+        long long t = 0;
+        for (unsigned long long j = j0 + lane; j < j1; j += 32) t += (long long)fix_term(__ldg(pc + __ldg(col + j)), sr);
+        sum = (double)warp_sum_fixed(t) / sr;
+    } else {
+        float s = 0.0f, comp = 0.0f;
+        for (unsigned long long j = j0 + lane; j < j1; j += 32) kahan_add(s, comp, __ldg(pc + __ldg(col + j)));
+        sum = warp_sum_compensated(s, comp);
+    }
     if (lane == 0) pn[row] = anchor_update(sum, row, bc, vox, p_init, seed, pc);
 }
 
@@ -742,7 +774,7 @@ void anchor_free(Anchor *A)
 }
 
 cudaError_t anchor_build(Geometry &geo, const Field &f, int method, bool bf16, long long ref_voxel,
-                         long long max_nnz, Anchor *A, cudaStream_t st, std::string *err)
+                         long long max_nnz, Anchor *A, cudaStream_t st, std::string *err, Fixed *fx)
 {
     const long long V = geo.grid.V;
     size_t *cap = A->cap;
@@ -835,12 +867,19 @@ cudaError_t anchor_build(Geometry &geo, const Field &f, int method, bool bf16, l
     S.col = unit_links ? A->col : nullptr;
     S.cw = unit_links ? nullptr : A->cw;
     S.bc = A->bc;
+    if (fx) {  // bit-reproducible: the rows' (b, c) in fixed point (scales set by the caller)
+        AN_TRY(grow(fx->bc64, fx->cap_bc64, sizeof(long long) * 2 * (size_t)std::max<long long>(n, 1)));
+        AN_TRY(cudaMemsetAsync(fx->bc64, 0, sizeof(long long) * 2 * (size_t)std::max<long long>(n, 1), st));
+        S.bc64 = fx->bc64;
+        S.fix = fx->scale;
+    }
     if (fb && n) {
         k_field_flags<<<grid_for(n), 256, 0, st>>>(n, A->vox, f.f32, bf16 ? f.bf16 : nullptr, 1);
         OM_COUNT_LAUNCH();
         AN_TRY(cudaGetLastError());
     }
     AN_TRY(run_pass<kFill>(geo, f, method, bf16, fb, S, st));
+    if (fx) AN_TRY(fix_rows_to_float(n, *fx, A->bc, false, st));
     if (n) {  // row lengths; the sweeps read the field unflagged
         k_fill_finish<<<grid_for(n), 256, 0, st>>>(n, A->rowptr, A->next, A->rowlen, fb ? 1 : 0, A->vox, f.f32,
                                                     bf16 ? f.bf16 : nullptr);
@@ -900,17 +939,25 @@ cudaError_t anchor_mark(const Geometry &geo, const Field &f, int method, bool bf
 }
 
 cudaError_t anchor_step(const Anchor &A, const float *p_init, bool seed, int gauge, long long ref_anchor,
-                        const float *p_cur, float *p_next, double *red2, cudaStream_t st, const int *stop)
+                        const float *p_cur, float *p_next, double *red2, cudaStream_t st, const int *stop,
+                        const Fixed *fx)
 {
     if (A.n == 0) return cudaSuccess;
     long long threads = A.n * 32;
+    const double *fix = nullptr;
+    if (fx) {  // bit-reproducible: the row sums' scale from this iterate's largest value
+        cudaError_t e = fix_row_scale(A.n, p_cur, *fx, st, stop);
+        if (e != cudaSuccess) return e;
+        fix = fx->scale;
+    }
     if (A.unit_weights)
         k_anchor_spmv_unit<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(A.n, A.rowptr, A.rowlen, A.col, A.bc, A.vox,
-                                                                               p_init, seed ? 1 : 0, p_cur, p_next, stop);
+                                                                               p_init, seed ? 1 : 0, p_cur, p_next, stop,
+                                                                               fix);
     else
         k_anchor_spmv<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(A.n, A.rowptr, A.rowlen, A.cw, A.bc,
                                                                           A.vox, p_init, seed ? 1 : 0, p_cur, p_next,
-                                                                          stop);
+                                                                          stop, fix);
     OM_COUNT_LAUNCH();
     if (red2 && A.n <= kChangeBlockMax) {
         k_change_block<<<1, 1024, 0, st>>>(A.n, p_cur, p_next, gauge, ref_anchor, red2, stop);
@@ -929,9 +976,11 @@ cudaError_t converged_test_launch(const double *red2, double tol, int j, int *st
     return cudaGetLastError();
 }
 
-cudaError_t anchor_refresh_rhs(const Geometry &geo, const Field &f, bool bf16, Anchor *A, cudaStream_t st)
+cudaError_t anchor_refresh_rhs(const Geometry &geo, const Field &f, bool bf16, Anchor *A, cudaStream_t st,
+                               const Fixed *fx)
 {
     if (A->n == 0) return cudaSuccess;
+    if (fx && (!fx->bc64 || fx->cap_bc64 < sizeof(long long) * 2 * (size_t)A->n)) return cudaErrorInvalidValue;
     k_clear_b<<<grid_for(A->n), 256, 0, st>>>(A->n, A->bc);
     OM_COUNT_LAUNCH();
     cudaError_t e = cudaGetLastError();
@@ -940,6 +989,11 @@ cudaError_t anchor_refresh_rhs(const Geometry &geo, const Field &f, bool bf16, A
     S.bits = A->bits;
     S.id = A->id;
     S.bc = A->bc;
+    if (fx) {
+        if ((e = cudaMemsetAsync(fx->bc64, 0, sizeof(long long) * 2 * (size_t)A->n, st)) != cudaSuccess) return e;
+        S.bc64 = fx->bc64;
+        S.fix = fx->scale;
+    }
     // the plain method's field carries no curl (.w = +0), so the anchors can be flagged in it
     const bool fb = bf16 || f.curl == nullptr;
     if (fb) {
@@ -947,6 +1001,7 @@ cudaError_t anchor_refresh_rhs(const Geometry &geo, const Field &f, bool bf16, A
         OM_COUNT_LAUNCH();
     }
     e = run_pass<kRhs>(geo, f, OMNI3D_METHOD_PLAIN, bf16, fb, S, st);
+    if (e == cudaSuccess && fx) e = fix_rows_to_float(A->n, *fx, A->bc, true, st);
     if (e != cudaSuccess || !fb) return e;
     k_field_flags<<<grid_for(A->n), 256, 0, st>>>(A->n, A->vox, f.f32, bf16 ? f.bf16 : nullptr, 0);
     OM_COUNT_LAUNCH();

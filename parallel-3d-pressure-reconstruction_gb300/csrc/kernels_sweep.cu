@@ -12,7 +12,9 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <type_traits>
 
+#include "fixed.cuh"
 #include "omni3d_internal.h"
 #include "walk.cuh"
 
@@ -73,13 +75,35 @@ struct LineWalk {
     }
 };
 
-// Contributions into the (pn, count) accumulators: one FP32 vector reduction, or (the FP64
-// defect-correction sweep) two FP64 reductions, each a native L2 atomic.
-__device__ __forceinline__ void acc_add(float2 *a, float x, float y) { atomicAdd(a, make_float2(x, y)); }
-__device__ __forceinline__ void acc_add(double2 *a, float x, float y)
+// Contributions into the (pn, count) accumulators: one FP32 vector reduction, (the FP64
+// defect-correction sweep) two FP64 reductions, each a native L2 atomic, or (the
+// bit-reproducible mode) two 64-bit fixed-point additions with the scales fs.
+struct FixScale {
+    double pn = 0.0, cnt = 0.0;
+};
+template <typename ACC>
+__device__ __forceinline__ FixScale load_fix(const double *fix)
+{
+    FixScale f;
+    if (std::is_same<ACC, Fix2>::value && fix) {
+        f.pn = fix[kFixPn];
+        f.cnt = fix[kFixCnt];
+    }
+    return f;
+}
+__device__ __forceinline__ void acc_add(const FixScale &, float2 *a, float x, float y)
+{
+    atomicAdd(a, make_float2(x, y));
+}
+__device__ __forceinline__ void acc_add(const FixScale &, double2 *a, float x, float y)
 {
     atomicAdd(&a->x, (double)x);
     atomicAdd(&a->y, (double)y);
+}
+__device__ __forceinline__ void acc_add(const FixScale &fs, Fix2 *a, float x, float y)
+{
+    fix_add(&a->pn, x, fs.pn);
+    fix_add(&a->cnt, y, fs.cnt);
 }
 
 __device__ __forceinline__ void kahan_add(float &s, float &c, float x)
@@ -98,22 +122,24 @@ __global__ void __launch_bounds__(256, 4) k_sweep_plain(Grid g, const LineRec *_
                                                      const uint32_t *__restrict__ desc, long long n_lines,
                                                      const float4 *__restrict__ f32,
                                                      const uint2 *__restrict__ b16,
-                                                     const float *__restrict__ p, ACC *pncnt)
+                                                     const float *__restrict__ p, ACC *pncnt,
+                                                      const double *__restrict__ fix)
 {
     long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (li >= n_lines) return;
     LineRec r = lines[li];
     LineWalk L;
     L.init(g, r, gbase, desc, li);
+    const FixScale fs = load_fix<ACC>(fix);
     const float pe = __ldg(p + r.e);
-    if (SELF) acc_add(pncnt + r.e, pe, 1.0f);
+    if (SELF) acc_add(fs, pncnt + r.e, pe, 1.0f);
     float4 gl = load_grad<BF16>(f32, b16, L.v);
     float I = 0.0f, comp = 0.0f;
     walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, false>(
         L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, nullptr, [&](int a, uint32_t v, const float4 &gv, uint32_t) {
             float term = sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z));
             kahan_add(I, comp, term);
-            acc_add(pncnt + v, pe + I, 1.0f);
+            acc_add(fs, pncnt + v, pe + I, 1.0f);
             gl = gv;
         });
 }
@@ -129,13 +155,15 @@ __global__ void __launch_bounds__(256, 4) k_sweep_weighted(Grid g, const LineRec
                                                         const float4 *__restrict__ f32,
                                                         const uint2 *__restrict__ b16,
                                                         const float *__restrict__ curl,
-                                                        const float *__restrict__ p, ACC *pncnt)
+                                                        const float *__restrict__ p, ACC *pncnt,
+                                                      const double *__restrict__ fix)
 {
     long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (li >= n_lines) return;
     LineRec r = lines[li];
     LineWalk L;
     L.init(g, r, gbase, desc, li);
+    const FixScale fs = load_fix<ACC>(fix);
     const float pe = __ldg(p + r.e);
     float4 gl = load_grad<BF16>(f32, b16, L.v);
     float I = 0.0f, comp = 0.0f, csum = 0.0f, nseg = 0.0f;
@@ -148,7 +176,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep_weighted(Grid g, const LineRec
             nseg += 1.0f;
             if (csum != 0.0f) {
                 float wc = __fdividef(nseg, csum);
-                acc_add(pncnt + v, (pe + I) * wc, wc);
+                acc_add(fs, pncnt + v, (pe + I) * wc, wc);
             }
             gl = gv;
         });
@@ -165,19 +193,21 @@ __global__ void __launch_bounds__(256, 4) k_sweep_weighted_raw(Grid g, const Lin
                                                             const float4 *__restrict__ f32,
                                                             const uint2 *__restrict__ b16,
                                                             const float *__restrict__ curl,
-                                                            const float *__restrict__ p, ACC *pncnt)
+                                                            const float *__restrict__ p, ACC *pncnt,
+                                                      const double *__restrict__ fix)
 {
     long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (li >= n_lines) return;
     LineRec r = lines[li];
     LineWalk L;
     L.init(g, r, gbase, desc, li);
+    const FixScale fs = load_fix<ACC>(fix);
     const float pe = __ldg(p + r.e);
     float4 gl = load_grad<BF16>(f32, b16, L.v);
     float csum = gl.w, nseg = 1.0f;
     {
         const float w0 = __frcp_rn(csum);
-        acc_add(pncnt + L.v, pe * w0, w0);
+        acc_add(fs, pncnt + L.v, pe * w0, w0);
     }
     float I = 0.0f, comp = 0.0f;
     walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, false>(
@@ -187,7 +217,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep_weighted_raw(Grid g, const Lin
             csum += cn;
             nseg += 1.0f;
             const float wc = __fdividef(nseg, csum);
-            acc_add(pncnt + v, (pe + I) * wc, wc);
+            acc_add(fs, pncnt + v, (pe + I) * wc, wc);
             gl = gv;
         });
 }
@@ -205,13 +235,15 @@ __global__ void __launch_bounds__(256, 4) k_sweep_select(Grid g, const LineRec *
                                                       const float4 *__restrict__ f32,
                                                       const uint2 *__restrict__ b16,
                                                       const float *__restrict__ curl,
-                                                      const float *__restrict__ p, ACC *pncnt)
+                                                      const float *__restrict__ p, ACC *pncnt,
+                                                      const double *__restrict__ fix)
 {
     long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (li >= n_lines) return;
     LineRec r = lines[li];
     LineWalk L;
     L.init(g, r, gbase, desc, li);
+    const FixScale fs = load_fix<ACC>(fix);
     const float thr = g.thr;
     float4 gl = load_grad<BF16>(f32, b16, L.v);
     float ce = gl.w;
@@ -241,7 +273,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep_select(Grid g, const LineRec *
                     csum += cn * 1.0e-4f;
                     nseg += 1.0f;
                     float wc = __fdividef(nseg, csum);
-                    acc_add(pncnt + v, (p0 + I) * wc, wc);
+                    acc_add(fs, pncnt + v, (p0 + I) * wc, wc);
                 }
                 bool enter_bad = (a == 0) ? ((!paused && cn >= thr) || cn == 0.0f) : (!paused && cn >= thr);
                 if (enter_bad) paused = true;
@@ -472,7 +504,7 @@ unsigned grid_for(long long n, int threads = 256)
 
 template <typename ACC>
 cudaError_t sweep_full_t(const Geometry &geo, const Field &f, int method, bool bf16, const float *p, ACC *pncnt,
-                         cudaStream_t st)
+                         cudaStream_t st, const double *fix = nullptr)
 {
     if (geo.n_lines == 0) return cudaSuccess;
     // every pointer the kernels dereference must be set: refuse to launch otherwise
@@ -484,42 +516,42 @@ cudaError_t sweep_full_t(const Geometry &geo, const Field &f, int method, bool b
     if (acc == kAccWeighted) {
         if (bf16)
             k_sweep_weighted<true, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
-                                                           geo.n_lines, f.f32, f.bf16, f.curl, p, pncnt);
+                                                           geo.n_lines, f.f32, f.bf16, f.curl, p, pncnt, fix);
         else
             k_sweep_weighted<false, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
-                                                            geo.n_lines, f.f32, f.bf16, f.curl, p, pncnt);
+                                                            geo.n_lines, f.f32, f.bf16, f.curl, p, pncnt, fix);
         OM_COUNT_LAUNCH();
     } else if (acc == kAccWeightedRawCurl) {
         if (bf16)
             k_sweep_weighted_raw<true, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
-                                                               geo.n_lines, f.f32, f.bf16, f.curl, p, pncnt);
+                                                               geo.n_lines, f.f32, f.bf16, f.curl, p, pncnt, fix);
         else
             k_sweep_weighted_raw<false, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
-                                                                geo.n_lines, f.f32, f.bf16, f.curl, p, pncnt);
+                                                                geo.n_lines, f.f32, f.bf16, f.curl, p, pncnt, fix);
         OM_COUNT_LAUNCH();
     } else if (acc == kAccSelect) {
         if (bf16)
             k_sweep_select<true, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
-                                                         f.f32, f.bf16, f.curl, p, pncnt);
+                                                         f.f32, f.bf16, f.curl, p, pncnt, fix);
         else
             k_sweep_select<false, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
-                                                          f.f32, f.bf16, f.curl, p, pncnt);
+                                                          f.f32, f.bf16, f.curl, p, pncnt, fix);
         OM_COUNT_LAUNCH();
     } else if (acc == kAccPlainNoEntry) {
         if (bf16)
             k_sweep_plain<true, false, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
-                                                               geo.n_lines, f.f32, f.bf16, p, pncnt);
+                                                               geo.n_lines, f.f32, f.bf16, p, pncnt, fix);
         else
             k_sweep_plain<false, false, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
-                                                                geo.n_lines, f.f32, f.bf16, p, pncnt);
+                                                                geo.n_lines, f.f32, f.bf16, p, pncnt, fix);
         OM_COUNT_LAUNCH();
     } else {
         if (bf16)
             k_sweep_plain<true, true, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
-                                                              geo.n_lines, f.f32, f.bf16, p, pncnt);
+                                                              geo.n_lines, f.f32, f.bf16, p, pncnt, fix);
         else
             k_sweep_plain<false, true, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
-                                                               geo.n_lines, f.f32, f.bf16, p, pncnt);
+                                                               geo.n_lines, f.f32, f.bf16, p, pncnt, fix);
         OM_COUNT_LAUNCH();
     }
     return cudaGetLastError();
@@ -537,6 +569,13 @@ cudaError_t sweep_full64(const Geometry &geo, const Field &f, int method, bool b
                          cudaStream_t st)
 {
     return sweep_full_t(geo, f, method, bf16, p, pncnt, st);
+}
+
+cudaError_t sweep_full_fix(const Geometry &geo, const Field &f, int method, bool bf16, const float *p, Fix2 *pncnt,
+                           const double *scale, cudaStream_t st)
+{
+    if (!scale) return cudaErrorInvalidValue;
+    return sweep_full_t(geo, f, method, bf16, p, pncnt, st, scale);
 }
 
 namespace {

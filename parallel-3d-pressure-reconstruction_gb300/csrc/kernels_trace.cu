@@ -371,10 +371,49 @@ cudaError_t ensure_lines_through(Geometry *g, cudaStream_t st)
     return cudaGetLastError();
 }
 
+namespace {
+__global__ void k_max_u32(long long n, const uint32_t *__restrict__ x, unsigned *out)
+{
+    unsigned m = 0u;
+    const long long nthr = ((n + 31) / 32) * 32;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nthr; i += (long long)gridDim.x * blockDim.x)
+        if (i < n) m = max(m, x[i]);
+    m = __reduce_max_sync(0xffffffffu, m);
+    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+}  // namespace
+
+cudaError_t max_lines_through(Geometry *g, cudaStream_t st, unsigned *out)
+{
+    if (!g->d_lines_through) g->max_through = 0;
+    if (g->max_through) {
+        *out = g->max_through;
+        return cudaSuccess;
+    }
+    cudaError_t e = ensure_lines_through(g, st);
+    if (e != cudaSuccess) return e;
+    TmpBuf tb;
+    unsigned *d = nullptr;
+    if ((e = tb.alloc(&d, 1)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(d, 0, sizeof(unsigned), st)) != cudaSuccess) return e;
+    const long long V = g->grid.V;
+    long long blocks = std::min<long long>((V + 255) / 256, 152LL * 64);
+    k_max_u32<<<(unsigned)std::max<long long>(blocks, 1), 256, 0, st>>>(V, g->d_lines_through, d);
+    OM_COUNT_LAUNCH();
+    unsigned h = 0;
+    if ((e = cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess)
+        return e;
+    g->max_through = h;
+    *out = h;
+    return cudaSuccess;
+}
+
 void free_geometry(Geometry *g)
 {
     cudaFree(g->d_lines_through);
     g->d_lines_through = nullptr;
+    g->max_through = 0;
     cudaFree(g->d_counters);
     g->d_counters = nullptr;
     cudaFree(g->d_off);
@@ -488,6 +527,7 @@ cudaError_t run_walk(Geometry *g, int rule, const float *curl, cudaStream_t st)
     // anything derived from the staircases is stale
     cudaFree(g->d_lines_through);
     g->d_lines_through = nullptr;
+    g->max_through = 0;
     g->walk_generation++;
     return cudaSuccess;
 }

@@ -63,6 +63,7 @@ struct Geometry {
     uint32_t *d_gbase = nullptr;    // n_groups + 1 prefix sums of words per lane
     uint32_t *d_desc = nullptr;
     uint32_t *d_lines_through = nullptr;  // per voxel: lines through it (built on first use)
+    unsigned max_through = 0;       // the most lines through one voxel (0: not computed)
     unsigned long long *d_counters = nullptr;  // walk counters (early stops, voxel visits)
     int walk_rule = 0;              // OmWalker rule of the staircases (3: per field, minimum curl)
     long long walk_generation = 0;  // incremented by every walk
@@ -83,6 +84,8 @@ void free_geometry(Geometry *g);
 cudaError_t run_walk(Geometry *g, int rule, const float *curl, cudaStream_t st);
 // Count the lines through every voxel into g->d_lines_through (once per geometry).
 cudaError_t ensure_lines_through(Geometry *g, cudaStream_t st);
+// The most lines through one voxel (once per geometry; synchronises st).
+cudaError_t max_lines_through(Geometry *g, cudaStream_t st, unsigned *out);
 
 // Exclusive scans (out has n + 1 entries; out[n] = total).  tmp must hold
 // scan_tmp_elems(n) elements.
@@ -193,6 +196,11 @@ cudaError_t sweep_full(const Geometry &geo, const Field &f, int method, bool bf1
 cudaError_t sweep_full64(const Geometry &geo, const Field &f, int method, bool bf16, const float *p,
                          double2 *pncnt, cudaStream_t st);
 cudaError_t init_accum64(long long V, const float *p_init, bool seed, double2 *pncnt, cudaStream_t st);
+// The same sweep accumulated in 64-bit fixed point (the bit-reproducible mode), with the
+// voxel scales scale[kFixPn], scale[kFixCnt] (fixed.cuh).
+struct Fix2;
+cudaError_t sweep_full_fix(const Geometry &geo, const Field &f, int method, bool bf16, const float *p, Fix2 *pncnt,
+                           const double *scale, cudaStream_t st);
 cudaError_t normalize64(long long V, const double2 *pncnt, const float *p_keep, float *p_out, float *cnt_out,
                         cudaStream_t st);
 
@@ -204,6 +212,35 @@ cudaError_t accum_split(long long V, const float2 *acc, float *pn, float *cnt, c
 // pncnt = (seed ? p_init : 0, 0)
 cudaError_t init_accum(long long V, const float *p_init, bool seed, float2 *pncnt,
                        cudaStream_t st);
+
+// Bit-reproducible mode (fixed.cuh, kernels_fixed.cu): device scales and bounds, and the
+// operator rows' fixed-point (b, c) while filling.  Kernels that get a null Fixed pointer (or
+// scale pointer) take the default FP32 sums.
+struct Fixed {
+    double *scale = nullptr;        // kFixSlots scales (device)
+    unsigned *bits = nullptr;       // kBitsSlots float bits (device)
+    long long *bc64 = nullptr;      // 2 per operator row (device)
+    size_t cap_bc64 = 0;
+    double lmax = 0.0;              // most lines through one voxel (geometry)
+    int acc = 0;                    // the method's accumulation kind (weight bound)
+    double hmax = 0.0;              // largest trapezoid coefficient rho * spacing / 2
+    double path = 0.0;              // X + Y + Z: bound of a staircase's length
+};
+// Field bounds (max |a|, least nonzero curl) of the packed field into fx->bits.
+cudaError_t fix_field_bounds(long long V, const float4 *f32, const Fixed &fx, cudaStream_t st);
+// Scales for filling the operator (b, c), for the row sums of an iteration from the
+// operator values pa (n of them), and for a full sweep reading the volume vol (V voxels).
+cudaError_t fix_fill_scales(const Fixed &fx, cudaStream_t st);
+cudaError_t fix_row_scale(long long n, const float *pa, const Fixed &fx, cudaStream_t st, const int *stop = nullptr);
+cudaError_t fix_sweep_scales(long long V, const float *vol, const Fixed &fx, cudaStream_t st);
+// bc = the fixed-point (b, c) rows as floats (only b when keep_c).
+cudaError_t fix_rows_to_float(long long n, const Fixed &fx, float2 *bc, bool keep_c, cudaStream_t st);
+// Fixed-point voxel sums: init (pn = seed ? p_init : 0, count = 0), one full sweep,
+// normalisation (p = pn / count where count > 0, else p_keep) -- in FP64 from the exact sums.
+struct Fix2;
+cudaError_t init_accum_fix(long long V, const float *p_init, bool seed, const Fixed &fx, Fix2 *acc, cudaStream_t st);
+cudaError_t normalize_fix(long long V, const Fix2 *acc, const Fixed &fx, const float *p_keep, float *p_out,
+                          float *cnt_out, cudaStream_t st);
 
 // Anchor operator (kernels_anchor.cu).
 struct Anchor {
@@ -231,20 +268,22 @@ struct Anchor {
 };
 // Builds the operator; returns cudaErrorNotSupported (nothing filled) when it would hold
 // more than max_nnz entries (max_nnz < 0: no limit).
+// fx (bit-reproducible mode): the rows' (b, c) are summed in fixed point with the scales of
+// fix_fill_scales, which the caller sets before.
 cudaError_t anchor_build(Geometry &geo, const Field &f, int method, bool bf16,
                          long long ref_voxel, long long max_nnz, Anchor *A, cudaStream_t st,
-                         std::string *err);
+                         std::string *err, Fixed *fx = nullptr);
 void anchor_free(Anchor *A);
 // Plain method: recompute only b (the field-dependent part) of an operator built by
 // anchor_build for the same geometry; rows, columns and c depend on the geometry alone.
 cudaError_t anchor_refresh_rhs(const Geometry &geo, const Field &f, bool bf16, Anchor *A,
-                               cudaStream_t st);
+                               cudaStream_t st, const Fixed *fx = nullptr);
 // One iteration p_next = (b + seed * p_init_a + M p_cur) / c; accumulates the gauged
 // change / norm sums into red[0..1] for the relative change.  With stop, every kernel of the
 // step returns at once while *stop != 0 (the gated steps of a graph-captured chunk).
 cudaError_t anchor_step(const Anchor &A, const float *p_init, bool seed, int gauge,
                         long long ref_anchor, const float *p_cur, float *p_next, double *red2,
-                        cudaStream_t st, const int *stop = nullptr);
+                        cudaStream_t st, const int *stop = nullptr, const Fixed *fx = nullptr);
 // Launch the convergence test of step j of a chunk: rel_out[j] = sqrt(red2[0] / red2[1]),
 // *stop = j + 1 when it is below tol (no-op while *stop != 0).
 cudaError_t converged_test_launch(const double *red2, double tol, int j, int *stop, double *rel_out,

@@ -39,7 +39,8 @@ class Params(C.Structure):
                 ("method", _i), ("solver", _i), ("grad_storage", _i), ("tol", _d), ("gauge", _i),
                 ("ref_i", _i), ("ref_j", _i), ("ref_k", _i), ("seed_first_iteration", _i), ("device", _i),
                 ("anchor_max_links", _ll), ("engine", _i), ("initial_guess", _i),
-                ("sweep_fp64", _i), ("tile_width", _i), ("dir_group", _i), ("autotune", _i)]
+                ("sweep_fp64", _i), ("tile_width", _i), ("dir_group", _i), ("autotune", _i),
+                ("deterministic", _i)]
 
 
 class Stats(C.Structure):

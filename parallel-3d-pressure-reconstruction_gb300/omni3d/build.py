@@ -22,7 +22,7 @@ CLI = os.path.join(BUILD, "omni3d")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 LIB_SOURCES = ["kernels_trace.cu", "kernels_sweep.cu", "kernels_anchor.cu", "kernels_adjoint.cu", "kernels_brick.cu",
-               "api.cu", "host_io.cpp", "noalloc.cu"]
+               "kernels_fixed.cu", "api.cu", "host_io.cpp", "noalloc.cu"]
 CLI_SOURCES = ["cli.cpp"]
 
 

@@ -50,7 +50,7 @@ class Omni3D:
     def __init__(self, dims, spacing, dirs, *, density=1.0, line_spacing=1.0, max_iter=4, threshold=0.0,
                  method="plain", solver="anchor", grad="f32", tol=0.0, gauge="none", ref=(0, 0, 0),
                  seed_first_iteration=True, device=0, anchor_max_links=0, engine="auto", initial_guess="zero",
-                 sweep_fp64=False, tile_width=0, dir_group=0, autotune=False):
+                 sweep_fp64=False, tile_width=0, dir_group=0, autotune=False, deterministic=False):
         nx, ny, nz = (int(d) for d in dims)
         self.dims = (nx, ny, nz)
         self.V = nx * ny * nz
@@ -81,6 +81,7 @@ class Omni3D:
         P.tile_width = int(tile_width)
         P.dir_group = int(dir_group)
         P.autotune = int(bool(autotune))
+        P.deterministic = int(bool(deterministic))
         self.params = P
         self.method = method
         self.solve_count = 0
