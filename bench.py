@@ -53,7 +53,7 @@ FLT_MAX = float(np.finfo(np.float32).max)
 # component read (3 x 4 B), the curl read (4 B) and the accumulator read + write (8 B); with
 # BF16 storage one 8-byte record holds the three components and the curl
 ALG_BYTES_PER_UNIT = {"f32": 24.0, "bf16": 16.0}
-PROFILE_SUMMARY = os.path.join(REPO, "profiles", "k_sweep_select_k_anchor_select_blobs192.md")
+PROFILE_SUMMARY = os.path.join(REPO, "profiles", "k_sweep_select_k_anchor_select_blobs128.md")
 
 
 def measured_traffic(workload, grad, engine):
