@@ -115,7 +115,7 @@ typedef struct {
     int sweep_fp64;            /* 1: full sweeps accumulate (pn, count) in FP64 and normalise in
                                   FP64 -- for the anchor solver its one final sweep, a
                                   defect-correction step from the FP32 iteration; for the sweep
-                                  solver every sweep.  Line integrals stay FP32 Kahan sums. */
+                                  solver every sweep.  Line integrals stay FP32 sums. */
     int tile_width;            /* line order: a warp walks the lines of one direction through a
                                   tile of 32 lattice points, tile_width (4, 8 or 16) wide;
                                   0: 8 */

@@ -21,6 +21,11 @@
 // of the curl in .w of the FP32 field, curl being non-negative; bit 31 of the BF16 entry's
 // second word), so a step costs one gather instead of a gather and a bitmap load.  A field
 // with a negative curl value keeps the bitmap.
+//
+// The filling pass sums each line's integral in plain FP32 in step order, as the reference
+// does (K:1816-1834); the final sweep, whose integrals reach every voxel directly, keeps
+// compensated sums.  The filling pass is bound by instruction issue, and the three
+// additions of the compensation took 2.7 ms of its 52.7 ms at 256^3 / 642 directions.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -181,11 +186,11 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_plain(Grid g, const
     const uint32_t ecol = start_col<PASS>(S, e);
     if (SELF) emit_w<PASS, true>(S, e, ecol, 1.0f, 0.0f, is_anchor(S.bits, e));
     float4 gl = load_grad<BF16>(f32, b16, e);
-    float I = 0.0f, comp = 0.0f;
+    float I = 0.0f;
     // the field (and without FB the anchor bitmap word) of every voxel gathered in batches
     walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, !FB>(
         L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, uint32_t v, const float4 &gv, uint32_t word) {
-            kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
+            I += sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z));
             gl = gv;
             emit_w<PASS, true>(S, v, ecol, 1.0f, I, anchor_of<FB>(gv, word, v));
         });
@@ -210,11 +215,11 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_weighted(Grid g, co
     const uint32_t e = r.e;
     const uint32_t ecol = start_col<PASS>(S, e);
     float4 gl = load_grad<BF16>(f32, b16, e);
-    float I = 0.0f, comp = 0.0f, csum = 0.0f, nseg = 0.0f;
+    float I = 0.0f, csum = 0.0f, nseg = 0.0f;
     walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, !FB>(
         L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, uint32_t v, const float4 &gv, uint32_t word) {
             float cn = curl_of<FB>(gv);
-            kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
+            I += sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z));
             csum += __fdiv_rn(cn, 1.0e4f);  // the weights as in k_sweep_weighted
             nseg += 1.0f;
             if (csum != 0.0f) emit_w<PASS, false>(S, v, ecol, __fdividef(nseg, csum), I, anchor_of<FB>(gv, word, v));
@@ -243,11 +248,11 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_weighted_raw(Grid g
     float4 gl = load_grad<BF16>(f32, b16, e);
     float csum = curl_of<FB>(gl), nseg = 1.0f;
     emit_w<PASS, false>(S, e, ecol, __frcp_rn(csum), 0.0f, FB ? anchor_of<FB>(gl, 0u, e) : is_anchor(S.bits, e));
-    float I = 0.0f, comp = 0.0f;
+    float I = 0.0f;
     walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, !FB>(
         L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, uint32_t v, const float4 &gv, uint32_t word) {
             float cn = curl_of<FB>(gv);
-            kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
+            I += sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z));
             csum += cn;
             nseg += 1.0f;
             emit_w<PASS, false>(S, v, ecol, __fdividef(nseg, csum), I, anchor_of<FB>(gv, word, v));
@@ -282,7 +287,7 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_select(Grid g, cons
     uint32_t start = L.v;
     if (PASS == kMark && started) S.flag[start] = 1;
     uint32_t scol = started ? start_col<PASS>(S, start) : 0u;
-    float I = 0.0f, comp = 0.0f, csum = 0.0f, nseg = 0.0f;
+    float I = 0.0f, csum = 0.0f, nseg = 0.0f;
     // the filling pass gathers the field (and without FB the anchor bitmap word) of every
     // voxel in batches
     constexpr int kGrad = PASS == kFill ? (BF16 ? kGradBF16 : kGradF32) : kNoGrad;
@@ -296,13 +301,13 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_select(Grid g, cons
                     if (PASS == kMark) S.flag[start] = 1;
                     scol = start_col<PASS>(S, start);
                     started = true;
-                    I = 0.0f; comp = 0.0f; nseg = 0.0f; csum = 0.0f;
+                    I = 0.0f; nseg = 0.0f; csum = 0.0f;
                 }
             } else {
                 bool good = cn < thr && cn != 0.0f;
                 if (!paused && good) {
                     if (PASS == kFill)
-                        kahan_add(I, comp, sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z)));
+                        I += sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z));
                     csum += cn * 1.0e-4f;  // the weights as in k_sweep_select
                     nseg += 1.0f;
                     if (PASS == kFill)
@@ -314,7 +319,7 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_select(Grid g, cons
                     start = v;
                     if (PASS == kMark) S.flag[start] = 1;
                     scol = start_col<PASS>(S, start);
-                    I = 0.0f; comp = 0.0f;
+                    I = 0.0f;
                     paused = false;
                     if (a != 2) { nseg = 0.0f; csum = 0.0f; }
                 }
