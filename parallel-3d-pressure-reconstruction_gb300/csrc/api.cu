@@ -381,7 +381,7 @@ cudaError_t enqueue_prepared(omni3d_ctx *ctx, const float *dax, const float *day
         dpinit = ctx->in_pinit.as<float>();
     }
     Anchor &A = ctx->anc;
-    if ((e = anchor_refresh_rhs(ctx->geo, F, bf16, &A, st)) != cudaSuccess) return e;
+    if ((e = anchor_refresh_rhs(ctx->geo, F, &A, st)) != cudaSuccess) return e;
     if ((e = anchor_gather(A, dpinit, A.pa, st)) != cudaSuccess) return e;
     const int K = P.max_iter;
     const bool seed = P.seed_first_iteration != 0;
@@ -975,7 +975,7 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
         std::string aerr;
         cudaError_t e;
         if (P.method == OMNI3D_METHOD_PLAIN && ctx->anc_cached) {
-            e = anchor_refresh_rhs(ctx->geo, F, bf16, &ctx->anc, st, fx);
+            e = anchor_refresh_rhs(ctx->geo, F, &ctx->anc, st, fx);
             aerr = cudaGetErrorString(e);
         } else {
             ctx->anc_cached = false;
@@ -985,7 +985,7 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
                 cudaMemGetInfo(&fr, &tot);
                 max_links = (long long)(0.8 * (double)fr / 8.0);
             }
-            e = anchor_build(ctx->geo, F, P.method, bf16, P.gauge == OMNI3D_GAUGE_POINT ? ref : -1, max_links,
+            e = anchor_build(ctx->geo, F, P.method, P.gauge == OMNI3D_GAUGE_POINT ? ref : -1, max_links,
                              &ctx->anc, st, &aerr, fx);
             ctx->anc_cached = e == cudaSuccess && P.method == OMNI3D_METHOD_PLAIN;
             adjoint_free(&ctx->adj);
@@ -1017,7 +1017,7 @@ int omni3d_solve(omni3d_ctx *ctx, const float *ax, const float *ay, const float 
             CK(ctx, ctx->flags.ensure((size_t)V + 64));
             amask = ctx->flags.as<uint8_t>();
             unsigned long long *cnt1 = reinterpret_cast<unsigned long long *>(amask + ((V + 7) / 8) * 8);
-            CK(ctx, anchor_mark(ctx->geo, F, P.method, bf16, P.gauge == OMNI3D_GAUGE_POINT ? ref : -1, amask, cnt1,
+            CK(ctx, anchor_mark(ctx->geo, F, P.method, P.gauge == OMNI3D_GAUGE_POINT ? ref : -1, amask, cnt1,
                                 st));
         }
         cudaEventRecord(ctx->ev[1], st);
@@ -1202,7 +1202,7 @@ int omni3d_adjoint(omni3d_ctx *ctx, const float *grad_p, float *grad_ax, float *
             F.curl = ctx->curl.as<float>();
         }
         std::string aerr;
-        cudaError_t e = anchor_build(ctx->geo, F, P.method, F.bf16 != nullptr, P.gauge == OMNI3D_GAUGE_POINT ? ref : -1,
+        cudaError_t e = anchor_build(ctx->geo, F, P.method, P.gauge == OMNI3D_GAUGE_POINT ? ref : -1,
                                      -1, &ctx->anc, st, &aerr);
         if (e != cudaSuccess) return fail(ctx, OMNI3D_ERR_CUDA, "anchor operator: " + aerr);
         ctx->anc_cached = plain;

@@ -18,16 +18,16 @@
 // (column = start anchor, weight) pairs and accumulates b and c.  The filling pass learns
 // whether a visited voxel is an anchor from the field gather itself: for the duration of
 // the pass the anchors' packed field entries carry a flag in a bit no value uses (the sign
-// of the curl in .w of the FP32 field, curl being non-negative; bit 31 of the BF16 entry's
-// second word), so a step costs one gather instead of a gather and a bitmap load.  A field
-// with a negative curl value keeps the bitmap.
+// of the curl in .w, curl being non-negative), so a step costs one gather instead of a
+// gather and a bitmap load.  A field with a negative curl value keeps the bitmap.  The
+// operator passes read the float4 entries, which with BF16 storage hold the stored values
+// (k_pack): they are bound by instruction issue, not by their gathers, and so read nothing
+// that needs unpacking.
 //
 // The filling pass sums each line's integral in plain FP32 in step order, as the reference
 // does (K:1816-1834); the final sweep, whose integrals reach every voxel directly, keeps
 // compensated sums.  The filling pass is bound by instruction issue, and the three
 // additions of the compensation took 2.7 ms of its 52.7 ms at 256^3 / 642 directions.
-#include <cuda_bf16.h>
-
 #include <algorithm>
 
 #include "fixed.cuh"
@@ -44,16 +44,6 @@ constexpr int kWalkBatch = 4;  // steps whose gathers a walk issues together (wa
 constexpr int kFillBlocks = 5;
 
 namespace {
-
-__device__ __forceinline__ float bf_lo(uint32_t u) { return __uint_as_float(u << 16); }
-__device__ __forceinline__ float bf_hi(uint32_t u) { return __uint_as_float(u & 0xffff0000u); }
-
-template <bool BF16>
-__device__ __forceinline__ float4 load_grad(const float4 *f32, const uint2 *b16, long long v)
-{
-    if (BF16) return load_grad_b16(b16, v);
-    return __ldg(f32 + v);
-}
 
 // Anchor flag of a gathered voxel: with FB the sign bit of its .w (the flag the filling
 // pass sets in the field), else its bit of the bitmap word gathered beside it.
@@ -175,12 +165,11 @@ __device__ __forceinline__ float step_term(int a, const Walk &L, const float4 &g
 
 // Plain method: anchors are the entries; every voxel of a line takes (p[entry] + I, 1).
 // SELF = false leaves the entry's own term out (the minimum-curl plain variant).
-template <int PASS, bool BF16, bool SELF, bool FB>
+template <int PASS, bool SELF, bool FB>
 __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_plain(Grid g, const LineRec *__restrict__ lines,
                                                       const uint32_t *__restrict__ gbase,
                                                       const uint32_t *__restrict__ desc, long long n_lines,
-                                                      const float4 *__restrict__ f32,
-                                                      const uint2 *__restrict__ b16, Sink S)
+                                                      const float4 *__restrict__ f32, Sink S)
 {
     long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (li >= n_lines) return;
@@ -194,11 +183,11 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_plain(Grid g, const
     const uint32_t e = r.e;
     const uint32_t ecol = start_col<PASS>(S, e);
     if (SELF) emit_w<PASS, true>(S, e, ecol, 1.0f, 0.0f, is_anchor(S.bits, e));
-    float4 gl = load_grad<BF16>(f32, b16, e);
+    float4 gl = __ldg(f32 + e);
     float I = 0.0f;
     // the field (and without FB the anchor bitmap word) of every voxel gathered in batches
-    walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, !FB>(
-        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, uint32_t v, const float4 &gv, uint32_t word) {
+    walk_steps<kWalkBatch, kGradF32, !FB>(
+        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, nullptr, S.bits, [&](int a, uint32_t v, const float4 &gv, uint32_t word) {
             I += step_term(a, L, gv, gl);
             gl = gv;
             emit_w<PASS, true>(S, v, ecol, 1.0f, I, anchor_of<FB>(gv, word, v));
@@ -207,12 +196,11 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_plain(Grid g, const
 
 // Weighted method: the walk of k_sweep_weighted (K:1993-2135); anchors are the entries
 // (the marking pass is the plain method's), the entry itself receives nothing.
-template <int PASS, bool BF16, bool FB>
+template <int PASS, bool FB>
 __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_weighted(Grid g, const LineRec *__restrict__ lines,
                                                          const uint32_t *__restrict__ gbase,
                                                          const uint32_t *__restrict__ desc, long long n_lines,
                                                          const float4 *__restrict__ f32,
-                                                         const uint2 *__restrict__ b16,
                                                          const float *__restrict__ curl, Sink S)
 {
     static_assert(PASS == kFill, "the weighted operator has only a filling pass");
@@ -223,10 +211,10 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_weighted(Grid g, co
     L.init(g, r, gbase, desc, li);
     const uint32_t e = r.e;
     const uint32_t ecol = start_col<PASS>(S, e);
-    float4 gl = load_grad<BF16>(f32, b16, e);
+    float4 gl = __ldg(f32 + e);
     float I = 0.0f, csum = 0.0f, nseg = 0.0f;
-    walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, !FB>(
-        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, uint32_t v, const float4 &gv, uint32_t word) {
+    walk_steps<kWalkBatch, kGradF32, !FB>(
+        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, nullptr, S.bits, [&](int a, uint32_t v, const float4 &gv, uint32_t word) {
             float cn = curl_of<FB>(gv);
             I += step_term(a, L, gv, gl);
             csum += __fdiv_rn(cn, 1.0e4f);  // the weights as in k_sweep_weighted
@@ -238,12 +226,11 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_weighted(Grid g, co
 
 // Weighted method with raw curl sums (the minimum-curl variant): the walk of
 // k_sweep_weighted_raw; anchors are the entries, the entry takes its own term.
-template <int PASS, bool BF16, bool FB>
+template <int PASS, bool FB>
 __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_weighted_raw(Grid g, const LineRec *__restrict__ lines,
                                                              const uint32_t *__restrict__ gbase,
                                                              const uint32_t *__restrict__ desc, long long n_lines,
                                                              const float4 *__restrict__ f32,
-                                                             const uint2 *__restrict__ b16,
                                                              const float *__restrict__ curl, Sink S)
 {
     static_assert(PASS == kFill, "the raw-curl weighted operator has only a filling pass");
@@ -254,12 +241,12 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_weighted_raw(Grid g
     L.init(g, r, gbase, desc, li);
     const uint32_t e = r.e;
     const uint32_t ecol = start_col<PASS>(S, e);
-    float4 gl = load_grad<BF16>(f32, b16, e);
+    float4 gl = __ldg(f32 + e);
     float csum = curl_of<FB>(gl), nseg = 1.0f;
     emit_w<PASS, false>(S, e, ecol, __frcp_rn(csum), 0.0f, FB ? anchor_of<FB>(gl, 0u, e) : is_anchor(S.bits, e));
     float I = 0.0f;
-    walk_steps<kWalkBatch, BF16 ? kGradBF16 : kGradF32, !FB>(
-        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, uint32_t v, const float4 &gv, uint32_t word) {
+    walk_steps<kWalkBatch, kGradF32, !FB>(
+        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, nullptr, S.bits, [&](int a, uint32_t v, const float4 &gv, uint32_t word) {
             float cn = curl_of<FB>(gv);
             I += step_term(a, L, gv, gl);
             csum += cn;
@@ -271,12 +258,11 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_weighted_raw(Grid g
 
 // Selected method: the state machine of k_sweep_select (K:2280-2537); anchors are the
 // segment starts.
-template <int PASS, bool BF16, bool FB>
+template <int PASS, bool FB>
 __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_select(Grid g, const LineRec *__restrict__ lines,
                                                        const uint32_t *__restrict__ gbase,
                                                        const uint32_t *__restrict__ desc, long long n_lines,
                                                        const float4 *__restrict__ f32,
-                                                       const uint2 *__restrict__ b16,
                                                        const float *__restrict__ curl, Sink S)
 {
     long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -286,9 +272,8 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_select(Grid g, cons
     L.init(g, r, gbase, desc, li);
     const float thr = g.thr;
     float4 gl = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (PASS == kFill) gl = load_grad<BF16>(f32, b16, L.v);
-    // the field carries curl (.w of the FP32 entry, the high half of the BF16 record's second
-    // word): one gather per step in the filling pass
+    if (PASS == kFill) gl = __ldg(f32 + L.v);
+    // the field carries curl (.w of its entries): one gather per step in the filling pass
     constexpr bool kW = PASS == kFill;
     float ce = kW ? curl_of<FB>(gl) : __ldg(curl + L.v);
     bool started = !(ce == 0.0f || ce > thr);
@@ -299,9 +284,9 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_select(Grid g, cons
     float I = 0.0f, csum = 0.0f, nseg = 0.0f;
     // the filling pass gathers the field (and without FB the anchor bitmap word) of every
     // voxel in batches
-    constexpr int kGrad = PASS == kFill ? (BF16 ? kGradBF16 : kGradF32) : kNoGrad;
+    constexpr int kGrad = PASS == kFill ? kGradF32 : kNoGrad;
     walk_steps<kWalkBatch, kGrad, PASS == kFill && !FB>(
-        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, b16, S.bits, [&](int a, uint32_t v, const float4 &gv, uint32_t word) {
+        L.v, L.d0, L.d1, L.d2, L.m, L.dp, f32, nullptr, S.bits, [&](int a, uint32_t v, const float4 &gv, uint32_t word) {
             const float cn = kW ? curl_of<FB>(gv) : __ldg(curl + v);
             if (!started) {
                 bool ok = (a == 0) ? (cn != 0.0f && cn < thr) : (cn != 0.0f);
@@ -650,25 +635,23 @@ __global__ void k_clear_b(long long n, float2 *bc)
 // anchor flags cleared from the field entries.
 __global__ void k_fill_finish(long long n, const unsigned long long *__restrict__ rowptr,
                               const unsigned long long *__restrict__ next, uint32_t *rowlen, int flags,
-                              const uint32_t *__restrict__ vox, float4 *f32, uint2 *b16)
+                              const uint32_t *__restrict__ vox, float4 *f32)
 {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         rowlen[i] = (uint32_t)(next[i] - rowptr[i]);
         if (flags) {
-            const uint32_t v = vox[i];
-            uint32_t *u = b16 ? &b16[v].y : reinterpret_cast<uint32_t *>(&f32[v].w);
+            uint32_t *u = reinterpret_cast<uint32_t *>(&f32[vox[i]].w);
             *u &= 0x7fffffffu;
         }
     }
 }
 
-// Set (set = 1) or clear the anchor flag in the field entries of the n anchors: bit 31 of
-// the BF16 entry's second word when b16 is given, else the sign bit of the FP32 entry's .w.
-__global__ void k_field_flags(long long n, const uint32_t *__restrict__ vox, float4 *f32, uint2 *b16, int set)
+// Set (set = 1) or clear the anchor flag, the sign bit of .w, in the field entries of the n
+// anchors.
+__global__ void k_field_flags(long long n, const uint32_t *__restrict__ vox, float4 *f32, int set)
 {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const uint32_t v = vox[i];
-        uint32_t *u = b16 ? &b16[v].y : reinterpret_cast<uint32_t *>(&f32[v].w);
+        uint32_t *u = reinterpret_cast<uint32_t *>(&f32[vox[i]].w);
         *u = set ? (*u | 0x80000000u) : (*u & 0x7fffffffu);
     }
 }
@@ -682,52 +665,51 @@ __global__ void k_sign_any(long long V, const float *__restrict__ curl, uint32_t
     if (__any_sync(0xffffffffu, neg) && (threadIdx.x & 31) == 0) *any = 1u;
 }
 
-// Launch the pass for the method's accumulation kind.  BF16: the gradient gathers read the
-// BF16 storage; FB: the anchors are flagged in the field (bitmap otherwise).
-template <int PASS, bool BF16, bool FB>
+// Launch the pass for the method's accumulation kind.  FB: the anchors are flagged in the
+// field (bitmap otherwise).
+template <int PASS, bool FB>
 void launch_pass(int acc, const Geometry &geo, const Field &f, const Sink &S, cudaStream_t st)
 {
     const unsigned blocks = (unsigned)((geo.n_lines + 255) / 256);
     const Grid &g = geo.grid;
     if constexpr (PASS == kFill) {
         if (acc == kAccWeightedRawCurl) {
-            k_anchor_weighted_raw<kFill, BF16, FB><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
-                                                                           geo.n_lines, f.f32, f.bf16, f.curl, S);
+            k_anchor_weighted_raw<kFill, FB><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
+                                                                     geo.n_lines, f.f32, f.curl, S);
             OM_COUNT_LAUNCH();
             return;
         }
         if (acc == kAccWeighted) {
-            k_anchor_weighted<kFill, BF16, FB><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
-                                                                       geo.n_lines, f.f32, f.bf16, f.curl, S);
+            k_anchor_weighted<kFill, FB><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
+                                                                 f.f32, f.curl, S);
             OM_COUNT_LAUNCH();
             return;
         }
         if (acc == kAccPlainNoEntry) {
-            k_anchor_plain<kFill, BF16, false, FB><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
-                                                                           geo.n_lines, f.f32, f.bf16, S);
+            k_anchor_plain<kFill, false, FB><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
+                                                                     geo.n_lines, f.f32, S);
             OM_COUNT_LAUNCH();
             return;
         }
     }
     if constexpr (PASS != kRhs) {
         if (acc == kAccSelect) {
-            k_anchor_select<PASS, BF16, FB><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
-                                                                    geo.n_lines, f.f32, f.bf16, f.curl, S);
+            k_anchor_select<PASS, FB><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
+                                                              f.f32, f.curl, S);
             OM_COUNT_LAUNCH();
             return;
         }
     }
     // plain method, and the marking pass of every method whose anchors are the entries
-    k_anchor_plain<PASS, BF16, true, FB><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
-                                                                 f.f32, f.bf16, S);
+    k_anchor_plain<PASS, true, FB><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
+                                                           f.f32, S);
     OM_COUNT_LAUNCH();
 }
 
-// fb: the anchors' field entries carry the anchor flag (k_field_flags); the BF16 storage
-// always can, the FP32 field when no curl value has its sign bit set.
+// fb: the anchors' field entries carry the anchor flag (k_field_flags): possible when no
+// curl value has its sign bit set.
 template <int PASS>
-cudaError_t run_pass(const Geometry &geo, const Field &f, int method, bool bf16, bool fb, const Sink &S,
-                     cudaStream_t st)
+cudaError_t run_pass(const Geometry &geo, const Field &f, int method, bool fb, const Sink &S, cudaStream_t st)
 {
     if (geo.n_lines == 0) return cudaSuccess;
     // every pointer the pass dereferences must be set: refuse to launch otherwise
@@ -737,17 +719,15 @@ cudaError_t run_pass(const Geometry &geo, const Field &f, int method, bool bf16,
     else ok = ok && S.bits && S.id && S.bc;
     const bool unit_links = method_accum(method) == kAccPlain || method_accum(method) == kAccPlainNoEntry;
     if (PASS == kFill) ok = ok && S.next && (unit_links ? S.col != nullptr : S.cw != nullptr);
-    if (need_field) ok = ok && (bf16 ? f.bf16 != nullptr : f.f32 != nullptr);
+    if (need_field) ok = ok && f.f32 != nullptr;
     const int acc = method_accum(method);
     const bool weighted = acc == kAccWeighted || acc == kAccWeightedRawCurl;
-    if (acc == kAccSelect || (weighted && PASS == kFill)) ok = ok && f.curl && (bf16 || f.f32);
+    if (acc == kAccSelect || (weighted && PASS == kFill)) ok = ok && f.curl && f.f32;
     if (PASS == kRhs && acc != kAccPlain) ok = false;  // only the plain operator is cached
     if (!ok) return cudaErrorInvalidValue;
-    if (PASS == kMark) launch_pass<kMark, false, false>(acc, geo, f, S, st);  // reads no field
-    else if (bf16 && fb) launch_pass<PASS, true, true>(acc, geo, f, S, st);
-    else if (bf16) launch_pass<PASS, true, false>(acc, geo, f, S, st);
-    else if (fb) launch_pass<PASS, false, true>(acc, geo, f, S, st);
-    else launch_pass<PASS, false, false>(acc, geo, f, S, st);
+    if (PASS == kMark) launch_pass<kMark, false>(acc, geo, f, S, st);  // reads no field
+    else if (fb) launch_pass<PASS, true>(acc, geo, f, S, st);
+    else launch_pass<PASS, false>(acc, geo, f, S, st);
     return cudaGetLastError();
 }
 
@@ -787,7 +767,7 @@ void anchor_free(Anchor *A)
     *A = Anchor();
 }
 
-cudaError_t anchor_build(Geometry &geo, const Field &f, int method, bool bf16, long long ref_voxel,
+cudaError_t anchor_build(Geometry &geo, const Field &f, int method, long long ref_voxel,
                          long long max_nnz, Anchor *A, cudaStream_t st, std::string *err, Fixed *fx)
 {
     const long long V = geo.grid.V;
@@ -817,11 +797,11 @@ cudaError_t anchor_build(Geometry &geo, const Field &f, int method, bool bf16, l
     }
     if (!marked) {
         AN_TRY(cudaMemsetAsync(A->flag, 0, (size_t)V, st));
-        AN_TRY(run_pass<kMark>(geo, f, method, bf16, false, S, st));
+        AN_TRY(run_pass<kMark>(geo, f, method, false, S, st));
     }
     if (ref_voxel >= 0 && ref_voxel < V) AN_TRY(cudaMemsetAsync(A->flag + ref_voxel, 1, 1, st));
-    // the field carries curl (FP32 .w, or the BF16 record's high half): its sign bit can flag
-    // the anchors unless a curl value already has it set
+    // the field carries curl in .w: its sign bit can flag the anchors unless a curl value
+    // already has it set
     const bool check_sign = f.curl != nullptr;
     AN_TRY(grow(A->neg, cap[18], sizeof(uint32_t)));
     AN_TRY(cudaMemsetAsync(A->neg, 0, sizeof(uint32_t), st));
@@ -888,15 +868,14 @@ cudaError_t anchor_build(Geometry &geo, const Field &f, int method, bool bf16, l
         S.fix = fx->scale;
     }
     if (fb && n) {
-        k_field_flags<<<grid_for(n), 256, 0, st>>>(n, A->vox, f.f32, bf16 ? f.bf16 : nullptr, 1);
+        k_field_flags<<<grid_for(n), 256, 0, st>>>(n, A->vox, f.f32, 1);
         OM_COUNT_LAUNCH();
         AN_TRY(cudaGetLastError());
     }
-    AN_TRY(run_pass<kFill>(geo, f, method, bf16, fb, S, st));
+    AN_TRY(run_pass<kFill>(geo, f, method, fb, S, st));
     if (fx) AN_TRY(fix_rows_to_float(n, *fx, A->bc, false, st));
     if (n) {  // row lengths; the sweeps read the field unflagged
-        k_fill_finish<<<grid_for(n), 256, 0, st>>>(n, A->rowptr, A->next, A->rowlen, fb ? 1 : 0, A->vox, f.f32,
-                                                    bf16 ? f.bf16 : nullptr);
+        k_fill_finish<<<grid_for(n), 256, 0, st>>>(n, A->rowptr, A->next, A->rowlen, fb ? 1 : 0, A->vox, f.f32);
         OM_COUNT_LAUNCH();
         AN_TRY(cudaGetLastError());
     }
@@ -923,7 +902,7 @@ cudaError_t change_sums(long long n, const float *pc, const float *pn, int gauge
     return cudaGetLastError();
 }
 
-cudaError_t anchor_mark(const Geometry &geo, const Field &f, int method, bool bf16, long long ref_voxel,
+cudaError_t anchor_mark(const Geometry &geo, const Field &f, int method, long long ref_voxel,
                         uint8_t *flag, unsigned long long *count1, cudaStream_t st)
 {
     const long long V = geo.grid.V;
@@ -945,7 +924,7 @@ cudaError_t anchor_mark(const Geometry &geo, const Field &f, int method, bool bf
         if (e != cudaSuccess) return e;
         Sink S{};
         S.flag = flag;
-        e = run_pass<kMark>(geo, f, method, bf16, false, S, st);
+        e = run_pass<kMark>(geo, f, method, false, S, st);
         if (e != cudaSuccess) return e;
     }
     if (ref_voxel >= 0 && ref_voxel < geo.grid.V) e = cudaMemsetAsync(flag + ref_voxel, 1, 1, st);
@@ -990,7 +969,7 @@ cudaError_t converged_test_launch(const double *red2, double tol, int j, int *st
     return cudaGetLastError();
 }
 
-cudaError_t anchor_refresh_rhs(const Geometry &geo, const Field &f, bool bf16, Anchor *A, cudaStream_t st,
+cudaError_t anchor_refresh_rhs(const Geometry &geo, const Field &f, Anchor *A, cudaStream_t st,
                                const Fixed *fx)
 {
     if (A->n == 0) return cudaSuccess;
@@ -1009,15 +988,15 @@ cudaError_t anchor_refresh_rhs(const Geometry &geo, const Field &f, bool bf16, A
         S.fix = fx->scale;
     }
     // the plain method's field carries no curl (.w = +0), so the anchors can be flagged in it
-    const bool fb = bf16 || f.curl == nullptr;
+    const bool fb = f.curl == nullptr;
     if (fb) {
-        k_field_flags<<<grid_for(A->n), 256, 0, st>>>(A->n, A->vox, f.f32, bf16 ? f.bf16 : nullptr, 1);
+        k_field_flags<<<grid_for(A->n), 256, 0, st>>>(A->n, A->vox, f.f32, 1);
         OM_COUNT_LAUNCH();
     }
-    e = run_pass<kRhs>(geo, f, OMNI3D_METHOD_PLAIN, bf16, fb, S, st);
+    e = run_pass<kRhs>(geo, f, OMNI3D_METHOD_PLAIN, fb, S, st);
     if (e == cudaSuccess && fx) e = fix_rows_to_float(A->n, *fx, A->bc, true, st);
     if (e != cudaSuccess || !fb) return e;
-    k_field_flags<<<grid_for(A->n), 256, 0, st>>>(A->n, A->vox, f.f32, bf16 ? f.bf16 : nullptr, 0);
+    k_field_flags<<<grid_for(A->n), 256, 0, st>>>(A->n, A->vox, f.f32, 0);
     OM_COUNT_LAUNCH();
     return cudaGetLastError();
 }

@@ -348,8 +348,11 @@ __device__ __forceinline__ uint32_t curl_bf16(float c, const Grid &g)
 
 // The packed field: float4 (ax, ay, az, curl) and, for BF16 storage, the 8-byte record
 // {ax | ay << 16, az | curl << 16} of round-to-nearest-even BF16 values (the curl by
-// curl_bf16).  With BF16 storage every curl decision must see the stored curl, so the FP32
-// entry's .w and curl_out (which may be the curl array itself) receive it as a float.
+// curl_bf16).  With BF16 storage the FP32 entry holds the stored values as floats, and
+// curl_out (which may be the curl array itself) the stored curl: every pass then sees the
+// same field, the full sweeps gathering the 8-byte records and the anchor operator's filling
+// pass, which is bound by instruction issue rather than by its gathers, the float4 entries
+// (nothing to unpack: 1.8 ms of its 50.9 ms at 256^3 / 642 directions).
 __global__ void k_pack(Grid g, const float *__restrict__ ax, const float *__restrict__ ay,
                        const float *__restrict__ az, const float *curl, float4 *f32, uint2 *b16, float *curl_out)
 {
@@ -359,8 +362,11 @@ __global__ void k_pack(Grid g, const float *__restrict__ ax, const float *__rest
         float x = ax[v], y = ay[v], z = az[v];
         float c = curl ? curl[v] : 0.0f;
         if (b16) {
-            const uint32_t cb = curl_bf16(c, g);
-            b16[v] = make_uint2(to_bf16(x) | (to_bf16(y) << 16), to_bf16(z) | (cb << 16));
+            const uint32_t bx = to_bf16(x), by = to_bf16(y), bz = to_bf16(z), cb = curl_bf16(c, g);
+            b16[v] = make_uint2(bx | (by << 16), bz | (cb << 16));
+            x = __uint_as_float(bx << 16);
+            y = __uint_as_float(by << 16);
+            z = __uint_as_float(bz << 16);
             c = __uint_as_float(cb << 16);
             if (curl_out) curl_out[v] = c;
         }

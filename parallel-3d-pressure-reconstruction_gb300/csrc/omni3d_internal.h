@@ -266,18 +266,19 @@ struct Anchor {
     // same geometry allocates nothing
     size_t cap[20] = {};
 };
-// Builds the operator; returns cudaErrorNotSupported (nothing filled) when it would hold
-// more than max_nnz entries (max_nnz < 0: no limit).
+// Builds the operator from the float4 entries of f (with BF16 storage they hold the stored
+// values); returns cudaErrorNotSupported (nothing filled) when it would hold more than
+// max_nnz entries (max_nnz < 0: no limit).
 // fx (bit-reproducible mode): the rows' (b, c) are summed in fixed point with the scales of
 // fix_fill_scales, which the caller sets before.
-cudaError_t anchor_build(Geometry &geo, const Field &f, int method, bool bf16,
-                         long long ref_voxel, long long max_nnz, Anchor *A, cudaStream_t st,
-                         std::string *err, Fixed *fx = nullptr);
+cudaError_t anchor_build(Geometry &geo, const Field &f, int method, long long ref_voxel,
+                         long long max_nnz, Anchor *A, cudaStream_t st, std::string *err,
+                         Fixed *fx = nullptr);
 void anchor_free(Anchor *A);
 // Plain method: recompute only b (the field-dependent part) of an operator built by
 // anchor_build for the same geometry; rows, columns and c depend on the geometry alone.
-cudaError_t anchor_refresh_rhs(const Geometry &geo, const Field &f, bool bf16, Anchor *A,
-                               cudaStream_t st, const Fixed *fx = nullptr);
+cudaError_t anchor_refresh_rhs(const Geometry &geo, const Field &f, Anchor *A, cudaStream_t st,
+                               const Fixed *fx = nullptr);
 // One iteration p_next = (b + seed * p_init_a + M p_cur) / c; accumulates the gauged
 // change / norm sums into red[0..1] for the relative change.  With stop, every kernel of the
 // step returns at once while *stop != 0 (the gated steps of a graph-captured chunk).
@@ -299,9 +300,8 @@ cudaError_t change_sums(long long n, const float *pc, const float *pn, int gauge
 // Flag the anchor voxels (line entries, or the segment starts of the selected method or a
 // small superset of them, plus ref_voxel when >= 0) into a V-byte array.  count1 is one
 // device word of scratch.
-cudaError_t anchor_mark(const Geometry &geo, const Field &f, int method, bool bf16,
-                        long long ref_voxel, uint8_t *flag, unsigned long long *count1,
-                        cudaStream_t st);
+cudaError_t anchor_mark(const Geometry &geo, const Field &f, int method, long long ref_voxel,
+                        uint8_t *flag, unsigned long long *count1, cudaStream_t st);
 // Scatter anchor values into a volume.
 cudaError_t anchor_scatter(const Anchor &A, const float *pa, float *vol, cudaStream_t st);
 // Gather anchor values from a volume.
