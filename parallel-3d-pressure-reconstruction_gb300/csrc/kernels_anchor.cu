@@ -38,9 +38,9 @@ namespace omni3d {
 
 constexpr int kWalkBatch = 4;  // steps whose gathers a walk issues together (walk.cuh)
 // Resident CTAs of 256 threads per SM for the operator passes: the filling pass waits on its
-// gathers (latency bound), and 5 CTAs (48 registers, a few bytes spilled to L1) beat 4 CTAs
-// (64 registers, no spill): 52.1 against 55.6 ms at 256^3 / 642 directions; 6 CTAs spill
-// more and took 60.8 ms.
+// gathers and issues many instructions per step, and 5 CTAs (48 registers, a few bytes
+// spilled to L1) beat 4 CTAs (64 registers, no spill) and 6 (more spills): 50.0 against
+// 55.1 and 56.2 ms at 256^3 / 642 directions.
 constexpr int kFillBlocks = 5;
 
 namespace {
