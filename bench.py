@@ -521,7 +521,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--deterministic", action="store_true", help="bit-reproducible solves (fixed-point sums)")
     ap.add_argument("--autotune", action="store_true", help="line order picked by the autotuner (default: 8 x 4 "
-                                                              "tiles, 4 directions per group)")
+                                                              "tiles, 32 directions per group up to 2^24 "
+                                                              "voxels, 4 above)")
     ap.add_argument("--profile", action="store_true",
                     help="only the warm-up and timed solves (for ncu): no calibration, e2e, variants or CPU arm")
     ap.add_argument("--no-variants", action="store_true", help="skip timing the sweep-solver and BF16 forms")

@@ -120,7 +120,7 @@ typedef struct {
                                   tile of 32 lattice points, tile_width (4, 8 or 16) wide;
                                   0: 8 */
     int dir_group;             /* line order: neighbouring directions interleaved per tile
-                                  (1-32); 0: 4 */
+                                  (1-32); 0: 32 for grids of up to 2^24 voxels, 4 above */
     int autotune;              /* 1: omni3d_create picks tile_width and dir_group by timing one
                                   sweep of each of a few candidate pairs on this grid and
                                   direction set, and keeps the choice for the process, per
