@@ -37,11 +37,14 @@
 namespace omni3d {
 
 constexpr int kWalkBatch = 4;  // steps whose gathers a walk issues together (walk.cuh)
-// Resident CTAs of 256 threads per SM for the operator passes: the filling pass waits on its
-// gathers and issues many instructions per step, and 5 CTAs (48 registers, a few bytes
-// spilled to L1) beat 4 CTAs (64 registers, no spill) and 6 (more spills): 50.0 against
-// 55.1 and 56.2 ms at 256^3 / 642 directions.
-constexpr int kFillBlocks = 5;
+// Launch shape of the operator passes: the filling pass waits on its gathers and issues many
+// instructions per step, and 40 resident warps per SM (48 registers, a few bytes spilled to
+// L1) beat 32 (64 registers, no spill) and 48 (more spills): with CTAs of 256 threads 50.0
+// against 55.1 and 56.2 ms at 256^3 / 642 directions.  Small CTAs then free their slots as
+// soon as their own few lines end, where a CTA of 8 warps waits for its longest line: 20
+// CTAs of 64 threads took the pass from 46.9 to 44.2 ms (10 of 128: 44.8 ms).
+constexpr int kFillBlocks = 20;
+constexpr int kFillThreads = 64;  // threads per CTA (whole warps: one line per thread)
 
 namespace {
 
@@ -166,7 +169,7 @@ __device__ __forceinline__ float step_term(int a, const Walk &L, const float4 &g
 // Plain method: anchors are the entries; every voxel of a line takes (p[entry] + I, 1).
 // SELF = false leaves the entry's own term out (the minimum-curl plain variant).
 template <int PASS, bool SELF, bool FB>
-__global__ void __launch_bounds__(256, kFillBlocks) k_anchor_plain(Grid g, const LineRec *__restrict__ lines,
+__global__ void __launch_bounds__(kFillThreads, kFillBlocks) k_anchor_plain(Grid g, const LineRec *__restrict__ lines,
                                                       const uint32_t *__restrict__ gbase,
                                                       const uint32_t *__restrict__ desc, long long n_lines,
                                                       const float4 *__restrict__ f32, Sink S)
@@ -197,7 +200,7 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_plain(Grid g, const
 // Weighted method: the walk of k_sweep_weighted (K:1993-2135); anchors are the entries
 // (the marking pass is the plain method's), the entry itself receives nothing.
 template <int PASS, bool FB>
-__global__ void __launch_bounds__(256, kFillBlocks) k_anchor_weighted(Grid g, const LineRec *__restrict__ lines,
+__global__ void __launch_bounds__(kFillThreads, kFillBlocks) k_anchor_weighted(Grid g, const LineRec *__restrict__ lines,
                                                          const uint32_t *__restrict__ gbase,
                                                          const uint32_t *__restrict__ desc, long long n_lines,
                                                          const float4 *__restrict__ f32,
@@ -227,7 +230,7 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_weighted(Grid g, co
 // Weighted method with raw curl sums (the minimum-curl variant): the walk of
 // k_sweep_weighted_raw; anchors are the entries, the entry takes its own term.
 template <int PASS, bool FB>
-__global__ void __launch_bounds__(256, kFillBlocks) k_anchor_weighted_raw(Grid g, const LineRec *__restrict__ lines,
+__global__ void __launch_bounds__(kFillThreads, kFillBlocks) k_anchor_weighted_raw(Grid g, const LineRec *__restrict__ lines,
                                                              const uint32_t *__restrict__ gbase,
                                                              const uint32_t *__restrict__ desc, long long n_lines,
                                                              const float4 *__restrict__ f32,
@@ -259,7 +262,7 @@ __global__ void __launch_bounds__(256, kFillBlocks) k_anchor_weighted_raw(Grid g
 // Selected method: the state machine of k_sweep_select (K:2280-2537); anchors are the
 // segment starts.
 template <int PASS, bool FB>
-__global__ void __launch_bounds__(256, kFillBlocks) k_anchor_select(Grid g, const LineRec *__restrict__ lines,
+__global__ void __launch_bounds__(kFillThreads, kFillBlocks) k_anchor_select(Grid g, const LineRec *__restrict__ lines,
                                                        const uint32_t *__restrict__ gbase,
                                                        const uint32_t *__restrict__ desc, long long n_lines,
                                                        const float4 *__restrict__ f32,
@@ -670,23 +673,23 @@ __global__ void k_sign_any(long long V, const float *__restrict__ curl, uint32_t
 template <int PASS, bool FB>
 void launch_pass(int acc, const Geometry &geo, const Field &f, const Sink &S, cudaStream_t st)
 {
-    const unsigned blocks = (unsigned)((geo.n_lines + 255) / 256);
+    const unsigned blocks = (unsigned)((geo.n_lines + kFillThreads - 1) / kFillThreads);
     const Grid &g = geo.grid;
     if constexpr (PASS == kFill) {
         if (acc == kAccWeightedRawCurl) {
-            k_anchor_weighted_raw<kFill, FB><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
+            k_anchor_weighted_raw<kFill, FB><<<blocks, kFillThreads, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
                                                                      geo.n_lines, f.f32, f.curl, S);
             OM_COUNT_LAUNCH();
             return;
         }
         if (acc == kAccWeighted) {
-            k_anchor_weighted<kFill, FB><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
+            k_anchor_weighted<kFill, FB><<<blocks, kFillThreads, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
                                                                  f.f32, f.curl, S);
             OM_COUNT_LAUNCH();
             return;
         }
         if (acc == kAccPlainNoEntry) {
-            k_anchor_plain<kFill, false, FB><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
+            k_anchor_plain<kFill, false, FB><<<blocks, kFillThreads, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc,
                                                                      geo.n_lines, f.f32, S);
             OM_COUNT_LAUNCH();
             return;
@@ -694,14 +697,14 @@ void launch_pass(int acc, const Geometry &geo, const Field &f, const Sink &S, cu
     }
     if constexpr (PASS != kRhs) {
         if (acc == kAccSelect) {
-            k_anchor_select<PASS, FB><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
+            k_anchor_select<PASS, FB><<<blocks, kFillThreads, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
                                                               f.f32, f.curl, S);
             OM_COUNT_LAUNCH();
             return;
         }
     }
     // plain method, and the marking pass of every method whose anchors are the entries
-    k_anchor_plain<PASS, true, FB><<<blocks, 256, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
+    k_anchor_plain<PASS, true, FB><<<blocks, kFillThreads, 0, st>>>(g, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
                                                            f.f32, S);
     OM_COUNT_LAUNCH();
 }

@@ -23,6 +23,7 @@ namespace omni3d {
 // Steps whose gathers a walk issues together (walk.cuh); the batched kernels run 4 CTAs of
 // 256 threads per SM (64 registers: the batch's gathers stay in registers).
 constexpr int kWalkBatch = 4;
+constexpr int kSweepThreads = 256, kSweepBlocks = 4;  // threads per CTA, CTAs per SM
 
 namespace {
 
@@ -117,7 +118,7 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x)
 // Plain method: every voxel of the line, the entry included, receives p[entry] + I(v).
 // SELF = false leaves the entry out (the minimum-curl plain variant, K:2797-2936).
 template <bool BF16, bool SELF, typename ACC>
-__global__ void __launch_bounds__(256, 4) k_sweep_plain(Grid g, const LineRec *__restrict__ lines,
+__global__ void __launch_bounds__(kSweepThreads, kSweepBlocks) k_sweep_plain(Grid g, const LineRec *__restrict__ lines,
                                                      const uint32_t *__restrict__ gbase,
                                                      const uint32_t *__restrict__ desc, long long n_lines,
                                                      const float4 *__restrict__ f32,
@@ -149,7 +150,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep_plain(Grid g, const LineRec *_
 // nonzero.  Each curl/1e4 term is the reference's correctly rounded float division, so the
 // "sum != 0" decision (all curls so far zero) is the reference's.
 template <bool BF16, typename ACC>
-__global__ void __launch_bounds__(256, 4) k_sweep_weighted(Grid g, const LineRec *__restrict__ lines,
+__global__ void __launch_bounds__(kSweepThreads, kSweepBlocks) k_sweep_weighted(Grid g, const LineRec *__restrict__ lines,
                                                         const uint32_t *__restrict__ gbase,
                                                         const uint32_t *__restrict__ desc, long long n_lines,
                                                         const float4 *__restrict__ f32,
@@ -187,7 +188,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep_weighted(Grid g, const LineRec
 // divided by 1e4) and contributes w (p[entry] + I), w = (s + 1) / C, with no test for a zero
 // sum: a zero sum gives infinities, as in the reference.
 template <bool BF16, typename ACC>
-__global__ void __launch_bounds__(256, 4) k_sweep_weighted_raw(Grid g, const LineRec *__restrict__ lines,
+__global__ void __launch_bounds__(kSweepThreads, kSweepBlocks) k_sweep_weighted_raw(Grid g, const LineRec *__restrict__ lines,
                                                             const uint32_t *__restrict__ gbase,
                                                             const uint32_t *__restrict__ desc, long long n_lines,
                                                             const float4 *__restrict__ f32,
@@ -229,7 +230,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep_weighted_raw(Grid g, const Lin
 // increment); a good voxel after a pause restarts the segment at that voxel; the z
 // branch keeps the running curl/count sums on restart.
 template <bool BF16, typename ACC>
-__global__ void __launch_bounds__(256, 4) k_sweep_select(Grid g, const LineRec *__restrict__ lines,
+__global__ void __launch_bounds__(kSweepThreads, kSweepBlocks) k_sweep_select(Grid g, const LineRec *__restrict__ lines,
                                                       const uint32_t *__restrict__ gbase,
                                                       const uint32_t *__restrict__ desc, long long n_lines,
                                                       const float4 *__restrict__ f32,
@@ -517,46 +518,46 @@ cudaError_t sweep_full_t(const Geometry &geo, const Field &f, int method, bool b
     if (!geo.d_lines || !geo.d_gbase || !geo.d_desc || !p || !pncnt || (bf16 ? !f.bf16 : !f.f32) ||
         (method_uses_curl(method) && !f.curl))
         return cudaErrorInvalidValue;
-    unsigned blocks = (unsigned)((geo.n_lines + 255) / 256);
+    unsigned blocks = (unsigned)((geo.n_lines + kSweepThreads - 1) / kSweepThreads);
     const int acc = method_accum(method);
     if (acc == kAccWeighted) {
         if (bf16)
-            k_sweep_weighted<true, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
+            k_sweep_weighted<true, ACC><<<blocks, kSweepThreads, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
                                                            geo.n_lines, f.f32, f.bf16, f.curl, p, pncnt, fix);
         else
-            k_sweep_weighted<false, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
+            k_sweep_weighted<false, ACC><<<blocks, kSweepThreads, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
                                                             geo.n_lines, f.f32, f.bf16, f.curl, p, pncnt, fix);
         OM_COUNT_LAUNCH();
     } else if (acc == kAccWeightedRawCurl) {
         if (bf16)
-            k_sweep_weighted_raw<true, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
+            k_sweep_weighted_raw<true, ACC><<<blocks, kSweepThreads, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
                                                                geo.n_lines, f.f32, f.bf16, f.curl, p, pncnt, fix);
         else
-            k_sweep_weighted_raw<false, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
+            k_sweep_weighted_raw<false, ACC><<<blocks, kSweepThreads, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
                                                                 geo.n_lines, f.f32, f.bf16, f.curl, p, pncnt, fix);
         OM_COUNT_LAUNCH();
     } else if (acc == kAccSelect) {
         if (bf16)
-            k_sweep_select<true, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
+            k_sweep_select<true, ACC><<<blocks, kSweepThreads, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
                                                          f.f32, f.bf16, f.curl, p, pncnt, fix);
         else
-            k_sweep_select<false, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
+            k_sweep_select<false, ACC><<<blocks, kSweepThreads, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc, geo.n_lines,
                                                           f.f32, f.bf16, f.curl, p, pncnt, fix);
         OM_COUNT_LAUNCH();
     } else if (acc == kAccPlainNoEntry) {
         if (bf16)
-            k_sweep_plain<true, false, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
+            k_sweep_plain<true, false, ACC><<<blocks, kSweepThreads, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
                                                                geo.n_lines, f.f32, f.bf16, p, pncnt, fix);
         else
-            k_sweep_plain<false, false, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
+            k_sweep_plain<false, false, ACC><<<blocks, kSweepThreads, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
                                                                 geo.n_lines, f.f32, f.bf16, p, pncnt, fix);
         OM_COUNT_LAUNCH();
     } else {
         if (bf16)
-            k_sweep_plain<true, true, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
+            k_sweep_plain<true, true, ACC><<<blocks, kSweepThreads, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
                                                               geo.n_lines, f.f32, f.bf16, p, pncnt, fix);
         else
-            k_sweep_plain<false, true, ACC><<<blocks, 256, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
+            k_sweep_plain<false, true, ACC><<<blocks, kSweepThreads, 0, st>>>(geo.grid, geo.d_lines, geo.d_gbase, geo.d_desc,
                                                                geo.n_lines, f.f32, f.bf16, p, pncnt, fix);
         OM_COUNT_LAUNCH();
     }
