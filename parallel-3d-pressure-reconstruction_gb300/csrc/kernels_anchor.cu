@@ -171,10 +171,11 @@ __device__ __forceinline__ float step_term(int a, const Walk &L, const float4 &g
 // Plain method: anchors are the entries; every voxel of a line takes (p[entry] + I, 1).
 // SELF = false leaves the entry's own term out (the minimum-curl plain variant).
 template <int PASS, bool SELF, bool FB>
-__global__ void __launch_bounds__(kFillThreads, kFillBlocks) k_anchor_plain(Grid g, const LineRec *__restrict__ lines,
-                                                      const uint32_t *__restrict__ gbase,
-                                                      const uint32_t *__restrict__ desc, long long n_lines,
-                                                      const float4 *__restrict__ f32, Sink S)
+__global__ void __launch_bounds__(kFillThreads, kFillBlocks)
+k_anchor_plain(Grid g, const LineRec *__restrict__ lines,
+               const uint32_t *__restrict__ gbase,
+               const uint32_t *__restrict__ desc, long long n_lines,
+               const float4 *__restrict__ f32, Sink S)
 {
     long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (li >= n_lines) return;
@@ -202,11 +203,12 @@ __global__ void __launch_bounds__(kFillThreads, kFillBlocks) k_anchor_plain(Grid
 // Weighted method: the walk of k_sweep_weighted (K:1993-2135); anchors are the entries
 // (the marking pass is the plain method's), the entry itself receives nothing.
 template <int PASS, bool FB>
-__global__ void __launch_bounds__(kFillThreads, kFillBlocks) k_anchor_weighted(Grid g, const LineRec *__restrict__ lines,
-                                                         const uint32_t *__restrict__ gbase,
-                                                         const uint32_t *__restrict__ desc, long long n_lines,
-                                                         const float4 *__restrict__ f32,
-                                                         const float *__restrict__ curl, Sink S)
+__global__ void __launch_bounds__(kFillThreads, kFillBlocks)
+k_anchor_weighted(Grid g, const LineRec *__restrict__ lines,
+                  const uint32_t *__restrict__ gbase,
+                  const uint32_t *__restrict__ desc, long long n_lines,
+                  const float4 *__restrict__ f32,
+                  const float *__restrict__ curl, Sink S)
 {
     static_assert(PASS == kFill, "the weighted operator has only a filling pass");
     long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -232,11 +234,12 @@ __global__ void __launch_bounds__(kFillThreads, kFillBlocks) k_anchor_weighted(G
 // Weighted method with raw curl sums (the minimum-curl variant): the walk of
 // k_sweep_weighted_raw; anchors are the entries, the entry takes its own term.
 template <int PASS, bool FB>
-__global__ void __launch_bounds__(kFillThreads, kFillBlocks) k_anchor_weighted_raw(Grid g, const LineRec *__restrict__ lines,
-                                                             const uint32_t *__restrict__ gbase,
-                                                             const uint32_t *__restrict__ desc, long long n_lines,
-                                                             const float4 *__restrict__ f32,
-                                                             const float *__restrict__ curl, Sink S)
+__global__ void __launch_bounds__(kFillThreads, kFillBlocks)
+k_anchor_weighted_raw(Grid g, const LineRec *__restrict__ lines,
+                      const uint32_t *__restrict__ gbase,
+                      const uint32_t *__restrict__ desc, long long n_lines,
+                      const float4 *__restrict__ f32,
+                      const float *__restrict__ curl, Sink S)
 {
     static_assert(PASS == kFill, "the raw-curl weighted operator has only a filling pass");
     long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -264,11 +267,12 @@ __global__ void __launch_bounds__(kFillThreads, kFillBlocks) k_anchor_weighted_r
 // Selected method: the state machine of k_sweep_select (K:2280-2537); anchors are the
 // segment starts.
 template <int PASS, bool FB>
-__global__ void __launch_bounds__(kFillThreads, kFillBlocks) k_anchor_select(Grid g, const LineRec *__restrict__ lines,
-                                                       const uint32_t *__restrict__ gbase,
-                                                       const uint32_t *__restrict__ desc, long long n_lines,
-                                                       const float4 *__restrict__ f32,
-                                                       const float *__restrict__ curl, Sink S)
+__global__ void __launch_bounds__(kFillThreads, kFillBlocks)
+k_anchor_select(Grid g, const LineRec *__restrict__ lines,
+                const uint32_t *__restrict__ gbase,
+                const uint32_t *__restrict__ desc, long long n_lines,
+                const float4 *__restrict__ f32,
+                const float *__restrict__ curl, Sink S)
 {
     long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (li >= n_lines) return;

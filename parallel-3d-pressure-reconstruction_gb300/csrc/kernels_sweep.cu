@@ -21,7 +21,9 @@
 namespace omni3d {
 
 // Steps whose gathers a walk issues together (walk.cuh); the batched kernels run 4 CTAs of
-// 256 threads per SM (64 registers: the batch's gathers stay in registers).
+// 256 threads per SM (64 registers: the batch's gathers stay in registers).  CTAs of 128 or
+// 64 threads changed nothing (73.7 and 73.9 against 73.8 ms at 256^3 / 642 directions): the
+// full sweep is bound by its scattered reductions.
 constexpr int kWalkBatch = 4;
 constexpr int kSweepThreads = 256, kSweepBlocks = 4;  // threads per CTA, CTAs per SM
 
@@ -118,13 +120,14 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x)
 // Plain method: every voxel of the line, the entry included, receives p[entry] + I(v).
 // SELF = false leaves the entry out (the minimum-curl plain variant, K:2797-2936).
 template <bool BF16, bool SELF, typename ACC>
-__global__ void __launch_bounds__(kSweepThreads, kSweepBlocks) k_sweep_plain(Grid g, const LineRec *__restrict__ lines,
-                                                     const uint32_t *__restrict__ gbase,
-                                                     const uint32_t *__restrict__ desc, long long n_lines,
-                                                     const float4 *__restrict__ f32,
-                                                     const uint2 *__restrict__ b16,
-                                                     const float *__restrict__ p, ACC *pncnt,
-                                                      const double *__restrict__ fix)
+__global__ void __launch_bounds__(kSweepThreads, kSweepBlocks)
+k_sweep_plain(Grid g, const LineRec *__restrict__ lines,
+              const uint32_t *__restrict__ gbase,
+              const uint32_t *__restrict__ desc, long long n_lines,
+              const float4 *__restrict__ f32,
+              const uint2 *__restrict__ b16,
+              const float *__restrict__ p, ACC *pncnt,
+              const double *__restrict__ fix)
 {
     long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (li >= n_lines) return;
@@ -150,14 +153,15 @@ __global__ void __launch_bounds__(kSweepThreads, kSweepBlocks) k_sweep_plain(Gri
 // nonzero.  Each curl/1e4 term is the reference's correctly rounded float division, so the
 // "sum != 0" decision (all curls so far zero) is the reference's.
 template <bool BF16, typename ACC>
-__global__ void __launch_bounds__(kSweepThreads, kSweepBlocks) k_sweep_weighted(Grid g, const LineRec *__restrict__ lines,
-                                                        const uint32_t *__restrict__ gbase,
-                                                        const uint32_t *__restrict__ desc, long long n_lines,
-                                                        const float4 *__restrict__ f32,
-                                                        const uint2 *__restrict__ b16,
-                                                        const float *__restrict__ curl,
-                                                        const float *__restrict__ p, ACC *pncnt,
-                                                      const double *__restrict__ fix)
+__global__ void __launch_bounds__(kSweepThreads, kSweepBlocks)
+k_sweep_weighted(Grid g, const LineRec *__restrict__ lines,
+                 const uint32_t *__restrict__ gbase,
+                 const uint32_t *__restrict__ desc, long long n_lines,
+                 const float4 *__restrict__ f32,
+                 const uint2 *__restrict__ b16,
+                 const float *__restrict__ curl,
+                 const float *__restrict__ p, ACC *pncnt,
+                 const double *__restrict__ fix)
 {
     long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (li >= n_lines) return;
@@ -188,14 +192,15 @@ __global__ void __launch_bounds__(kSweepThreads, kSweepBlocks) k_sweep_weighted(
 // divided by 1e4) and contributes w (p[entry] + I), w = (s + 1) / C, with no test for a zero
 // sum: a zero sum gives infinities, as in the reference.
 template <bool BF16, typename ACC>
-__global__ void __launch_bounds__(kSweepThreads, kSweepBlocks) k_sweep_weighted_raw(Grid g, const LineRec *__restrict__ lines,
-                                                            const uint32_t *__restrict__ gbase,
-                                                            const uint32_t *__restrict__ desc, long long n_lines,
-                                                            const float4 *__restrict__ f32,
-                                                            const uint2 *__restrict__ b16,
-                                                            const float *__restrict__ curl,
-                                                            const float *__restrict__ p, ACC *pncnt,
-                                                      const double *__restrict__ fix)
+__global__ void __launch_bounds__(kSweepThreads, kSweepBlocks)
+k_sweep_weighted_raw(Grid g, const LineRec *__restrict__ lines,
+                     const uint32_t *__restrict__ gbase,
+                     const uint32_t *__restrict__ desc, long long n_lines,
+                     const float4 *__restrict__ f32,
+                     const uint2 *__restrict__ b16,
+                     const float *__restrict__ curl,
+                     const float *__restrict__ p, ACC *pncnt,
+                     const double *__restrict__ fix)
 {
     long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (li >= n_lines) return;
@@ -230,14 +235,15 @@ __global__ void __launch_bounds__(kSweepThreads, kSweepBlocks) k_sweep_weighted_
 // increment); a good voxel after a pause restarts the segment at that voxel; the z
 // branch keeps the running curl/count sums on restart.
 template <bool BF16, typename ACC>
-__global__ void __launch_bounds__(kSweepThreads, kSweepBlocks) k_sweep_select(Grid g, const LineRec *__restrict__ lines,
-                                                      const uint32_t *__restrict__ gbase,
-                                                      const uint32_t *__restrict__ desc, long long n_lines,
-                                                      const float4 *__restrict__ f32,
-                                                      const uint2 *__restrict__ b16,
-                                                      const float *__restrict__ curl,
-                                                      const float *__restrict__ p, ACC *pncnt,
-                                                      const double *__restrict__ fix)
+__global__ void __launch_bounds__(kSweepThreads, kSweepBlocks)
+k_sweep_select(Grid g, const LineRec *__restrict__ lines,
+               const uint32_t *__restrict__ gbase,
+               const uint32_t *__restrict__ desc, long long n_lines,
+               const float4 *__restrict__ f32,
+               const uint2 *__restrict__ b16,
+               const float *__restrict__ curl,
+               const float *__restrict__ p, ACC *pncnt,
+               const double *__restrict__ fix)
 {
     long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (li >= n_lines) return;
