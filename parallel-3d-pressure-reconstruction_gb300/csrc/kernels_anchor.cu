@@ -44,7 +44,8 @@ constexpr int kWalkBatch = 4;
 // L1) beat 32 (64 registers, no spill) and 48 (more spills): with CTAs of 256 threads 50.0
 // against 55.1 and 56.2 ms at 256^3 / 642 directions.  Small CTAs then free their slots as
 // soon as their own few lines end, where a CTA of 8 warps waits for its longest line: 20
-// CTAs of 64 threads took the pass from 46.9 to 44.2 ms (10 of 128: 44.8 ms).
+// CTAs of 64 threads took the pass from 46.9 to 44.2 ms (10 of 128: 44.8 ms; 32 warps
+// without spills, 32 CTAs of 32 threads or 16 of 64: 48.1 ms).
 constexpr int kFillBlocks = 20;
 constexpr int kFillThreads = 64;  // threads per CTA (whole warps: one line per thread)
 
